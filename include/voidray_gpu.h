@@ -1,0 +1,289 @@
+/*
+ * voidray_gpu.h — C ABI of the GB300 (sm_103a) path-tracing backend.
+ *
+ * The library replaces voidray's CPU integrator: the progressive sample loop
+ * `iterative_render` (voidray_renderer/src/render/iterative.rs:11-55), the
+ * recursive estimator `trace_ray` (voidray_renderer/src/core/tracer.rs:9-56)
+ * and the intersection query `SceneAcceleration::hit`
+ * (voidray_renderer/src/core/scene.rs:182-185), plus the colour-management
+ * arithmetic of post_process.glsl / tonemapping.glsl
+ * (voidray_renderer/src/shaders/post_process.glsl:23-49,
+ *  voidray_renderer/src/shaders/tonemapping.glsl:2-40).
+ *
+ * Conventions
+ *  - Every entry point returns a vr_status; VR_OK is 0.  On failure the
+ *    thread-local message is available from vr_last_error().  Nothing aborts
+ *    the process (the reference panics / unwraps instead,
+ *    voidray_renderer/src/render/renderer.rs:104,204).
+ *  - Plain pointers and sizes only.  "host" arguments are CPU memory owned by
+ *    the caller; "_device" variants take CUDA device pointers and an optional
+ *    CUDA stream passed as void* (NULL = the library's per-handle stream).
+ *  - A vr_scene owns its device memory (BVH, triangles, shading data,
+ *    environment, importance-sampling tables).  Calls on different scenes
+ *    may come from different threads; calls on one scene must be serialised
+ *    by the caller, as the reference serialises them on its render thread
+ *    (voidray_renderer/src/render/renderer.rs:47).
+ *  - There is no CPU fallback: without a usable CUDA device every compute
+ *    entry point returns VR_ERR_NO_DEVICE.
+ */
+#ifndef VOIDRAY_GPU_H
+#define VOIDRAY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VR_ABI_VERSION 1
+
+typedef enum vr_status {
+    VR_OK = 0,
+    VR_ERR_INVALID = 1,     /* bad argument / descriptor                          */
+    VR_ERR_UNSUPPORTED = 2, /* feature the GPU path does not cover               */
+    VR_ERR_CUDA = 3,        /* CUDA runtime error                                */
+    VR_ERR_OOM = 4,         /* device allocation failed                          */
+    VR_ERR_STACK = 5,       /* traversal stack overflow detected by a kernel     */
+    VR_ERR_TIMEOUT = 6,     /* a bounded device wait or budget ran out           */
+    VR_ERR_NO_DEVICE = 7,   /* no CUDA device                                    */
+    VR_ERR_CANCELLED = 8    /* job cancelled                                     */
+} vr_status;
+
+/* ---------------------------------------------------------------- scene -- */
+
+/* Material kinds: the closed set of voidray_common materials.
+ * voidray_common/src/simple.rs:15-58 (Materials::*), :60-81 (LambertianBSDF),
+ * voidray_common/src/microfacet.rs:9-101 (MicrofacetBSDF). */
+typedef enum vr_material_kind {
+    VR_MAT_LAMBERTIAN = 0,      /* Materials::lambertian(albedo)                */
+    VR_MAT_METAL = 1,           /* Materials::metal(albedo, fuzz)               */
+    VR_MAT_DIELECTRIC = 2,      /* Materials::dielectric(ir)                    */
+    VR_MAT_EMISSION = 3,        /* Materials::{emissive,colored_emissive}; color
+                                   already multiplied by strength               */
+    VR_MAT_LAMBERTIAN_BSDF = 4, /* Materials::lambertian_bsdf(albedo)           */
+    VR_MAT_MICROFACET = 5       /* MicrofacetBSDF {color,index,roughness,
+                                   metallic,emittance,transparent}              */
+} vr_material_kind;
+
+typedef struct vr_material {
+    int32_t kind;       /* vr_material_kind                                     */
+    float color[3];     /* albedo / emitted radiance / microfacet colour        */
+    float fuzz;         /* metal                                                */
+    float ir;           /* dielectric ior; microfacet index                     */
+    float roughness;    /* microfacet Beckmann m                                */
+    float metallic;     /* microfacet                                           */
+    float emittance;    /* microfacet (stored, unused by its scatter, as in the
+                           reference)                                           */
+    int32_t transparent;/* microfacet                                           */
+} vr_material;
+
+/* One triangle mesh: Mesh::from_buffers (voidray_renderer/src/core/mesh.rs:76-116).
+ * normals == NULL means zero vertex normals, like Vertex::position
+ * (mesh.rs:25-33, used by Surfaces::quad).  uvs == NULL means zero uvs. */
+typedef struct vr_mesh_desc {
+    const float* positions;   /* 3 * num_vertices                              */
+    const float* normals;     /* 3 * num_vertices or NULL                      */
+    const float* uvs;         /* 2 * num_vertices or NULL                      */
+    const uint32_t* indices;  /* 3 * num_triangles                             */
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+    uint32_t material;        /* index into vr_scene_desc.materials            */
+    uint32_t pad_;
+} vr_mesh_desc;
+
+typedef enum vr_env_kind {
+    VR_ENV_NONE = 0,    /* scene.environment == None -> black (tracer.rs:31)   */
+    VR_ENV_UNIFORM = 1, /* Environments::uniform (environments.rs:29-33)       */
+    VR_ENV_HDRI = 2     /* Environments::hdri lat-long RGB f32 (environments.rs:35-90) */
+} vr_env_kind;
+
+typedef struct vr_environment_desc {
+    int32_t kind;         /* vr_env_kind                                        */
+    float color[3];       /* uniform colour                                     */
+    const float* image;   /* HDRI: width*height*3 f32, row 0 first (image crate order) */
+    uint32_t width;
+    uint32_t height;
+    int32_t importance_sample; /* build the 2D CDF used by VR_EST_NEE          */
+    int32_t pad_;
+} vr_environment_desc;
+
+/* Camera (voidray_renderer/src/core/camera.rs:7-22).  direction and up as the
+ * reference stores them after Camera::look_at (unit, orthogonal). */
+typedef struct vr_camera_desc {
+    float eye[3];
+    float direction[3];
+    float up[3];
+    float fov;            /* radians, on the longer image axis                  */
+    int32_t has_dof;
+    float aperture;
+    float focal_point[3];
+} vr_camera_desc;
+
+typedef struct vr_scene_desc {
+    const vr_mesh_desc* meshes;
+    uint32_t num_meshes;
+    uint32_t num_materials;
+    const vr_material* materials;
+    vr_environment_desc environment;
+    vr_camera_desc camera;
+    uint32_t bvh_max_leaf;  /* 0 = default (4)                                  */
+    uint32_t bvh_bins;      /* 0 = default (16)                                 */
+} vr_scene_desc;
+
+typedef struct vr_scene vr_scene;
+
+/* Builds the scene: binned-SAH BVH2 on the host, flattened to 64-byte nodes and
+ * 48-byte triangles (16-byte aligned), uploaded to the current CUDA device.
+ * Replaces Scene::build_acceleration (voidray_renderer/src/core/scene.rs:163-178). */
+vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out);
+vr_status vr_scene_destroy(vr_scene* scene);
+
+typedef struct vr_scene_info {
+    uint64_t num_triangles;
+    uint64_t num_nodes;
+    uint64_t device_bytes;   /* all device memory held by the scene           */
+    uint32_t max_depth;
+    uint32_t max_leaf;
+    double sah_cost;
+    double build_ms;
+} vr_scene_info;
+vr_status vr_scene_info_get(const vr_scene* scene, vr_scene_info* info);
+
+/* Host-only structural check, usable without a GPU: lowers the descriptor,
+ * builds and flattens the BVH and verifies its invariants (every triangle in
+ * exactly one leaf, every child box encloses its subtree, depth within the
+ * traversal stack).  Fills info (device_bytes = bytes the scene would hold). */
+vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info);
+
+/* Replace the camera of a built scene (the GUI edits Scene.camera between renders). */
+vr_status vr_scene_set_camera(vr_scene* scene, const vr_camera_desc* camera);
+
+/* ------------------------------------------------------------ settings -- */
+
+/* RenderMode (voidray_renderer/src/core/settings.rs:8-12): Normal = 0, Full = 1. */
+typedef enum vr_render_mode { VR_MODE_NORMAL = 0, VR_MODE_FULL = 1 } vr_render_mode;
+
+/* Estimator.  VR_EST_REFERENCE reproduces trace_ray_internal exactly
+ * (tracer.rs:19-56: per-level firefly clamp, miss -> environment).
+ * VR_EST_NEE is the production estimator (no reference counterpart):
+ * forward throughput, environment importance sampling with shadow rays and
+ * MIS at Lambertian vertices, per-contribution clamp. */
+typedef enum vr_estimator { VR_EST_REFERENCE = 0, VR_EST_NEE = 1 } vr_estimator;
+
+/* RenderSettings (settings.rs:15-34) plus the GPU-only knobs. */
+typedef struct vr_render_settings {
+    uint32_t total_samples;   /* divides the accumulated sum (iterative.rs:45)  */
+    float update_frequency;   /* render-thread chunking (renderer.rs:78); unused by vr_render */
+    int32_t render_mode;      /* vr_render_mode                                 */
+    float firefly_clamp;      /* Color::clamp(max) per level (tracer.rs:50)     */
+    uint32_t max_bounces;
+    int32_t estimator;        /* vr_estimator                                   */
+    uint32_t rr_depth;        /* Russian roulette from this depth; 0 = off      */
+    uint32_t wavefront_paths; /* paths per wavefront; 0 = autotuned default     */
+} vr_render_settings;
+
+/* Tonemap (settings.rs:36-55): None=0, ACES=1, Reinhard=2, Filmic=3, Uncharted2=4. */
+typedef struct vr_color_management {
+    int32_t tonemap;
+    float gamma;
+    float exposure;
+    int32_t transparent;
+} vr_color_management;
+
+/* ------------------------------------------------------------- render -- */
+
+/* iterative_render (voidray_renderer/src/render/iterative.rs:11-55):
+ * for every pixel, sums `samples` jittered paths, scales by
+ * 1/settings.total_samples and adds the result to rgba (RGBA f32, row-major,
+ * width*height*4); alpha gains 1.0 per call as Color::a() returns 1
+ * (voidray_renderer/src/util/color.rs:54-56).  Sample s of pixel p draws from
+ * the PCG32 stream (seed, first_sample + s, p), so successive calls with
+ * advancing first_sample continue one progressive render.
+ * The row of pixel index i is i / width (the reference's i / height,
+ * iterative.rs:26, is only correct for square images). */
+vr_status vr_render(vr_scene* scene, const vr_render_settings* settings,
+                    uint32_t samples, float* rgba, uint32_t width,
+                    uint32_t height, uint64_t seed, uint32_t first_sample);
+/* Same, rgba is device memory; runs on `stream` (NULL = scene stream). */
+vr_status vr_render_device(vr_scene* scene, const vr_render_settings* settings,
+                           uint32_t samples, float* rgba_device, uint32_t width,
+                           uint32_t height, uint64_t seed, uint32_t first_sample,
+                           void* stream);
+
+typedef struct vr_render_stats {
+    uint64_t paths;          /* camera paths traced                            */
+    uint64_t extend_rays;    /* closest-hit rays                               */
+    uint64_t shadow_rays;    /* any-hit rays                                   */
+    uint64_t wavefronts;
+    double ms;               /* wall time of the last render call             */
+    uint32_t error_flags;    /* device status word (VR_ERR_STACK etc.)        */
+    uint32_t pad_;
+} vr_render_stats;
+vr_status vr_render_stats_get(const vr_scene* scene, vr_render_stats* stats);
+
+/* post_process.glsl:23-49: out = pow(tonemap(rgb * scale * 2^exposure), 1/gamma), a = 1. */
+vr_status vr_tonemap(const float* rgba_in, float* rgba_out, uint32_t width,
+                     uint32_t height, const vr_color_management* cm, float scale);
+vr_status vr_tonemap_device(const float* rgba_in_device, float* rgba_out_device,
+                            uint32_t width, uint32_t height,
+                            const vr_color_management* cm, float scale, void* stream);
+
+/* relative MSE over RGB: mean((x-r)^2/(r^2+eps)), eps = 1e-2; each image is
+ * RGBA f32 scaled by its own factor first. */
+vr_status vr_relmse_device(const float* rgba_device, float scale,
+                           const float* ref_rgba_device, float ref_scale,
+                           uint32_t width, uint32_t height, double* out, void* stream);
+
+/* ---------------------------------------------------------- intersect -- */
+
+/* A ray: origin, tmin, direction, tmax (32 bytes).  The triangle test rejects
+ * |det| < tmin, as Triangle::hit does with its t_min argument
+ * (voidray_renderer/src/core/mesh.rs:156). */
+typedef struct vr_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} vr_ray;
+
+/* Closest (or any) hit: triangle id in mesh-concatenation order, t and the
+ * barycentrics (u weights vertex 1, v weights vertex 2, as mesh.rs:176-178).
+ * prim == VR_MISS for no hit. */
+#define VR_MISS 0xFFFFFFFFu
+typedef struct vr_hit {
+    uint32_t prim;
+    float t;
+    float u;
+    float v;
+} vr_hit;
+
+/* SceneAcceleration::hit over a batch of rays (host memory). any_hit != 0
+ * returns any intersection in (tmin, tmax) instead of the closest. */
+vr_status vr_intersect(vr_scene* scene, const vr_ray* rays, uint64_t count,
+                       vr_hit* hits, int32_t any_hit);
+vr_status vr_intersect_device(vr_scene* scene, const vr_ray* rays_device,
+                              uint64_t count, vr_hit* hits_device,
+                              int32_t any_hit, void* stream);
+
+/* Traversal work counters for the same rays and kernels (inner-node visits,
+ * triangle tests), used to state the algorithmic bytes of a launch. */
+vr_status vr_intersect_count_device(vr_scene* scene, const vr_ray* rays_device,
+                                    uint64_t count, int32_t any_hit,
+                                    uint64_t* node_visits, uint64_t* tri_tests,
+                                    void* stream);
+
+/* --------------------------------------------------------------- misc -- */
+
+const char* vr_last_error(void);
+int32_t vr_abi_version(void);
+/* 1 if a CUDA device is usable, 0 otherwise (never fails). */
+int32_t vr_device_available(void);
+/* Device synchronisation of the scene stream. */
+vr_status vr_scene_synchronize(vr_scene* scene);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOIDRAY_GPU_H */

@@ -1,0 +1,112 @@
+"""The C-ABI library loads, exports every symbol include/voidray_gpu.h declares,
+and its host-side logic (scene lowering, SAH BVH build, flattening) holds its
+invariants.  No GPU: nothing here launches a kernel."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import voidray_gb300 as vr
+from voidray_gb300 import workloads as W
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "voidray_gpu.h"
+
+
+def declared():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(vr_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(native):
+    lib = native.lib()
+    names = declared()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(native.EXPORTED)
+    assert lib.vr_abi_version() == 1
+
+
+def test_no_device_is_an_error_not_a_fallback(native):
+    if native.lib().vr_device_available():
+        pytest.skip("a CUDA device is present")
+    scene, _ = W.cornell_box()
+    with pytest.raises(native.VoidrayError) as e:
+        scene.build_acceleration()
+    assert e.value.status == 7
+
+
+@pytest.mark.parametrize("n,leaf,bins", [(1, 0, 0), (2, 0, 0), (5, 0, 0), (1000, 0, 0), (20000, 0, 0),
+                                         (20000, 8, 32), (5000, 1, 4)])
+def test_bvh_invariants_soup(native, n, leaf, bins):
+    info = W.soup_scene(n, seed=n).validate(bvh_max_leaf=leaf, bvh_bins=bins)
+    assert info.num_triangles == n
+    assert info.max_depth < 64
+    assert 1 <= info.num_nodes <= 2 * n
+
+
+def test_bvh_invariants_degenerate(native):
+    # every triangle identical: centroids coincide, the builder falls back to median splits
+    pos = np.tile(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), (4096, 1))
+    s = vr.Scene()
+    m = s.add_material(vr.Materials.lambertian((0.5, 0.5, 0.5)))
+    s.add_object(m, s.add_mesh(vr.Mesh(pos, np.arange(len(pos)))))
+    info = s.validate()
+    assert info.num_triangles == 4096 and info.max_depth < 64
+
+
+def test_bvh_invariants_cornell_and_icosphere(native):
+    scene, _ = W.cornell_box()
+    assert scene.validate().num_triangles == 36
+    v, t = W.geodesic_sphere(40)
+    s = vr.Scene()
+    m = s.add_material(vr.Materials.lambertian((0.5, 0.5, 0.5)))
+    s.add_object(m, s.add_mesh(vr.Mesh(v, t)))
+    info = s.validate()
+    assert info.num_triangles == 20 * 40 * 40
+
+
+def test_descriptor_errors(native):
+    s = vr.Scene()
+    m = s.add_material(vr.Materials.lambertian((0.5, 0.5, 0.5)))
+    with pytest.raises(vr.VoidrayError):
+        vr.Mesh(np.zeros((3, 3), np.float32), [0, 1, 3])
+    # surface without an object at the same index (the reference panics)
+    s.add_mesh(vr.Mesh(np.eye(3, dtype=np.float32), [0, 1, 2]))
+    with pytest.raises(vr.VoidrayError):
+        s.validate()
+    s.add_object(m + 5, 0)
+    with pytest.raises(vr.VoidrayError):
+        s.validate()
+    with pytest.raises(vr.VoidrayError) as e:
+        s.add_analytic_surface(None)
+    assert e.value.status == 2
+
+
+def test_surface_index_quirk(native):
+    """scene.rs:377: the hit surface index selects the object, so surface s
+    renders with objects[s].material even if that object names another surface."""
+    s = vr.Scene()
+    a = s.add_material(vr.Materials.lambertian((1, 0, 0)))
+    b = s.add_material(vr.Materials.lambertian((0, 1, 0)))
+    s0 = s.add_mesh(vr.Mesh(np.eye(3, dtype=np.float32), [0, 1, 2]))
+    s1 = s.add_mesh(vr.Mesh(np.eye(3, dtype=np.float32) * 2, [0, 1, 2]))
+    s.add_object(b, s1)
+    s.add_object(a, s0)
+    assert s.surface_materials() == [b, a]
+
+
+def test_camera_look_at_f32(native):
+    cam = vr.Camera.look_at((1.0, 0.0, 10.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 0.5)
+    assert cam.direction.dtype == np.float32
+    assert abs(float(np.dot(cam.direction, cam.up))) < 1e-6
+    assert np.isclose(np.linalg.norm(cam.direction), 1.0, atol=1e-6)
+
+
+def test_settings_defaults_match_reference(native):
+    st = vr.RenderSettings()
+    assert (st.total_samples, st.update_frequency, st.render_mode, st.firefly_clamp, st.max_bounces) == \
+           (100, 0.1, vr.RenderMode.Full, 3.0, 10)
+    cm = vr.ColorManagementSettings()
+    assert (cm.tonemap, cm.gamma, cm.exposure, cm.transparent) == (vr.Tonemap.NONE, 2.2, 0.0, True)

@@ -1,0 +1,17 @@
+"""voidray_gb300 — GB300 (sm_103a) wavefront path-tracing backend for voidray.
+
+The compute path is the native library ``_lib/libvoidray_gb300.so`` (C ABI in
+``include/voidray_gpu.h``); this package mirrors voidray_renderer's scene,
+camera, material and settings API on top of it.
+"""
+from ._native import EXPORTED, VR_MISS, VoidrayError, lib
+from .scene import (Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
+                    Materials, Mesh, MicrofacetBSDF, RenderMode, RenderSettings, Scene, SceneAcceleration, Settings,
+                    Surfaces, Tonemap, Vertex, degrees_to_radians, hex_color, iterative_render, tonemap)
+
+__all__ = [
+    "EXPORTED", "VR_MISS", "VoidrayError", "lib", "Camera", "ColorManagementSettings", "CpuRenderTarget",
+    "Environment", "Environments", "Estimator", "Material", "Materials", "Mesh", "MicrofacetBSDF", "RenderMode",
+    "RenderSettings", "Scene", "SceneAcceleration", "Settings", "Surfaces", "Tonemap", "Vertex",
+    "degrees_to_radians", "hex_color", "iterative_render", "tonemap",
+]

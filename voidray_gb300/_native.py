@@ -1,0 +1,137 @@
+"""ctypes binding of ``include/voidray_gpu.h`` (libvoidray_gb300.so).
+
+The library is the only compute path: if it is missing, importing anything
+that renders raises immediately; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libvoidray_gb300.so"
+
+VR_OK = 0
+STATUS_NAMES = {
+    0: "VR_OK", 1: "VR_ERR_INVALID", 2: "VR_ERR_UNSUPPORTED", 3: "VR_ERR_CUDA", 4: "VR_ERR_OOM",
+    5: "VR_ERR_STACK", 6: "VR_ERR_TIMEOUT", 7: "VR_ERR_NO_DEVICE", 8: "VR_ERR_CANCELLED",
+}
+VR_MISS = 0xFFFFFFFF
+
+
+class VoidrayError(RuntimeError):
+    """A non-OK vr_status with the library's message."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class vr_material(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("fuzz", C.c_float), ("ir", C.c_float),
+                ("roughness", C.c_float), ("metallic", C.c_float), ("emittance", C.c_float),
+                ("transparent", C.c_int32)]
+
+
+class vr_mesh_desc(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p), ("indices", C.c_void_p),
+                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32), ("material", C.c_uint32),
+                ("pad_", C.c_uint32)]
+
+
+class vr_environment_desc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("image", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("importance_sample", C.c_int32), ("pad_", C.c_int32)]
+
+
+class vr_camera_desc(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("direction", C.c_float * 3), ("up", C.c_float * 3), ("fov", C.c_float),
+                ("has_dof", C.c_int32), ("aperture", C.c_float), ("focal_point", C.c_float * 3)]
+
+
+class vr_scene_desc(C.Structure):
+    _fields_ = [("meshes", C.c_void_p), ("num_meshes", C.c_uint32), ("num_materials", C.c_uint32),
+                ("materials", C.c_void_p), ("environment", vr_environment_desc), ("camera", vr_camera_desc),
+                ("bvh_max_leaf", C.c_uint32), ("bvh_bins", C.c_uint32)]
+
+
+class vr_scene_info(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint64), ("num_nodes", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("max_depth", C.c_uint32), ("max_leaf", C.c_uint32), ("sah_cost", C.c_double),
+                ("build_ms", C.c_double)]
+
+
+class vr_render_settings(C.Structure):
+    _fields_ = [("total_samples", C.c_uint32), ("update_frequency", C.c_float), ("render_mode", C.c_int32),
+                ("firefly_clamp", C.c_float), ("max_bounces", C.c_uint32), ("estimator", C.c_int32),
+                ("rr_depth", C.c_uint32), ("wavefront_paths", C.c_uint32)]
+
+
+class vr_color_management(C.Structure):
+    _fields_ = [("tonemap", C.c_int32), ("gamma", C.c_float), ("exposure", C.c_float), ("transparent", C.c_int32)]
+
+
+class vr_render_stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("wavefronts", C.c_uint64), ("ms", C.c_double), ("error_flags", C.c_uint32), ("pad_", C.c_uint32)]
+
+
+# every function declared in include/voidray_gpu.h: (name, restype, argtypes)
+P = C.c_void_p
+_SIGS = [
+    ("vr_scene_create", C.c_int, [P, P]),
+    ("vr_scene_destroy", C.c_int, [P]),
+    ("vr_scene_info_get", C.c_int, [P, P]),
+    ("vr_scene_validate", C.c_int, [P, P]),
+    ("vr_scene_set_camera", C.c_int, [P, P]),
+    ("vr_render", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32]),
+    ("vr_render_device", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, P]),
+    ("vr_render_stats_get", C.c_int, [P, P]),
+    ("vr_tonemap", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float]),
+    ("vr_tonemap_device", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float, P]),
+    ("vr_relmse_device", C.c_int, [P, C.c_float, P, C.c_float, C.c_uint32, C.c_uint32, P, P]),
+    ("vr_intersect", C.c_int, [P, P, C.c_uint64, P, C.c_int32]),
+    ("vr_intersect_device", C.c_int, [P, P, C.c_uint64, P, C.c_int32, P]),
+    ("vr_intersect_count_device", C.c_int, [P, P, C.c_uint64, C.c_int32, P, P, P]),
+    ("vr_last_error", C.c_char_p, []),
+    ("vr_abi_version", C.c_int32, []),
+    ("vr_device_available", C.c_int32, []),
+    ("vr_scene_synchronize", C.c_int, [P]),
+]
+EXPORTED = [name for name, _, _ in _SIGS]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads the native library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("VOIDRAY_GB300_LIB", LIB_PATH))
+        if not path.exists():
+            raise VoidrayError(7, f"native library {path} is missing; build it with "
+                                  "`python -c 'import __graft_entry__ as g; g.build()'`")
+        dll = C.CDLL(str(path))
+        for name, res, args in _SIGS:
+            fn = getattr(dll, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = dll
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != VR_OK:
+        msg = lib().vr_last_error()
+        raise VoidrayError(status, msg.decode() if msg else "")
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

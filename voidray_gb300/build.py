@@ -1,0 +1,85 @@
+"""Builds the native library libvoidray_gb300.so for sm_103a, in-tree.
+
+Each translation unit is compiled by nvcc in parallel, then linked into
+``voidray_gb300/_lib/libvoidray_gb300.so`` with the CUDA runtime linked
+statically.  Device code is compiled with ``-fmad=false`` and host code with
+``-ffp-contract=off`` so that every f32 operation on the reference-estimator
+path rounds separately, as the reference computes it.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIBDIR = PKG / "_lib"
+LIB = LIBDIR / "libvoidray_gb300.so"
+
+SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the GPU library cannot be built")
+
+
+def _flags(src: str) -> list[str]:
+    common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
+              "-I", str(CSRC), "-I", str(PKG.parent / "include")]
+    if src.endswith(".cu"):
+        return ARCH + common + ["-fmad=false", "-Xptxas", "-v" if os.environ.get("VR_PTXAS_VERBOSE") else "-O3"]
+    return common + ["-x", "cu"] + ARCH + ["-fmad=false"]
+
+
+def _stale(obj: Path, deps: list[Path]) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "voidray_gpu.h"]
+    procs = []
+    objs = []
+    for src in SOURCES:
+        s = CSRC / src
+        o = BUILD / (src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s, *headers, Path(__file__)]):
+            cmd = [nvcc(), "-c", str(s), "-o", str(o), *_flags(src)]
+            if verbose:
+                print(" ".join(cmd), file=sys.stderr)
+            procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    failed = []
+    for src, p in procs:
+        out, _ = p.communicate()
+        if out and (verbose or p.returncode):
+            print(out, file=sys.stderr)
+        if p.returncode:
+            failed.append(src)
+    if failed:
+        raise RuntimeError(f"nvcc failed for {failed}")
+    if force or procs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    print(LIB)

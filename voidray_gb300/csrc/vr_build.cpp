@@ -1,0 +1,531 @@
+// vr_build.cpp — host-side scene lowering: binned-SAH BVH2 builder,
+// flattening to the 16-byte-aligned node / triangle arrays the traversal
+// kernels read with 128-bit loads, shading records, camera and environment
+// importance-sampling tables.
+//
+// Replaces Scene::build_acceleration (voidray_renderer/src/core/scene.rs:163-178)
+// and the per-mesh BvhNode::from_list (core/bvh.rs:48-130, a median split).
+// The two-level surface/mesh structure of the reference is flattened into one
+// BVH over all triangles, each carrying its mesh's material; closest-hit
+// results do not depend on the tree (only exact ties in t may resolve
+// differently).  Compiled with -ffp-contract=off: face normals and edge
+// vectors round exactly as the reference computes them.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <thread>
+
+#include "vr_host.h"
+
+namespace vr {
+namespace {
+
+struct PrimRef {
+    float lo[3], hi[3], c[3];
+    uint32_t id;
+};
+struct BNode {
+    float lo[3], hi[3];
+    int32_t left = -1, right = -1;  // children (inner) ; -1 for leaves
+    uint32_t first = 0, count = 0;  // leaf range in the prim order
+};
+struct Box {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    void grow(const float* l, const float* h) {
+        for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], l[a]); hi[a] = std::max(hi[a], h[a]); }
+    }
+    void growp(const float* p) { grow(p, p); }
+    double area() const {
+        double dx = (double)hi[0] - lo[0], dy = (double)hi[1] - lo[1], dz = (double)hi[2] - lo[2];
+        if (!(dx >= 0) || !(dy >= 0) || !(dz >= 0)) return 0.0;
+        return 2.0 * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+constexpr int DEPTH_LIMIT = STACK_SIZE - 2;  // keeps the traversal stack in bounds
+constexpr double C_TRAV = 1.0, C_ISECT = 1.0;
+
+struct Builder {
+    std::vector<PrimRef>& refs;
+    uint32_t max_leaf;
+    int nbins;
+    std::vector<BNode> nodes;
+    uint32_t max_depth = 0;
+    Builder(std::vector<PrimRef>& r, uint32_t ml, int nb) : refs(r), max_leaf(ml), nbins(nb) {}
+
+    static int ceil_log2(uint64_t n) {
+        int k = 0;
+        while ((1ull << k) < n) ++k;
+        return k;
+    }
+
+    int make_leaf(uint32_t b, uint32_t e, const Box& bx) {
+        BNode n;
+        std::memcpy(n.lo, bx.lo, sizeof n.lo);
+        std::memcpy(n.hi, bx.hi, sizeof n.hi);
+        n.first = b;
+        n.count = e - b;
+        nodes.push_back(n);
+        return (int)nodes.size() - 1;
+    }
+
+    // Builds [b, e) and returns its node index.
+    int build(uint32_t b, uint32_t e, int depth) {
+        max_depth = std::max<uint32_t>(max_depth, (uint32_t)depth);
+        Box bx, cb;
+        for (uint32_t i = b; i < e; ++i) { bx.grow(refs[i].lo, refs[i].hi); cb.growp(refs[i].c); }
+        const uint32_t n = e - b;
+        if (n == 1) return make_leaf(b, e, bx);
+        const bool force_median = depth + ceil_log2((n + max_leaf - 1) / max_leaf) + 1 >= DEPTH_LIMIT;
+        if (force_median && n <= max_leaf) return make_leaf(b, e, bx);
+        int best_axis = -1, best_bin = -1;
+        double best_cost = INFINITY;
+        const double parent_area = bx.area();
+        if (!force_median) {
+            std::vector<Box> bb(nbins);
+            std::vector<uint32_t> bc(nbins);
+            std::vector<double> right_area(nbins), right_cnt(nbins);
+            for (int a = 0; a < 3; ++a) {
+                const float ext = cb.hi[a] - cb.lo[a];
+                if (!(ext > 0.0f)) continue;
+                const float scale = (float)nbins / ext;
+                for (int k = 0; k < nbins; ++k) { bb[k] = Box(); bc[k] = 0; }
+                for (uint32_t i = b; i < e; ++i) {
+                    int k = (int)((refs[i].c[a] - cb.lo[a]) * scale);
+                    k = std::min(std::max(k, 0), nbins - 1);
+                    bb[k].grow(refs[i].lo, refs[i].hi);
+                    bc[k]++;
+                }
+                Box acc;
+                uint32_t cnt = 0;
+                for (int k = nbins - 1; k > 0; --k) {
+                    acc.grow(bb[k].lo, bb[k].hi);
+                    cnt += bc[k];
+                    right_area[k] = acc.area();
+                    right_cnt[k] = cnt;
+                }
+                acc = Box();
+                cnt = 0;
+                for (int k = 0; k < nbins - 1; ++k) {
+                    acc.grow(bb[k].lo, bb[k].hi);
+                    cnt += bc[k];
+                    if (cnt == 0 || cnt == n) continue;
+                    double cost = C_TRAV + C_ISECT * (acc.area() * cnt + right_area[k + 1] * right_cnt[k + 1]) /
+                                               std::max(parent_area, 1e-300);
+                    if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = k; }
+                }
+            }
+            const double leaf_cost = C_ISECT * n;
+            if (n <= max_leaf && (best_axis < 0 || leaf_cost <= best_cost)) return make_leaf(b, e, bx);
+        }
+        uint32_t mid;
+        if (best_axis >= 0) {
+            const int a = best_axis;
+            const float ext = cb.hi[a] - cb.lo[a];
+            const float scale = (float)nbins / ext;
+            auto it = std::partition(refs.begin() + b, refs.begin() + e, [&](const PrimRef& r) {
+                int k = (int)((r.c[a] - cb.lo[a]) * scale);
+                k = std::min(std::max(k, 0), nbins - 1);
+                return k <= best_bin;
+            });
+            mid = (uint32_t)(it - refs.begin());
+        } else {
+            // degenerate centroids or depth guard: object median on the widest axis
+            int a = 0;
+            float w = -1.0f;
+            for (int k = 0; k < 3; ++k)
+                if (cb.hi[k] - cb.lo[k] > w) { w = cb.hi[k] - cb.lo[k]; a = k; }
+            mid = b + n / 2;
+            std::nth_element(refs.begin() + b, refs.begin() + mid, refs.begin() + e,
+                             [a](const PrimRef& x, const PrimRef& y) { return x.c[a] < y.c[a]; });
+        }
+        if (mid == b || mid == e) mid = b + n / 2;
+        BNode node;
+        std::memcpy(node.lo, bx.lo, sizeof node.lo);
+        std::memcpy(node.hi, bx.hi, sizeof node.hi);
+        nodes.push_back(node);
+        const int self = (int)nodes.size() - 1;
+        const int l = build(b, mid, depth + 1);
+        const int r = build(mid, e, depth + 1);
+        nodes[self].left = l;
+        nodes[self].right = r;
+        return self;
+    }
+};
+
+inline V3 dir_from_angles(float sin_t, float cos_t, float phi) {
+    return v3(-sin_t * std::cos(phi), -cos_t, sin_t * std::sin(phi));
+}
+
+inline size_t sat_usize(float x) {
+    if (!(x > 0.0f)) return 0;
+    if (x >= 18446744073709551615.0f) return SIZE_MAX;
+    return (size_t)x;
+}
+
+void build_env_tables(HostScene& hs) {
+    const SceneView& v = hs.view;
+    const uint32_t W = v.env_w, H = v.env_h;
+    EnvTables& T = hs.tables;
+    T.W = W;
+    T.H = H;
+    std::vector<double> lum((size_t)W * H);
+    double lsum = 0.0;
+    for (uint32_t j = 0; j < H; ++j) {
+        float theta = ((float)j + 0.5f) * (PI_F / (float)H);
+        float st = std::sin(theta), ct = std::cos(theta);
+        for (uint32_t i = 0; i < W; ++i) {
+            float phi = ((float)i + 0.5f) * (2.0f * PI_F / (float)W);
+            V3 c = env_eval_host(v, hs.env_img.data(), dir_from_angles(st, ct, phi));
+            float l = 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+            if (!(l > 0.0f) || !std::isfinite(l)) l = 0.0f;
+            lum[(size_t)j * W + i] = (double)l;
+            lsum += (double)l;
+        }
+    }
+    double floor_l = 1e-3 * (lsum / ((double)W * H));
+    if (!(floor_l > 0.0)) floor_l = 1.0;
+    std::vector<double> w((size_t)W * H), rows(H);
+    double total = 0.0;
+    for (uint32_t j = 0; j < H; ++j) {
+        float theta = ((float)j + 0.5f) * (PI_F / (float)H);
+        double st = (double)std::sin(theta);
+        double rs = 0.0;
+        for (uint32_t i = 0; i < W; ++i) {
+            double x = (lum[(size_t)j * W + i] + floor_l) * st;
+            w[(size_t)j * W + i] = x;
+            rs += x;
+        }
+        rows[j] = rs;
+        total += rs;
+    }
+    T.marginal.assign(H + 1, 0.0f);
+    T.conditional.assign((size_t)H * (W + 1), 0.0f);
+    T.cell.assign((size_t)W * H, 0.0f);
+    double acc = 0.0;
+    for (uint32_t j = 0; j < H; ++j) {
+        T.marginal[j] = (float)(acc / total);
+        acc += rows[j];
+        double ra = 0.0;
+        float* cr = &T.conditional[(size_t)j * (W + 1)];
+        for (uint32_t i = 0; i < W; ++i) {
+            cr[i] = (float)(ra / rows[j]);
+            ra += w[(size_t)j * W + i];
+            T.cell[(size_t)j * W + i] = (float)(w[(size_t)j * W + i] / total);
+        }
+        cr[W] = 1.0f;
+    }
+    T.marginal[H] = 1.0f;
+}
+
+}  // namespace
+
+V3 env_eval_host(const SceneView& v, const float* img, V3 dir) {
+    if (v.env_kind == VR_ENV_UNIFORM) return load3(v.env_color);
+    if (v.env_kind != VR_ENV_HDRI) return v3(0.0f, 0.0f, 0.0f);
+    V3 d = normalize(dir);
+    float sx = std::acos(-d.y);
+    float sy = std::atan2(-d.z, d.x) + PI_F;
+    float u = sx / PI_F;
+    float vv = sy / (2.0f * PI_F);
+    float x = vv * (float)v.env_w;
+    float y = (float)(v.env_h - 1) - (u * (float)v.env_h);
+    size_t W = v.env_w, H = v.env_h, len = W * H;
+    size_t x0 = std::min(sat_usize(x), W - 1);
+    size_t y0 = std::min(sat_usize(y), H - 1);
+    float ax = x - (float)x0;
+    float ay = y - (float)y0;
+    auto px = [&](size_t i) { return load3(img + 3 * (i % len)); };
+    return lerp3(lerp3(px(y0 * W + x0), px(y0 * W + x0 + 1), ax),
+                 lerp3(px((y0 + 1) * W + x0), px((y0 + 1) * W + x0 + 1), ax), ay);
+}
+
+void set_camera(SceneView& v, const vr_camera_desc& c) {
+    V3 dir = load3(c.direction), up = load3(c.up), eye = load3(c.eye);
+    V3 right = normalize(cross(dir, up));
+    for (int a = 0; a < 3; ++a) {
+        v.c_origin[a] = (&eye.x)[a];
+        v.c_dir[a] = (&dir.x)[a];
+        v.c_up[a] = (&up.x)[a];
+        v.c_right[a] = (&right.x)[a];
+    }
+    v.c_d = 1.0f / std::tan(c.fov / 2.0f);
+    v.c_dof = c.has_dof ? 1 : 0;
+    v.c_aperture = c.has_dof ? c.aperture : 0.0f;
+    v.c_focal = c.has_dof ? dot(load3(c.focal_point) - eye, dir) : 0.0f;
+}
+
+vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& err) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!d) { err = "null scene descriptor"; return VR_ERR_INVALID; }
+    if (d->num_meshes && !d->meshes) { err = "meshes is NULL"; return VR_ERR_INVALID; }
+    if (d->num_materials && !d->materials) { err = "materials is NULL"; return VR_ERR_INVALID; }
+    hs.materials.resize(d->num_materials);
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        static_assert(sizeof(Material) == sizeof(vr_material), "material layout");
+        std::memcpy(&hs.materials[i], &d->materials[i], sizeof(Material));
+        if (hs.materials[i].kind < 0 || hs.materials[i].kind > M_MICRO) {
+            err = "material " + std::to_string(i) + ": unsupported kind";
+            return VR_ERR_UNSUPPORTED;
+        }
+    }
+    uint64_t np = 0;
+    bool any_uv = false;
+    for (uint32_t m = 0; m < d->num_meshes; ++m) {
+        const vr_mesh_desc& md = d->meshes[m];
+        if (md.num_triangles && (!md.positions || !md.indices)) {
+            err = "mesh " + std::to_string(m) + ": positions/indices NULL";
+            return VR_ERR_INVALID;
+        }
+        if (md.material >= d->num_materials) {
+            err = "mesh " + std::to_string(m) + ": material index out of range";
+            return VR_ERR_INVALID;
+        }
+        np += md.num_triangles;
+        any_uv = any_uv || md.uvs;
+    }
+    if (np >= (1ull << 31)) { err = "too many triangles"; return VR_ERR_INVALID; }
+    hs.num_prims = np;
+    std::vector<PrimRef> refs(np);
+    std::vector<float4> v0e(np * 3);  // v0, e1, e2 by prim id
+    hs.shade.resize(np * 4);
+    if (any_uv) hs.uvs.resize(np * 3);
+    Box scene_box;
+    uint64_t p = 0;
+    for (uint32_t m = 0; m < d->num_meshes; ++m) {
+        const vr_mesh_desc& md = d->meshes[m];
+        for (uint32_t t = 0; t < md.num_triangles; ++t, ++p) {
+            uint32_t ix[3] = {md.indices[3 * t], md.indices[3 * t + 1], md.indices[3 * t + 2]};
+            for (int k = 0; k < 3; ++k)
+                if (ix[k] >= md.num_vertices) {
+                    err = "mesh " + std::to_string(m) + ": index out of range";
+                    return VR_ERR_INVALID;
+                }
+            V3 P[3], N[3];
+            for (int k = 0; k < 3; ++k) {
+                P[k] = load3(md.positions + 3 * (size_t)ix[k]);
+                N[k] = md.normals ? load3(md.normals + 3 * (size_t)ix[k]) : v3(0.0f, 0.0f, 0.0f);
+                if (any_uv) {
+                    hs.uvs[3 * p + k] = md.uvs ? make_float2(md.uvs[2 * (size_t)ix[k]], md.uvs[2 * (size_t)ix[k] + 1])
+                                               : make_float2(0.0f, 0.0f);
+                }
+            }
+            // Triangle::hit edges (mesh.rs:150-151)
+            V3 e1 = P[1] - P[0], e2 = P[2] - P[0];
+            // face normal, Mesh::from_buffers (mesh.rs:80-84)
+            V3 fe1 = P[0] - P[1], fe2 = P[2] - P[1];
+            V3 fn = normalize(cross(fe2, fe1));
+            uint32_t pid = (uint32_t)p;
+            float pbits;
+            std::memcpy(&pbits, &pid, 4);
+            float mbits;
+            std::memcpy(&mbits, &md.material, 4);
+            v0e[3 * p + 0] = make_float4(P[0].x, P[0].y, P[0].z, pbits);
+            v0e[3 * p + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+            v0e[3 * p + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+            hs.shade[4 * p + 0] = make_float4(N[0].x, N[0].y, N[0].z, mbits);
+            hs.shade[4 * p + 1] = make_float4(N[1].x, N[1].y, N[1].z, 0.0f);
+            hs.shade[4 * p + 2] = make_float4(N[2].x, N[2].y, N[2].z, 0.0f);
+            hs.shade[4 * p + 3] = make_float4(fn.x, fn.y, fn.z, 0.0f);
+            PrimRef& r = refs[p];
+            for (int a = 0; a < 3; ++a) {
+                float x0 = (&P[0].x)[a], x1 = (&P[1].x)[a], x2 = (&P[2].x)[a];
+                r.lo[a] = std::min(x0, std::min(x1, x2));
+                r.hi[a] = std::max(x0, std::max(x1, x2));
+                r.c[a] = 0.5f * (r.lo[a] + r.hi[a]);
+            }
+            r.id = pid;
+            scene_box.grow(r.lo, r.hi);
+        }
+    }
+    // BVH
+    uint32_t max_leaf = d->bvh_max_leaf ? d->bvh_max_leaf : 4;
+    int nbins = d->bvh_bins ? (int)d->bvh_bins : 16;
+    if (max_leaf > 16) max_leaf = 16;
+    if (nbins < 2) nbins = 2;
+    if (nbins > 64) nbins = 64;
+    hs.max_leaf = max_leaf;
+    hs.nodes.clear();
+    hs.tris.clear();
+    if (np > 0) {
+        Builder B(refs, max_leaf, nbins);
+        B.nodes.reserve(np / 2 + 16);
+        int root = B.build(0, (uint32_t)np, 0);
+        hs.max_depth = B.max_depth + 1;
+        // conservative padding keeps the f32 slab test from culling a box whose
+        // triangle is hit right on its boundary
+        float smax = 0.0f;
+        for (int a = 0; a < 3; ++a) smax = std::max(smax, std::max(std::fabs(scene_box.lo[a]), std::fabs(scene_box.hi[a])));
+        const float pad = std::max(smax, 1e-20f) * 1e-6f;
+        // triangle order = prim order after partitioning
+        hs.tris.resize(np * 3);
+        for (uint64_t i = 0; i < np; ++i)
+            for (int k = 0; k < 3; ++k) hs.tris[3 * i + k] = v0e[3 * (size_t)refs[i].id + k];
+        // flatten inner nodes depth first
+        std::vector<int> order;  // builder node -> flat index
+        std::vector<int> flat_of(B.nodes.size(), -1);
+        std::vector<int> stack;
+        auto is_leaf = [&](int n) { return B.nodes[n].left < 0; };
+        int root_inner = root;
+        if (is_leaf(root)) {
+            // single leaf: an inner root whose both children are that leaf
+            BNode rn = B.nodes[root];
+            rn.left = root;
+            rn.right = root;
+            B.nodes.push_back(rn);
+            root_inner = (int)B.nodes.size() - 1;
+            flat_of.push_back(-1);
+        }
+        stack.push_back(root_inner);
+        while (!stack.empty()) {
+            int n = stack.back();
+            stack.pop_back();
+            flat_of[n] = (int)order.size();
+            order.push_back(n);
+            const BNode& bn = B.nodes[n];
+            if (!is_leaf(bn.right) && bn.right != n) stack.push_back(bn.right);
+            if (!is_leaf(bn.left) && bn.left != n) stack.push_back(bn.left);
+        }
+        hs.nodes.resize(order.size() * 4);
+        double sah = 0.0;
+        const double root_area = Box(scene_box).area();
+        for (size_t f = 0; f < order.size(); ++f) {
+            const BNode& bn = B.nodes[order[f]];
+            const BNode& c0 = B.nodes[bn.left];
+            const BNode& c1 = B.nodes[bn.right];
+            auto lo = [&](const BNode& c, int a) { return c.lo[a] - pad; };
+            auto hi = [&](const BNode& c, int a) { return c.hi[a] + pad; };
+            hs.nodes[4 * f + 0] = make_float4(lo(c0, 0), hi(c0, 0), lo(c0, 1), hi(c0, 1));
+            hs.nodes[4 * f + 1] = make_float4(lo(c1, 0), hi(c1, 0), lo(c1, 1), hi(c1, 1));
+            hs.nodes[4 * f + 2] = make_float4(lo(c0, 2), hi(c0, 2), lo(c1, 2), hi(c1, 2));
+            int32_t r0 = is_leaf(bn.left) ? (int32_t)c0.first : flat_of[bn.left];
+            int32_t r1 = is_leaf(bn.right) ? (int32_t)c1.first : flat_of[bn.right];
+            int32_t n0 = is_leaf(bn.left) ? (int32_t)c0.count : 0;
+            int32_t n1 = is_leaf(bn.right) ? (int32_t)c1.count : 0;
+            float fr0, fr1, fn0, fn1;
+            std::memcpy(&fr0, &r0, 4);
+            std::memcpy(&fr1, &r1, 4);
+            std::memcpy(&fn0, &n0, 4);
+            std::memcpy(&fn1, &n1, 4);
+            hs.nodes[4 * f + 3] = make_float4(fr0, fr1, fn0, fn1);
+            Box nb;
+            nb.grow(bn.lo, bn.hi);
+            sah += C_TRAV * nb.area() / std::max(root_area, 1e-300);
+            for (const BNode* c : {&c0, &c1}) {
+                if (c->left < 0) {
+                    Box cb2;
+                    cb2.grow(c->lo, c->hi);
+                    sah += C_ISECT * c->count * cb2.area() / std::max(root_area, 1e-300);
+                }
+            }
+        }
+        hs.sah_cost = sah;
+    }
+    // environment
+    SceneView& v = hs.view;
+    v.env_kind = d->environment.kind;
+    for (int a = 0; a < 3; ++a) v.env_color[a] = d->environment.color[a];
+    if (v.env_kind == VR_ENV_HDRI) {
+        const vr_environment_desc& e = d->environment;
+        if (!e.image || e.width == 0 || e.height == 0) { err = "HDRI environment without an image"; return VR_ERR_INVALID; }
+        v.env_w = e.width;
+        v.env_h = e.height;
+        hs.env_img.assign(e.image, e.image + 3 * (size_t)e.width * e.height);
+        if (e.importance_sample) {
+            build_env_tables(hs);
+            hs.has_tables = true;
+            // W*H / (2 pi^2): the cell solid-angle factor, same rounding as the oracle
+            v.env_density_scale = (float)((double)e.width * (double)e.height *
+                                          (1.0 / (2.0 * 3.14159265358979323846 * 3.14159265358979323846)));
+        }
+    } else if (v.env_kind != VR_ENV_NONE && v.env_kind != VR_ENV_UNIFORM) {
+        err = "unsupported environment kind";
+        return VR_ERR_UNSUPPORTED;
+    }
+    v.env_is = hs.has_tables ? 1 : 0;
+    v.num_materials = (int32_t)d->num_materials;
+    set_camera(v, d->camera);
+    hs.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return VR_OK;
+}
+
+vr_status validate_host_scene(const HostScene& hs, std::string& err) {
+    const uint64_t np = hs.num_prims;
+    if (np == 0) return hs.nodes.empty() ? VR_OK : (err = "nodes without triangles", VR_ERR_INVALID);
+    const uint64_t nn = hs.nodes.size() / 4;
+    std::vector<uint32_t> seen(np, 0);
+    std::vector<uint8_t> visited(nn, 0);
+    struct Item {
+        int32_t node;
+        float lo[3], hi[3];
+        uint32_t depth;
+    };
+    std::vector<Item> stack;
+    Item root{0, {-INFINITY, -INFINITY, -INFINITY}, {INFINITY, INFINITY, INFINITY}, 1};
+    stack.push_back(root);
+    auto as_int = [](float f) {
+        int32_t i;
+        std::memcpy(&i, &f, 4);
+        return i;
+    };
+    while (!stack.empty()) {
+        Item it = stack.back();
+        stack.pop_back();
+        if (it.node < 0 || (uint64_t)it.node >= nn) { err = "child index out of range"; return VR_ERR_INVALID; }
+        if (visited[it.node]++) { err = "node reached twice"; return VR_ERR_INVALID; }
+        if (it.depth >= (uint32_t)STACK_SIZE) { err = "tree deeper than the traversal stack"; return VR_ERR_INVALID; }
+        const float4* n = &hs.nodes[4 * (size_t)it.node];
+        float clo[2][3] = {{n[0].x, n[0].z, n[2].x}, {n[1].x, n[1].z, n[2].z}};
+        float chi[2][3] = {{n[0].y, n[0].w, n[2].y}, {n[1].y, n[1].w, n[2].w}};
+        int32_t ref[2] = {as_int(n[3].x), as_int(n[3].y)};
+        int32_t cnt[2] = {as_int(n[3].z), as_int(n[3].w)};
+        const bool dup_root = (it.node == 0 && ref[0] == ref[1] && cnt[0] == cnt[1] && cnt[0] > 0);
+        for (int c = 0; c < 2; ++c) {
+            for (int a = 0; a < 3; ++a) {
+                if (!(clo[c][a] <= chi[c][a])) { err = "inverted child box"; return VR_ERR_INVALID; }
+                if (clo[c][a] < it.lo[a] || chi[c][a] > it.hi[a]) {
+                    // a child box lies inside its parent's (padded) box
+                    const float slack = 4e-6f * std::max(1.0f, std::max(std::fabs(it.lo[a]), std::fabs(it.hi[a])));
+                    if (clo[c][a] < it.lo[a] - slack || chi[c][a] > it.hi[a] + slack) {
+                        err = "child box outside its parent";
+                        return VR_ERR_INVALID;
+                    }
+                }
+            }
+            if (cnt[c] > 0) {
+                if (dup_root && c == 1) continue;
+                if (ref[c] < 0 || (uint64_t)ref[c] + cnt[c] > np) { err = "leaf range out of bounds"; return VR_ERR_INVALID; }
+                for (int32_t k = 0; k < cnt[c]; ++k) {
+                    const float4* t = &hs.tris[3 * ((size_t)ref[c] + k)];
+                    uint32_t pid;
+                    std::memcpy(&pid, &t[0].w, 4);
+                    if (pid >= np) { err = "prim id out of range"; return VR_ERR_INVALID; }
+                    seen[pid]++;
+                    const float vx[3][3] = {{t[0].x, t[0].y, t[0].z},
+                                            {t[0].x + t[1].x, t[0].y + t[1].y, t[0].z + t[1].z},
+                                            {t[0].x + t[2].x, t[0].y + t[2].y, t[0].z + t[2].z}};
+                    for (int q = 0; q < 3; ++q)
+                        for (int a = 0; a < 3; ++a) {
+                            const float slack = 4e-6f * std::max(1.0f, std::fabs(vx[q][a]));
+                            if (vx[q][a] < clo[c][a] - slack || vx[q][a] > chi[c][a] + slack) {
+                                err = "triangle outside its leaf box";
+                                return VR_ERR_INVALID;
+                            }
+                        }
+                }
+            } else {
+                Item ch{ref[c], {clo[c][0], clo[c][1], clo[c][2]}, {chi[c][0], chi[c][1], chi[c][2]}, it.depth + 1};
+                stack.push_back(ch);
+            }
+        }
+    }
+    for (uint64_t i = 0; i < nn; ++i)
+        if (!visited[i]) { err = "unreachable node"; return VR_ERR_INVALID; }
+    for (uint64_t p = 0; p < np; ++p)
+        if (seen[p] != 1) { err = "triangle " + std::to_string(p) + " appears " + std::to_string(seen[p]) + " times"; return VR_ERR_INVALID; }
+    return VR_OK;
+}
+
+}  // namespace vr

@@ -1,0 +1,478 @@
+// vr_capi.cu — implementation of the C ABI declared in include/voidray_gpu.h.
+//
+// Ownership: a vr_scene owns its device memory and one non-blocking CUDA
+// stream.  Render scratch (path state, ray queues, pixel sums) is allocated
+// lazily per scene and grown when a larger wavefront is requested.  Errors are
+// returned as vr_status with a thread-local message; kernel-side faults that
+// can be detected (traversal stack overflow) are recorded in a per-scene
+// device status word and reported by the next synchronising call.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/voidray_gpu.h"
+#include "vr_host.h"
+#include "vr_kernels.h"
+
+namespace {
+thread_local std::string g_err;
+
+vr_status fail(vr_status s, const std::string& m) {
+    g_err = m;
+    return s;
+}
+
+#define VR_CK(expr)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (expr);                                                                      \
+        if (e_ != cudaSuccess) {                                                                      \
+            vr_status s_ = (e_ == cudaErrorMemoryAllocation) ? VR_ERR_OOM : VR_ERR_CUDA;              \
+            return fail(s_, std::string(#expr) + ": " + cudaGetErrorString(e_));                       \
+        }                                                                                             \
+    } while (0)
+
+bool device_ok() {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct vr_scene {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    vr::SceneView view{};
+    std::vector<void*> allocs;
+    uint64_t scene_bytes = 0;
+    vr_scene_info info{};
+    vr_render_stats stats{};
+    uint32_t* status = nullptr;               // device status word
+    unsigned long long* totals = nullptr;     // device: paths, extend, shadow, counters x2
+    double* dres = nullptr;                   // device scratch for reductions
+    // render scratch
+    vr::PathState ps{};
+    uint32_t ps_cap = 0, ps_bounces = 0;
+    std::vector<void*> ps_allocs;
+    uint64_t ps_bytes = 0;
+    float4* psum = nullptr;
+    uint32_t psum_cap = 0;
+    // host-call staging
+    DevBuf stage_a, stage_b;
+};
+
+namespace {
+
+template <class T>
+vr_status upload(vr_scene* s, const std::vector<T>& v, const T** out) {
+    *out = nullptr;
+    if (v.empty()) return VR_OK;
+    void* p = nullptr;
+    size_t bytes = v.size() * sizeof(T);
+    VR_CK(cudaMalloc(&p, bytes));
+    s->allocs.push_back(p);
+    s->scene_bytes += bytes;
+    VR_CK(cudaMemcpy(p, v.data(), bytes, cudaMemcpyHostToDevice));
+    *out = static_cast<const T*>(p);
+    return VR_OK;
+}
+
+void free_scratch(vr_scene* s) {
+    for (void* p : s->ps_allocs) cudaFree(p);
+    s->ps_allocs.clear();
+    s->ps = vr::PathState{};
+    s->ps_cap = 0;
+    s->ps_bounces = 0;
+    s->ps_bytes = 0;
+}
+
+template <class T>
+vr_status scratch_alloc(vr_scene* s, T** out, size_t count) {
+    void* p = nullptr;
+    size_t bytes = count * sizeof(T);
+    VR_CK(cudaMalloc(&p, bytes == 0 ? 16 : bytes));
+    s->ps_allocs.push_back(p);
+    s->ps_bytes += bytes;
+    *out = static_cast<T*>(p);
+    return VR_OK;
+}
+
+vr_status ensure_scratch(vr_scene* s, uint32_t cap, uint32_t bounces, bool need_att) {
+    uint32_t need_b = need_att ? bounces : 0;
+    if (s->ps_cap >= cap && s->ps_bounces >= need_b) return VR_OK;
+    VR_CK(cudaStreamSynchronize(s->stream));
+    free_scratch(s);
+    vr::PathState& ps = s->ps;
+    vr_status st;
+#define SA(field, n)                                            \
+    if ((st = scratch_alloc(s, &ps.field, (n))) != VR_OK) {     \
+        free_scratch(s);                                        \
+        return st;                                              \
+    }
+    SA(q_org, 2 * (size_t)cap);
+    SA(q_dir, 2 * (size_t)cap);
+    SA(q_path, 2 * (size_t)cap);
+    SA(hits, (size_t)cap);
+    SA(rng, (size_t)cap);
+    SA(thr, (size_t)cap);
+    SA(rad, (size_t)cap);
+    SA(att, (size_t)std::max<uint32_t>(need_b, 1) * 3 * cap);
+    SA(s_org, (size_t)cap);
+    SA(s_dir, (size_t)cap);
+    SA(s_contrib, (size_t)cap);
+    SA(s_path, (size_t)cap);
+    SA(counts, 2 * (size_t)vr::MAX_DEPTH_SLOTS);
+#undef SA
+    ps.cap = cap;
+    s->ps_cap = cap;
+    s->ps_bounces = need_b;
+    return VR_OK;
+}
+
+vr_status ensure_buf(DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes) return VR_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    VR_CK(cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return VR_OK;
+}
+
+cudaStream_t pick(vr_scene* s, void* stream) { return stream ? static_cast<cudaStream_t>(stream) : s->stream; }
+
+vr_status check_status(vr_scene* s) {
+    uint32_t flags = 0;
+    VR_CK(cudaMemcpy(&flags, s->status, 4, cudaMemcpyDeviceToHost));
+    s->stats.error_flags |= flags;
+    if (flags) {
+        VR_CK(cudaMemset(s->status, 0, 4));
+        if (flags & vr::ERRF_STACK) return fail(VR_ERR_STACK, "traversal stack overflow in a kernel");
+        return fail(VR_ERR_CUDA, "kernel reported error flags " + std::to_string(flags));
+    }
+    return VR_OK;
+}
+
+vr_status validate_render(const vr_scene* scene, const vr_render_settings* st, uint32_t w, uint32_t h) {
+    if (!scene || !st) return fail(VR_ERR_INVALID, "null scene or settings");
+    if (w == 0 || h == 0) return fail(VR_ERR_INVALID, "empty image");
+    if ((uint64_t)w * h >= (1ull << 31)) return fail(VR_ERR_INVALID, "image too large");
+    if (st->total_samples == 0) return fail(VR_ERR_INVALID, "total_samples must be > 0");
+    if (st->max_bounces >= vr::MAX_DEPTH_SLOTS)
+        return fail(VR_ERR_UNSUPPORTED, "max_bounces must be below " + std::to_string(vr::MAX_DEPTH_SLOTS));
+    if (st->render_mode != VR_MODE_NORMAL && st->render_mode != VR_MODE_FULL)
+        return fail(VR_ERR_INVALID, "render_mode");
+    if (st->estimator != VR_EST_REFERENCE && st->estimator != VR_EST_NEE) return fail(VR_ERR_INVALID, "estimator");
+    return VR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* vr_last_error(void) { return g_err.c_str(); }
+int32_t vr_abi_version(void) { return VR_ABI_VERSION; }
+int32_t vr_device_available(void) { return device_ok() ? 1 : 0; }
+
+vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
+    if (!out) return fail(VR_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    vr::HostScene hs;
+    std::string err;
+    vr_status st = vr::build_host_scene(desc, hs, err);
+    if (st != VR_OK) return fail(st, err);
+    vr_scene* s = new vr_scene();
+    auto cleanup = [&](vr_status r) {
+        vr_scene_destroy(s);
+        return r;
+    };
+    cudaGetDevice(&s->device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(VR_ERR_CUDA, "stream creation failed"));
+    s->view = hs.view;
+    if ((st = upload(s, hs.nodes, &s->view.nodes)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.tris, &s->view.tris)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.shade, &s->view.shade)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.uvs, &s->view.uvs)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.materials, &s->view.materials)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.env_img, &s->view.env_img)) != VR_OK) return cleanup(st);
+    if (hs.has_tables) {
+        if ((st = upload(s, hs.tables.marginal, &s->view.env_marg)) != VR_OK) return cleanup(st);
+        if ((st = upload(s, hs.tables.conditional, &s->view.env_cond)) != VR_OK) return cleanup(st);
+        if ((st = upload(s, hs.tables.cell, &s->view.env_cell)) != VR_OK) return cleanup(st);
+    }
+    void* p = nullptr;
+    if (cudaMalloc(&p, 64) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "status alloc"));
+    s->allocs.push_back(p);
+    s->status = static_cast<uint32_t*>(p);
+    if (cudaMalloc(&p, 8 * sizeof(unsigned long long)) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "totals alloc"));
+    s->allocs.push_back(p);
+    s->totals = static_cast<unsigned long long*>(p);
+    if (cudaMalloc(&p, 8 * sizeof(double)) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "result alloc"));
+    s->allocs.push_back(p);
+    s->dres = static_cast<double*>(p);
+    if (cudaMemset(s->status, 0, 64) != cudaSuccess || cudaMemset(s->totals, 0, 64) != cudaSuccess)
+        return cleanup(fail(VR_ERR_CUDA, "memset"));
+    s->info.num_triangles = hs.num_prims;
+    s->info.num_nodes = hs.nodes.size() / 4;
+    s->info.device_bytes = s->scene_bytes;
+    s->info.max_depth = hs.max_depth;
+    s->info.max_leaf = hs.max_leaf;
+    s->info.sah_cost = hs.sah_cost;
+    s->info.build_ms = hs.build_ms;
+    *out = s;
+    return VR_OK;
+}
+
+vr_status vr_scene_destroy(vr_scene* s) {
+    if (!s) return VR_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_scratch(s);
+    if (s->psum) cudaFree(s->psum);
+    if (s->stage_a.p) cudaFree(s->stage_a.p);
+    if (s->stage_b.p) cudaFree(s->stage_b.p);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return VR_OK;
+}
+
+vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
+    vr::HostScene hs;
+    std::string err;
+    vr_status st = vr::build_host_scene(desc, hs, err);
+    if (st != VR_OK) return fail(st, err);
+    st = vr::validate_host_scene(hs, err);
+    if (st != VR_OK) return fail(st, err);
+    if (info) {
+        *info = vr_scene_info{};
+        info->num_triangles = hs.num_prims;
+        info->num_nodes = hs.nodes.size() / 4;
+        info->device_bytes = hs.nodes.size() * 16 + hs.tris.size() * 16 + hs.shade.size() * 16 + hs.uvs.size() * 8 +
+                             hs.env_img.size() * 4 +
+                             (hs.tables.marginal.size() + hs.tables.conditional.size() + hs.tables.cell.size()) * 4;
+        info->max_depth = hs.max_depth;
+        info->max_leaf = hs.max_leaf;
+        info->sah_cost = hs.sah_cost;
+        info->build_ms = hs.build_ms;
+    }
+    return VR_OK;
+}
+
+vr_status vr_scene_info_get(const vr_scene* s, vr_scene_info* info) {
+    if (!s || !info) return fail(VR_ERR_INVALID, "null argument");
+    *info = s->info;
+    info->device_bytes = s->scene_bytes;
+    return VR_OK;
+}
+
+vr_status vr_scene_set_camera(vr_scene* s, const vr_camera_desc* cam) {
+    if (!s || !cam) return fail(VR_ERR_INVALID, "null argument");
+    vr::set_camera(s->view, *cam);
+    return VR_OK;
+}
+
+vr_status vr_scene_synchronize(vr_scene* s) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    VR_CK(cudaStreamSynchronize(s->stream));
+    return check_status(s);
+}
+
+vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba, uint32_t w,
+                           uint32_t h, uint64_t seed, uint32_t first_sample, void* stream) {
+    vr_status r = validate_render(s, st, w, h);
+    if (r != VR_OK) return r;
+    if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
+    if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
+    if (samples == 0) return VR_OK;
+    cudaStream_t cs = pick(s, stream);
+    const uint32_t np = w * h;
+    const uint64_t total = (uint64_t)samples * np;
+    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 22);
+    if (cap > (1ull << 26)) cap = 1ull << 26;
+    if (cap > total) cap = total;
+    const bool need_att = st->estimator == VR_EST_REFERENCE;
+    if ((r = ensure_scratch(s, (uint32_t)cap, st->max_bounces, need_att)) != VR_OK) return r;
+    if (s->psum_cap < np) {
+        VR_CK(cudaStreamSynchronize(s->stream));
+        if (s->psum) cudaFree(s->psum);
+        s->psum = nullptr;
+        s->psum_cap = 0;
+        VR_CK(cudaMalloc(&s->psum, (size_t)np * sizeof(float4)));
+        s->psum_cap = np;
+    }
+    VR_CK(cudaMemsetAsync(s->psum, 0, (size_t)np * sizeof(float4), cs));
+    vr::RenderParams rp{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
+    auto t0 = std::chrono::steady_clock::now();
+    uint64_t waves = 0;
+    for (uint64_t g0 = 0; g0 < total; g0 += cap) {
+        vr::WaveParams wp{};
+        wp.g0 = g0;
+        wp.seed = seed;
+        wp.paths = (uint32_t)std::min<uint64_t>(cap, total - g0);
+        wp.num_pixels = np;
+        wp.width = w;
+        wp.height = h;
+        wp.first_sample = first_sample;
+        VR_CK(vr::launch_wavefront(s->view, wp, rp, s->ps, s->psum, s->totals, s->status, cs));
+        ++waves;
+    }
+    VR_CK(vr::launch_finalize(s->psum, reinterpret_cast<float4*>(rgba), np, 1.0f / (float)st->total_samples, cs));
+    s->stats.wavefronts += waves;
+    s->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return VR_OK;
+}
+
+vr_status vr_render(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba, uint32_t w, uint32_t h,
+                    uint64_t seed, uint32_t first_sample) {
+    vr_status r = validate_render(s, st, w, h);
+    if (r != VR_OK) return r;
+    if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
+    const size_t bytes = (size_t)w * h * 4 * sizeof(float);
+    if ((r = ensure_buf(s->stage_a, bytes)) != VR_OK) return r;
+    auto t0 = std::chrono::steady_clock::now();
+    VR_CK(cudaMemcpyAsync(s->stage_a.p, rgba, bytes, cudaMemcpyHostToDevice, s->stream));
+    if ((r = vr_render_device(s, st, samples, static_cast<float*>(s->stage_a.p), w, h, seed, first_sample, nullptr)) !=
+        VR_OK)
+        return r;
+    VR_CK(cudaMemcpyAsync(rgba, s->stage_a.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    VR_CK(cudaStreamSynchronize(s->stream));
+    s->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return check_status(s);
+}
+
+vr_status vr_render_stats_get(const vr_scene* cs, vr_render_stats* out) {
+    if (!cs || !out) return fail(VR_ERR_INVALID, "null argument");
+    vr_scene* s = const_cast<vr_scene*>(cs);
+    VR_CK(cudaStreamSynchronize(s->stream));
+    unsigned long long t[3] = {0, 0, 0};
+    VR_CK(cudaMemcpy(t, s->totals, sizeof t, cudaMemcpyDeviceToHost));
+    uint32_t flags = 0;
+    VR_CK(cudaMemcpy(&flags, s->status, 4, cudaMemcpyDeviceToHost));
+    *out = s->stats;
+    out->paths = t[0];
+    out->extend_rays = t[1];
+    out->shadow_rays = t[2];
+    out->error_flags |= flags;
+    return VR_OK;
+}
+
+vr_status vr_intersect_device(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hit* hits, int32_t any_hit,
+                              void* stream) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    if (n && (!rays || !hits)) return fail(VR_ERR_INVALID, "null rays/hits");
+    if (n == 0) return VR_OK;
+    cudaStream_t cs = pick(s, stream);
+    if (s->info.num_triangles == 0) {
+        // empty scene: every ray misses
+        VR_CK(cudaMemsetAsync(hits, 0xFF, n * sizeof(vr_hit), cs));
+        return VR_OK;
+    }
+    VR_CK(vr::launch_intersect(s->view, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<float4*>(hits),
+                               any_hit != 0, s->status, cs));
+    return VR_OK;
+}
+
+vr_status vr_intersect(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hit* hits, int32_t any_hit) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    if (n == 0) return VR_OK;
+    if (!rays || !hits) return fail(VR_ERR_INVALID, "null rays/hits");
+    vr_status r;
+    if ((r = ensure_buf(s->stage_a, n * sizeof(vr_ray))) != VR_OK) return r;
+    if ((r = ensure_buf(s->stage_b, n * sizeof(vr_hit))) != VR_OK) return r;
+    VR_CK(cudaMemcpyAsync(s->stage_a.p, rays, n * sizeof(vr_ray), cudaMemcpyHostToDevice, s->stream));
+    if ((r = vr_intersect_device(s, static_cast<const vr_ray*>(s->stage_a.p), n, static_cast<vr_hit*>(s->stage_b.p),
+                                 any_hit, nullptr)) != VR_OK)
+        return r;
+    VR_CK(cudaMemcpyAsync(hits, s->stage_b.p, n * sizeof(vr_hit), cudaMemcpyDeviceToHost, s->stream));
+    VR_CK(cudaStreamSynchronize(s->stream));
+    return check_status(s);
+}
+
+vr_status vr_intersect_count_device(vr_scene* s, const vr_ray* rays, uint64_t n, int32_t any_hit,
+                                    uint64_t* node_visits, uint64_t* tri_tests, void* stream) {
+    if (!s || !node_visits || !tri_tests) return fail(VR_ERR_INVALID, "null argument");
+    *node_visits = 0;
+    *tri_tests = 0;
+    if (n == 0 || s->info.num_triangles == 0) return VR_OK;
+    if (!rays) return fail(VR_ERR_INVALID, "null rays");
+    cudaStream_t cs = pick(s, stream);
+    unsigned long long* c = s->totals + 4;
+    VR_CK(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned long long), cs));
+    VR_CK(vr::launch_intersect_count(s->view, reinterpret_cast<const float4*>(rays), n, any_hit != 0, c, s->status,
+                                     cs));
+    unsigned long long hc[2];
+    VR_CK(cudaMemcpyAsync(hc, c, sizeof hc, cudaMemcpyDeviceToHost, cs));
+    VR_CK(cudaStreamSynchronize(cs));
+    *node_visits = hc[0];
+    *tri_tests = hc[1];
+    return check_status(s);
+}
+
+vr_status vr_tonemap_device(const float* in, float* out, uint32_t w, uint32_t h, const vr_color_management* cm,
+                            float scale, void* stream) {
+    if (!in || !out || !cm) return fail(VR_ERR_INVALID, "null argument");
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    if (cm->tonemap < 0 || cm->tonemap > 4) return fail(VR_ERR_INVALID, "tonemap");
+    const float ex = std::pow(2.0f, cm->exposure);
+    const float inv_gamma = 1.0f / cm->gamma;
+    VR_CK(vr::launch_tonemap(reinterpret_cast<const float4*>(in), reinterpret_cast<float4*>(out), w * h, cm->tonemap,
+                             inv_gamma, ex, scale, static_cast<cudaStream_t>(stream)));
+    return VR_OK;
+}
+
+vr_status vr_tonemap(const float* in, float* out, uint32_t w, uint32_t h, const vr_color_management* cm, float scale) {
+    if (!in || !out || !cm) return fail(VR_ERR_INVALID, "null argument");
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    const size_t bytes = (size_t)w * h * 16;
+    if (bytes == 0) return VR_OK;
+    void *din = nullptr, *dout = nullptr;
+    VR_CK(cudaMalloc(&din, bytes));
+    if (cudaMalloc(&dout, bytes) != cudaSuccess) {
+        cudaFree(din);
+        return fail(VR_ERR_OOM, "tonemap buffer");
+    }
+    vr_status r = VR_OK;
+    if (cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy in");
+    if (r == VR_OK) r = vr_tonemap_device(static_cast<float*>(din), static_cast<float*>(dout), w, h, cm, scale, nullptr);
+    if (r == VR_OK && cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy out");
+    cudaFree(din);
+    cudaFree(dout);
+    return r;
+}
+
+vr_status vr_relmse_device(const float* a, float sa, const float* ref, float sr, uint32_t w, uint32_t h, double* out,
+                           void* stream) {
+    if (!a || !ref || !out) return fail(VR_ERR_INVALID, "null argument");
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    double* d = nullptr;
+    VR_CK(cudaMalloc(&d, sizeof(double)));
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    vr_status r = VR_OK;
+    if (cudaMemsetAsync(d, 0, sizeof(double), cs) != cudaSuccess) r = fail(VR_ERR_CUDA, "memset");
+    if (r == VR_OK && vr::launch_relmse(reinterpret_cast<const float4*>(a), sa, reinterpret_cast<const float4*>(ref),
+                                        sr, w * h, d, cs) != cudaSuccess)
+        r = fail(VR_ERR_CUDA, "relmse launch");
+    double sum = 0.0;
+    if (r == VR_OK && cudaMemcpyAsync(&sum, d, sizeof(double), cudaMemcpyDeviceToHost, cs) != cudaSuccess)
+        r = fail(VR_ERR_CUDA, "copy");
+    if (r == VR_OK && cudaStreamSynchronize(cs) != cudaSuccess) r = fail(VR_ERR_CUDA, "sync");
+    cudaFree(d);
+    if (r == VR_OK) *out = sum / (3.0 * (double)w * (double)h);
+    return r;
+}
+
+}  // extern "C"
