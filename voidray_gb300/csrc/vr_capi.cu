@@ -71,6 +71,14 @@ struct vr_scene {
     uint32_t psum_cap = 0;
     // host-call staging
     DevBuf stage_a, stage_b;
+    // instrumentation
+    uint32_t instr = 0;
+    std::vector<cudaEvent_t> events;   // pool, reused across calls
+    std::vector<int> event_stage;      // stage of the launch that ends at events[i] (i >= 1)
+    size_t events_used = 0;
+    double stage_ms[8] = {0};
+    uint64_t stage_launches[8] = {0};
+    unsigned long long* work = nullptr; // device: extend visits, tests, shadow visits, tests
 };
 
 namespace {
@@ -165,6 +173,35 @@ vr_status check_status(vr_scene* s) {
     return VR_OK;
 }
 
+// Records the event that closes a launch of `stage` (the previous event opened it).
+vr_status mark(vr_scene* s, int stage, cudaStream_t cs) {
+    if (!(s->instr & VR_INSTR_STAGE_TIMES)) return VR_OK;
+    if (s->events_used == s->events.size()) {
+        cudaEvent_t e;
+        VR_CK(cudaEventCreate(&e));
+        s->events.push_back(e);
+        s->event_stage.push_back(-1);
+    }
+    s->event_stage[s->events_used] = stage;
+    VR_CK(cudaEventRecord(s->events[s->events_used], cs));
+    s->events_used++;
+    return VR_OK;
+}
+
+// Folds recorded events into the per-stage totals (after a synchronisation).
+vr_status collect_events(vr_scene* s) {
+    for (size_t i = 1; i < s->events_used; ++i) {
+        int st = s->event_stage[i];
+        if (st < 0) continue;
+        float ms = 0.0f;
+        VR_CK(cudaEventElapsedTime(&ms, s->events[i - 1], s->events[i]));
+        s->stage_ms[st] += ms;
+        s->stage_launches[st] += 1;
+    }
+    s->events_used = 0;
+    return VR_OK;
+}
+
 vr_status validate_render(const vr_scene* scene, const vr_render_settings* st, uint32_t w, uint32_t h) {
     if (!scene || !st) return fail(VR_ERR_INVALID, "null scene or settings");
     if (w == 0 || h == 0) return fail(VR_ERR_INVALID, "empty image");
@@ -237,9 +274,46 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     return VR_OK;
 }
 
+vr_status vr_scene_instrument(vr_scene* s, uint32_t flags) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    VR_CK(cudaStreamSynchronize(s->stream));
+    if (!s->work) VR_CK(cudaMalloc(&s->work, 4 * sizeof(unsigned long long)));
+    VR_CK(cudaMemset(s->work, 0, 4 * sizeof(unsigned long long)));
+    s->instr = flags;
+    s->events_used = 0;
+    for (int i = 0; i < 8; ++i) {
+        s->stage_ms[i] = 0.0;
+        s->stage_launches[i] = 0;
+    }
+    return VR_OK;
+}
+
+vr_status vr_scene_instrument_get(vr_scene* s, vr_instrument* out) {
+    if (!s || !out) return fail(VR_ERR_INVALID, "null argument");
+    VR_CK(cudaDeviceSynchronize());
+    vr_status r = collect_events(s);
+    if (r != VR_OK) return r;
+    *out = vr_instrument{};
+    for (int i = 0; i < 8; ++i) {
+        out->stage_ms[i] = s->stage_ms[i];
+        out->stage_launches[i] = s->stage_launches[i];
+    }
+    if (s->work) {
+        unsigned long long w[4];
+        VR_CK(cudaMemcpy(w, s->work, sizeof w, cudaMemcpyDeviceToHost));
+        out->extend_node_visits = w[0];
+        out->extend_tri_tests = w[1];
+        out->shadow_node_visits = w[2];
+        out->shadow_tri_tests = w[3];
+    }
+    return VR_OK;
+}
+
 vr_status vr_scene_destroy(vr_scene* s) {
     if (!s) return VR_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    if (s->work) cudaFree(s->work);
     free_scratch(s);
     if (s->psum) cudaFree(s->psum);
     if (s->stage_a.p) cudaFree(s->stage_a.p);
@@ -318,6 +392,13 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
     vr::RenderParams rp{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
     auto t0 = std::chrono::steady_clock::now();
     uint64_t waves = 0;
+    const bool nee = st->estimator == VR_EST_NEE;
+    unsigned long long* wk = (s->instr & VR_INSTR_WORK) ? s->work : nullptr;
+    if ((s->instr & VR_INSTR_STAGE_TIMES) && s->events_used > 0) {
+        VR_CK(cudaStreamSynchronize(cs));
+        if ((r = collect_events(s)) != VR_OK) return r;
+    }
+    if ((r = mark(s, -1, cs)) != VR_OK) return r;
     for (uint64_t g0 = 0; g0 < total; g0 += cap) {
         vr::WaveParams wp{};
         wp.g0 = g0;
@@ -327,7 +408,20 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
         wp.width = w;
         wp.height = h;
         wp.first_sample = first_sample;
-        VR_CK(vr::launch_wavefront(s->view, wp, rp, s->ps, s->psum, s->totals, s->status, cs));
+        VR_CK(vr::launch_raygen(s->view, wp, s->ps, cs));
+        if ((r = mark(s, VR_STAGE_RAYGEN, cs)) != VR_OK) return r;
+        for (uint32_t k = 0; k < st->max_bounces; ++k) {
+            VR_CK(vr::launch_extend(s->view, wp, s->ps, k, s->status, wk, cs));
+            if ((r = mark(s, VR_STAGE_EXTEND, cs)) != VR_OK) return r;
+            VR_CK(vr::launch_shade(s->view, wp, rp, s->ps, k, cs));
+            if ((r = mark(s, VR_STAGE_SHADE, cs)) != VR_OK) return r;
+            if (nee) {
+                VR_CK(vr::launch_shadow(s->view, wp, rp, s->ps, k, s->status, wk ? wk + 2 : nullptr, cs));
+                if ((r = mark(s, VR_STAGE_SHADOW, cs)) != VR_OK) return r;
+            }
+        }
+        VR_CK(vr::launch_accumulate(wp, s->ps, rp, s->psum, s->totals, cs));
+        if ((r = mark(s, VR_STAGE_ACCUMULATE, cs)) != VR_OK) return r;
         ++waves;
     }
     VR_CK(vr::launch_finalize(s->psum, reinterpret_cast<float4*>(rgba), np, 1.0f / (float)st->total_samples, cs));

@@ -507,20 +507,41 @@ __global__ void k_raygen(SceneView s, WaveParams w, PathState ps) {
 }
 
 // Closest hit of the live queue of depth k.
-__global__ void __launch_bounds__(128) k_extend(SceneView s, PathState ps, uint32_t k, uint32_t* status) {
+// Warp-reduced work counters (inner-node visits, triangle tests).
+__device__ __forceinline__ void add_work(unsigned long long* work, uint32_t nv, uint32_t nt) {
+    unsigned long long a = nv, b = nt;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(work, a);
+        atomicAdd(work + 1, b);
+    }
+}
+
+// Closest hit of the live queue of depth k.  COUNT adds the traversal work
+// to work[0..1] (a separate, untimed instrumentation launch).
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend(SceneView s, PathState ps, uint32_t k, uint32_t* status,
+                                                unsigned long long* work) {
     const uint32_t n = (k == 0) ? ps.first_count : ps.counts[k];
     const uint32_t base = (k & 1) ? ps.cap : 0;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 ro = ps.q_org[base + i], rd = ps.q_dir[base + i];
-        HitOut h;
-        uint32_t nv = 0, nt = 0;
-        if (!traverse<false, false>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt)) {
-            atomicOr(status, ERRF_STACK);
-            h.prim = MISS;
+    uint32_t nv = 0, nt = 0;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + threadIdx.x;
+        if (i < n) {
+            const float4 ro = ps.q_org[base + i], rd = ps.q_dir[base + i];
+            HitOut h;
+            if (!traverse<false, COUNT>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt)) {
+                atomicOr(status, ERRF_STACK);
+                h.prim = MISS;
+            }
+            ps.hits[i] = pack_hit(h);
         }
-        ps.hits[i] = pack_hit(h);
     }
+    if (COUNT) add_work(work, nv, nt);
 }
 
 // Reference estimator: the path's radiance is the recursion of
@@ -698,21 +719,26 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, WaveParams w, Render
 }
 
 // NEE visibility: adds the (clamped) contribution when nothing is hit.
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_shadow(SceneView s, RenderParams rp, PathState ps, uint32_t k,
-                                                uint32_t* status) {
+                                                uint32_t* status, unsigned long long* work) {
     const uint32_t n = ps.counts[MAX_DEPTH_SLOTS + k];
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 ro = ps.s_org[i], rd = ps.s_dir[i];
-        HitOut h;
-        uint32_t nv = 0, nt = 0;
-        bool ok = traverse<true, false>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt);
-        if (!ok) atomicOr(status, ERRF_STACK);
-        if (ok && h.prim == MISS) {
-            const uint32_t p = ps.s_path[i];
-            rad_add(ps, p, clampc(xyz(ps.s_contrib[i]), rp.firefly_clamp));
+    uint32_t nv = 0, nt = 0;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + threadIdx.x;
+        if (i < n) {
+            const float4 ro = ps.s_org[i], rd = ps.s_dir[i];
+            HitOut h;
+            bool ok = traverse<true, COUNT>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt);
+            if (!ok) atomicOr(status, ERRF_STACK);
+            if (ok && h.prim == MISS) {
+                const uint32_t p = ps.s_path[i];
+                rad_add(ps, p, clampc(xyz(ps.s_contrib[i]), rp.firefly_clamp));
+            }
         }
     }
+    if (COUNT) add_work(work, nv, nt);
 }
 
 // Per-pixel running sum in sample order over this wavefront's paths.
@@ -869,19 +895,39 @@ cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint6
     return cudaGetLastError();
 }
 
-cudaError_t launch_wavefront(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                             float4* psum, unsigned long long* totals, uint32_t* status, cudaStream_t st) {
+cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathState& ps, cudaStream_t st) {
     k_raygen<<<grid_for(w.paths, 256, 8), 256, 0, st>>>(s, w, ps);
-    PathState ps0 = ps;
-    ps0.first_count = w.paths;
-    const bool nee = rp.estimator == 1;
-    for (uint32_t k = 0; k < rp.max_bounces; ++k) {
-        k_extend<<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, ps0, k, status);
-        k_shade<<<grid_for(w.paths, 256, 8), 256, 0, st>>>(s, w, rp, ps0, k);
-        if (nee) k_shadow<<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, rp, ps0, k, status);
-    }
-    k_accumulate<<<grid_for(w.num_pixels, 256, 8), 256, 0, st>>>(w, ps0, psum);
-    if (totals) k_wave_stats<<<1, 32, 0, st>>>(ps0, w.paths, rp.max_bounces, totals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extend(const SceneView& s, const WaveParams& w, const PathState& ps, uint32_t k, uint32_t* status,
+                          unsigned long long* work, cudaStream_t st) {
+    PathState p = ps;
+    p.first_count = w.paths;
+    if (work) k_extend<true><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, p, k, status, work);
+    else k_extend<false><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, p, k, status, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
+                         uint32_t k, cudaStream_t st) {
+    PathState p = ps;
+    p.first_count = w.paths;
+    k_shade<<<grid_for(w.paths, 256, 8), 256, 0, st>>>(s, w, rp, p, k);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
+                          uint32_t k, uint32_t* status, unsigned long long* work, cudaStream_t st) {
+    if (work) k_shadow<true><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, rp, ps, k, status, work);
+    else k_shadow<false><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, rp, ps, k, status, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(const WaveParams& w, const PathState& ps, const RenderParams& rp, float4* psum,
+                              unsigned long long* totals, cudaStream_t st) {
+    k_accumulate<<<grid_for(w.num_pixels, 256, 8), 256, 0, st>>>(w, ps, psum);
+    if (totals) k_wave_stats<<<1, 32, 0, st>>>(ps, w.paths, rp.max_bounces, totals);
     return cudaGetLastError();
 }
 

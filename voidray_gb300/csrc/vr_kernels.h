@@ -52,8 +52,18 @@ cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n,
                              uint32_t* status, cudaStream_t st);
 cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, bool any,
                                    unsigned long long* counters, uint32_t* status, cudaStream_t st);
-cudaError_t launch_wavefront(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                             float4* psum, unsigned long long* totals, uint32_t* status, cudaStream_t st);
+// Wavefront stages, in launch order: raygen, then per depth k extend, shade
+// and (NEE) shadow, then accumulate.  `work` (optional) receives traversal
+// work counters (node visits, triangle tests) of that launch.
+cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathState& ps, cudaStream_t st);
+cudaError_t launch_extend(const SceneView& s, const WaveParams& w, const PathState& ps, uint32_t k, uint32_t* status,
+                          unsigned long long* work, cudaStream_t st);
+cudaError_t launch_shade(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
+                         uint32_t k, cudaStream_t st);
+cudaError_t launch_shadow(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
+                          uint32_t k, uint32_t* status, unsigned long long* work, cudaStream_t st);
+cudaError_t launch_accumulate(const WaveParams& w, const PathState& ps, const RenderParams& rp, float4* psum,
+                              unsigned long long* totals, cudaStream_t st);
 cudaError_t launch_finalize(const float4* psum, float4* rgba, uint32_t np, float inv_total, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, float4* out, uint32_t np, int32_t tonemap, float inv_gamma, float ex,
                            float scale, cudaStream_t st);
