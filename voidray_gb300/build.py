@@ -34,6 +34,8 @@ def nvcc() -> str:
 def _flags(src: str) -> list[str]:
     common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
               "-I", str(CSRC), "-I", str(PKG.parent / "include")]
+    # tuning knobs for sweeps, e.g. VR_NVCC_EXTRA="-DVR_TRACE_MINB=12 -DVR_DYN_FETCH=16" (rebuild with --force)
+    common += os.environ.get("VR_NVCC_EXTRA", "").split()
     if src.endswith(".cu"):
         return ARCH + common + ["-fmad=false", "-Xptxas", "-v" if os.environ.get("VR_PTXAS_VERBOSE") else "-O3"]
     return common + ["-x", "cu"] + ARCH + ["-fmad=false"]

@@ -286,7 +286,7 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
         np += md.num_triangles;
         any_uv = any_uv || md.uvs;
     }
-    if (np >= (1ull << 31)) { err = "too many triangles"; return VR_ERR_INVALID; }
+    if (np >= (1ull << 27)) { err = "too many triangles (the leaf encoding holds 2^27)"; return VR_ERR_INVALID; }
     hs.num_prims = np;
     std::vector<PrimRef> refs(np);
     std::vector<float4> v0e(np * 3);  // v0, e1, e2 by prim id
@@ -400,8 +400,10 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             hs.nodes[4 * f + 0] = make_float4(lo(c0, 0), hi(c0, 0), lo(c0, 1), hi(c0, 1));
             hs.nodes[4 * f + 1] = make_float4(lo(c1, 0), hi(c1, 0), lo(c1, 1), hi(c1, 1));
             hs.nodes[4 * f + 2] = make_float4(lo(c0, 2), hi(c0, 2), lo(c1, 2), hi(c1, 2));
-            int32_t r0 = is_leaf(bn.left) ? (int32_t)c0.first : flat_of[bn.left];
-            int32_t r1 = is_leaf(bn.right) ? (int32_t)c1.first : flat_of[bn.right];
+            // leaf child: ~(first << 4 | count - 1), negative; inner child: its flat index
+            auto leaf_code = [](const BNode& c) { return (int32_t)~((c.first << 4) | (c.count - 1)); };
+            int32_t r0 = is_leaf(bn.left) ? leaf_code(c0) : flat_of[bn.left];
+            int32_t r1 = is_leaf(bn.right) ? leaf_code(c1) : flat_of[bn.right];
             int32_t n0 = is_leaf(bn.left) ? (int32_t)c0.count : 0;
             int32_t n1 = is_leaf(bn.right) ? (int32_t)c1.count : 0;
             float fr0, fr1, fn0, fn1;
@@ -496,9 +498,14 @@ vr_status validate_host_scene(const HostScene& hs, std::string& err) {
             }
             if (cnt[c] > 0) {
                 if (dup_root && c == 1) continue;
-                if (ref[c] < 0 || (uint64_t)ref[c] + cnt[c] > np) { err = "leaf range out of bounds"; return VR_ERR_INVALID; }
+                // leaf code ~(first << 4 | count - 1)
+                if (ref[c] >= 0) { err = "leaf child without a leaf code"; return VR_ERR_INVALID; }
+                const uint32_t code = ~(uint32_t)ref[c];
+                const uint32_t first = code >> 4, count = (code & 15u) + 1u;
+                if ((int32_t)count != cnt[c]) { err = "leaf code and count disagree"; return VR_ERR_INVALID; }
+                if ((uint64_t)first + count > np) { err = "leaf range out of bounds"; return VR_ERR_INVALID; }
                 for (int32_t k = 0; k < cnt[c]; ++k) {
-                    const float4* t = &hs.tris[3 * ((size_t)ref[c] + k)];
+                    const float4* t = &hs.tris[3 * ((size_t)first + k)];
                     uint32_t pid;
                     std::memcpy(&pid, &t[0].w, 4);
                     if (pid >= np) { err = "prim id out of range"; return VR_ERR_INVALID; }

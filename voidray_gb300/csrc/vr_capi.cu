@@ -60,6 +60,7 @@ struct vr_scene {
     vr_scene_info info{};
     vr_render_stats stats{};
     uint32_t* status = nullptr;               // device status word
+    uint32_t* fetch = nullptr;                // ray-fetch cursor of the batch intersection kernel
     unsigned long long* totals = nullptr;     // device: paths, extend, shadow, counters x2
     double* dres = nullptr;                   // device scratch for reductions
     // render scratch
@@ -141,7 +142,7 @@ vr_status ensure_scratch(vr_scene* s, uint32_t cap, uint32_t bounces, bool need_
     SA(s_dir, (size_t)cap);
     SA(s_contrib, (size_t)cap);
     SA(s_path, (size_t)cap);
-    SA(counts, 2 * (size_t)vr::MAX_DEPTH_SLOTS);
+    SA(counts, 4 * (size_t)vr::MAX_DEPTH_SLOTS);
 #undef SA
     ps.cap = cap;
     s->ps_cap = cap;
@@ -255,6 +256,9 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if (cudaMalloc(&p, 64) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "status alloc"));
     s->allocs.push_back(p);
     s->status = static_cast<uint32_t*>(p);
+    if (cudaMalloc(&p, 64) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "fetch alloc"));
+    s->allocs.push_back(p);
+    s->fetch = static_cast<uint32_t*>(p);
     if (cudaMalloc(&p, 8 * sizeof(unsigned long long)) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "totals alloc"));
     s->allocs.push_back(p);
     s->totals = static_cast<unsigned long long*>(p);
@@ -475,8 +479,12 @@ vr_status vr_intersect_device(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hi
         VR_CK(cudaMemsetAsync(hits, 0xFF, n * sizeof(vr_hit), cs));
         return VR_OK;
     }
-    VR_CK(vr::launch_intersect(s->view, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<float4*>(hits),
-                               any_hit != 0, s->status, cs));
+    const uint64_t chunk = 1ull << 30;  // the persistent kernel indexes rays with 32 bits
+    for (uint64_t b = 0; b < n; b += chunk) {
+        const uint64_t m = std::min(chunk, n - b);
+        VR_CK(vr::launch_intersect(s->view, reinterpret_cast<const float4*>(rays + b), m,
+                                   reinterpret_cast<float4*>(hits + b), any_hit != 0, s->fetch, s->status, cs));
+    }
     return VR_OK;
 }
 
@@ -503,11 +511,14 @@ vr_status vr_intersect_count_device(vr_scene* s, const vr_ray* rays, uint64_t n,
     *tri_tests = 0;
     if (n == 0 || s->info.num_triangles == 0) return VR_OK;
     if (!rays) return fail(VR_ERR_INVALID, "null rays");
+    if (n >= (1ull << 31)) return fail(VR_ERR_INVALID, "too many rays for one counting launch");
     cudaStream_t cs = pick(s, stream);
+    vr_status r;
+    if ((r = ensure_buf(s->stage_b, n * sizeof(vr_hit))) != VR_OK) return r;
     unsigned long long* c = s->totals + 4;
     VR_CK(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned long long), cs));
-    VR_CK(vr::launch_intersect_count(s->view, reinterpret_cast<const float4*>(rays), n, any_hit != 0, c, s->status,
-                                     cs));
+    VR_CK(vr::launch_intersect_count(s->view, reinterpret_cast<const float4*>(rays), n,
+                                     static_cast<float4*>(s->stage_b.p), any_hit != 0, s->fetch, c, s->status, cs));
     unsigned long long hc[2];
     VR_CK(cudaMemcpyAsync(hc, c, sizeof hc, cudaMemcpyDeviceToHost, cs));
     VR_CK(cudaStreamSynchronize(cs));

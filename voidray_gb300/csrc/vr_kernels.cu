@@ -22,173 +22,33 @@
 
 #include "vr_device.cuh"
 #include "vr_kernels.h"
+#include "vr_traverse.cuh"
 
 namespace vr {
 
 // ----------------------------------------------------------------------------
 // Traversal
 // ----------------------------------------------------------------------------
-struct HitOut {
-    uint32_t prim;
-    float t, u, v;
+// vr_ray batch -> vr_hit batch
+struct BatchIo {
+    const float4* rays;
+    float4* hits;
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
+        ro = __ldg(rays + 2 * (size_t)i);
+        rd = __ldg(rays + 2 * (size_t)i + 1);
+    }
+    __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
+        HitOut o = h;
+        if (overflow) o.prim = MISS;
+        hits[i] = pack_hit(o);
+    }
 };
 
-// Triangle::hit (mesh.rs:144-188) on a precomputed (v0, e1, e2): same
-// operations in the same order, each rounded separately, so t/u/v are the
-// values the reference computes.  The determinant test uses tmin as an
-// absolute epsilon like the reference; a hit is accepted for tmin < t < best.
-template <bool ANY>
-__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int first, int count, V3 o, V3 d,
-                                          float tmin, float& best, HitOut& h, uint32_t& ntest, bool counting) {
-    for (int k = 0; k < count; ++k) {
-        const float4* tp = tris + 3 * (first + k);
-        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-        if (counting) ntest++;
-        V3 v0 = xyz(a), e1 = xyz(b), e2 = xyz(c);
-        V3 hh = cross(d, e2);
-        float det = dot(e1, hh);
-        if (det > -tmin && det < tmin) continue;
-        float f = 1.0f / det;
-        V3 s = o - v0;
-        float u = f * dot(s, hh);
-        if (u < 0.0f || u > 1.0f) continue;
-        V3 q = cross(s, e1);
-        float v = f * dot(d, q);
-        if (v < 0.0f || u + v > 1.0f) continue;
-        float t = f * dot(e2, q);
-        if (t > tmin && t < best) {
-            best = t;
-            h.prim = __float_as_uint(a.w);
-            h.t = t;
-            h.u = u;
-            h.v = v;
-            if (ANY) return true;
-        }
-    }
-    return false;
-}
-
-// Stack-based BVH2 traversal, nearest child first, far child pushed with its
-// entry distance so that popped nodes beyond the current hit are skipped.
-// Returns false if the stack would overflow (sets ERRF_STACK).
 template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, V3 o,
-                                         V3 d, float tmin, float tmax, HitOut& h, uint32_t& nvisit,
-                                         uint32_t& ntest) {
-    h.prim = MISS;
-    h.t = INF_F;
-    h.u = 0.0f;
-    h.v = 0.0f;
-    if (nodes == nullptr) return true;  // scene without triangles: every ray misses
-    const float eps = 1e-18f;
-    const float ix = 1.0f / (fabsf(d.x) > eps ? d.x : copysignf(eps, d.x));
-    const float iy = 1.0f / (fabsf(d.y) > eps ? d.y : copysignf(eps, d.y));
-    const float iz = 1.0f / (fabsf(d.z) > eps ? d.z : copysignf(eps, d.z));
-    const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
-    int stack_node[STACK_SIZE];
-    float stack_t[STACK_SIZE];
-    int sp = 0;
-    int node = 0;
-    float best = tmax;
-    while (true) {
-        const float4* n = nodes + 4 * node;
-        const float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2);
-        const int4 n3 = __ldg(reinterpret_cast<const int4*>(n) + 3);
-        if (COUNT) nvisit++;
-        const float a0 = fmaf(n0.x, ix, -ox), b0 = fmaf(n0.y, ix, -ox);
-        const float c0 = fmaf(n0.z, iy, -oy), d0 = fmaf(n0.w, iy, -oy);
-        const float e0 = fmaf(n2.x, iz, -oz), f0 = fmaf(n2.y, iz, -oz);
-        const float a1 = fmaf(n1.x, ix, -ox), b1 = fmaf(n1.y, ix, -ox);
-        const float c1 = fmaf(n1.z, iy, -oy), d1 = fmaf(n1.w, iy, -oy);
-        const float e1 = fmaf(n2.z, iz, -oz), f1 = fmaf(n2.w, iz, -oz);
-        const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
-        const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), best));
-        const float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
-        const float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), best));
-        bool hit0 = tn0 <= tf0, hit1 = tn1 <= tf1;
-        if (hit0 && n3.z > 0) {
-            if (leaf_test<ANY>(tris, n3.x, n3.z, o, d, tmin, best, h, ntest, COUNT) && ANY) return true;
-            hit0 = false;
-        }
-        if (hit1 && n3.w > 0) {
-            if (tn1 <= best && leaf_test<ANY>(tris, n3.y, n3.w, o, d, tmin, best, h, ntest, COUNT) && ANY)
-                return true;
-            hit1 = false;
-        }
-        hit1 = hit1 && tn1 <= best;
-        if (hit0 && hit1) {
-            const bool swap = tn1 < tn0;
-            const int nearn = swap ? n3.y : n3.x;
-            const int farn = swap ? n3.x : n3.y;
-            if (sp >= STACK_SIZE) return false;
-            stack_node[sp] = farn;
-            stack_t[sp] = swap ? tn0 : tn1;
-            ++sp;
-            node = nearn;
-        } else if (hit0) {
-            node = n3.x;
-        } else if (hit1) {
-            node = n3.y;
-        } else {
-            bool found = false;
-            while (sp > 0) {
-                --sp;
-                if (stack_t[sp] <= best) {
-                    node = stack_node[sp];
-                    found = true;
-                    break;
-                }
-            }
-            if (!found) return true;
-        }
-    }
-}
-
-__device__ __forceinline__ float4 pack_hit(const HitOut& h) {
-    return make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
-}
-
-template <bool ANY>
-__global__ void __launch_bounds__(128) k_intersect(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                   const float4* __restrict__ rays, uint64_t n,
-                                                   float4* __restrict__ hits, uint32_t* __restrict__ status) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 ro = __ldg(rays + 2 * i), rd = __ldg(rays + 2 * i + 1);
-        HitOut h;
-        uint32_t nv = 0, nt = 0;
-        if (!traverse<ANY, false>(nodes, tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt)) {
-            atomicOr(status, ERRF_STACK);
-            h.prim = MISS;
-        }
-        hits[i] = pack_hit(h);
-    }
-}
-
-template <bool ANY>
-__global__ void __launch_bounds__(128) k_intersect_count(const float4* __restrict__ nodes,
-                                                         const float4* __restrict__ tris,
-                                                         const float4* __restrict__ rays, uint64_t n,
-                                                         unsigned long long* __restrict__ counters,
-                                                         uint32_t* __restrict__ status) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    unsigned long long nv_sum = 0, nt_sum = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 ro = __ldg(rays + 2 * i), rd = __ldg(rays + 2 * i + 1);
-        HitOut h;
-        uint32_t nv = 0, nt = 0;
-        if (!traverse<ANY, true>(nodes, tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt)) atomicOr(status, ERRF_STACK);
-        nv_sum += nv;
-        nt_sum += nt;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        nv_sum += __shfl_down_sync(0xffffffffu, nv_sum, off);
-        nt_sum += __shfl_down_sync(0xffffffffu, nt_sum, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(counters, nv_sum);
-        atomicAdd(counters + 1, nt_sum);
-    }
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_intersect(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                   BatchIo io, uint32_t n, uint32_t* counter, uint32_t* status,
+                                                   unsigned long long* work) {
+    persistent_trace<ANY, COUNT>(nodes, tris, n, counter, io, status, work);
 }
 
 // ----------------------------------------------------------------------------
@@ -469,7 +329,7 @@ __device__ __forceinline__ void path_coords(const WaveParams& w, uint32_t p, uin
 
 __global__ void k_raygen(SceneView s, WaveParams w, PathState ps) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    if (blockIdx.x == 0 && threadIdx.x < MAX_DEPTH_SLOTS * 2) ps.counts[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < MAX_DEPTH_SLOTS * 4) ps.counts[threadIdx.x] = 0;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.paths; p += stride) {
         uint32_t pixel, sample;
         path_coords(w, p, pixel, sample);
@@ -507,41 +367,29 @@ __global__ void k_raygen(SceneView s, WaveParams w, PathState ps) {
 }
 
 // Closest hit of the live queue of depth k.
-// Warp-reduced work counters (inner-node visits, triangle tests).
-__device__ __forceinline__ void add_work(unsigned long long* work, uint32_t nv, uint32_t nt) {
-    unsigned long long a = nv, b = nt;
-    for (int off = 16; off > 0; off >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, off);
-        b += __shfl_down_sync(0xffffffffu, b, off);
+// Closest hit of the live queue of depth k (persistent, dynamic fetch).
+struct ExtendIo {
+    const float4* org;
+    const float4* dir;
+    float4* hits;
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
+        ro = org[i];
+        rd = dir[i];
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(work, a);
-        atomicAdd(work + 1, b);
+    __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
+        HitOut o = h;
+        if (overflow) o.prim = MISS;
+        hits[i] = pack_hit(o);
     }
-}
+};
 
-// Closest hit of the live queue of depth k.  COUNT adds the traversal work
-// to work[0..1] (a separate, untimed instrumentation launch).
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend(SceneView s, PathState ps, uint32_t k, uint32_t* status,
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_extend(SceneView s, PathState ps, uint32_t k, uint32_t* status,
                                                 unsigned long long* work) {
     const uint32_t n = (k == 0) ? ps.first_count : ps.counts[k];
     const uint32_t base = (k & 1) ? ps.cap : 0;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t nv = 0, nt = 0;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-        const uint32_t i = i0 + threadIdx.x;
-        if (i < n) {
-            const float4 ro = ps.q_org[base + i], rd = ps.q_dir[base + i];
-            HitOut h;
-            if (!traverse<false, COUNT>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt)) {
-                atomicOr(status, ERRF_STACK);
-                h.prim = MISS;
-            }
-            ps.hits[i] = pack_hit(h);
-        }
-    }
-    if (COUNT) add_work(work, nv, nt);
+    ExtendIo io{ps.q_org + base, ps.q_dir + base, ps.hits};
+    persistent_trace<false, COUNT>(s.nodes, s.tris, n, &ps.counts[2 * MAX_DEPTH_SLOTS + k], io, status, work);
 }
 
 // Reference estimator: the path's radiance is the recursion of
@@ -718,27 +566,30 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, WaveParams w, Render
     }
 }
 
-// NEE visibility: adds the (clamped) contribution when nothing is hit.
+// NEE visibility: adds the (clamped) contribution when nothing is hit
+// (persistent any-hit traversal).  A stack overflow counts as occluded.
+struct ShadowIo {
+    const float4* org;
+    const float4* dir;
+    const uint32_t* path;
+    const float4* contrib;
+    PathState ps;
+    float fc;
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
+        ro = org[i];
+        rd = dir[i];
+    }
+    __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
+        if (!overflow && h.prim == MISS) rad_add(ps, path[i], clampc(xyz(contrib[i]), fc));
+    }
+};
+
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_shadow(SceneView s, RenderParams rp, PathState ps, uint32_t k,
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(SceneView s, RenderParams rp, PathState ps, uint32_t k,
                                                 uint32_t* status, unsigned long long* work) {
     const uint32_t n = ps.counts[MAX_DEPTH_SLOTS + k];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t nv = 0, nt = 0;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-        const uint32_t i = i0 + threadIdx.x;
-        if (i < n) {
-            const float4 ro = ps.s_org[i], rd = ps.s_dir[i];
-            HitOut h;
-            bool ok = traverse<true, COUNT>(s.nodes, s.tris, xyz(ro), xyz(rd), ro.w, rd.w, h, nv, nt);
-            if (!ok) atomicOr(status, ERRF_STACK);
-            if (ok && h.prim == MISS) {
-                const uint32_t p = ps.s_path[i];
-                rad_add(ps, p, clampc(xyz(ps.s_contrib[i]), rp.firefly_clamp));
-            }
-        }
-    }
-    if (COUNT) add_work(work, nv, nt);
+    ShadowIo io{ps.s_org, ps.s_dir, ps.s_path, ps.s_contrib, ps, rp.firefly_clamp};
+    persistent_trace<true, COUNT>(s.nodes, s.tris, n, &ps.counts[3 * MAX_DEPTH_SLOTS + k], io, status, work);
 }
 
 // Per-pixel running sum in sample order over this wavefront's paths.
@@ -877,22 +728,39 @@ static unsigned grid_for(uint64_t n, int block, int per_sm) {
     return (unsigned)want;
 }
 
-cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
-                             uint32_t* status, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    const unsigned g = grid_for(n, 128, 16);
-    if (any) k_intersect<true><<<g, 128, 0, st>>>(s.nodes, s.tris, rays, n, hits, status);
-    else k_intersect<false><<<g, 128, 0, st>>>(s.nodes, s.tris, rays, n, hits, status);
+// Resident blocks of a persistent kernel: SMs x blocks per SM at its occupancy.
+template <class K>
+static unsigned persistent_grid(K kernel, int block) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm <= 0)
+        per_sm = 4;
+    return (unsigned)(num_sms() * per_sm);
+}
+
+template <bool ANY, bool COUNT>
+static cudaError_t intersect_impl(const SceneView& s, const float4* rays, uint64_t n, float4* hits,
+                                  uint32_t* counter, uint32_t* status, unsigned long long* work, cudaStream_t st) {
+    static unsigned grid = 0;
+    if (!grid) grid = persistent_grid(k_intersect<ANY, COUNT>, 128);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(s.nodes, s.tris, BatchIo{rays, hits}, (uint32_t)n, counter, status,
+                                                   work);
     return cudaGetLastError();
 }
 
-cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, bool any,
-                                   unsigned long long* counters, uint32_t* status, cudaStream_t st) {
+cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
+                             uint32_t* counter, uint32_t* status, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    const unsigned g = grid_for(n, 128, 16);
-    if (any) k_intersect_count<true><<<g, 128, 0, st>>>(s.nodes, s.tris, rays, n, counters, status);
-    else k_intersect_count<false><<<g, 128, 0, st>>>(s.nodes, s.tris, rays, n, counters, status);
-    return cudaGetLastError();
+    return any ? intersect_impl<true, false>(s, rays, n, hits, counter, status, nullptr, st)
+               : intersect_impl<false, false>(s, rays, n, hits, counter, status, nullptr, st);
+}
+
+cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
+                                   uint32_t* counter, unsigned long long* work, uint32_t* status, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    return any ? intersect_impl<true, true>(s, rays, n, hits, counter, status, work, st)
+               : intersect_impl<false, true>(s, rays, n, hits, counter, status, work, st);
 }
 
 cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathState& ps, cudaStream_t st) {
@@ -902,10 +770,16 @@ cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathSta
 
 cudaError_t launch_extend(const SceneView& s, const WaveParams& w, const PathState& ps, uint32_t k, uint32_t* status,
                           unsigned long long* work, cudaStream_t st) {
+    static unsigned g0 = 0, g1 = 0;
     PathState p = ps;
     p.first_count = w.paths;
-    if (work) k_extend<true><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, p, k, status, work);
-    else k_extend<false><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, p, k, status, nullptr);
+    if (work) {
+        if (!g1) g1 = persistent_grid(k_extend<true>, 128);
+        k_extend<true><<<g1, 128, 0, st>>>(s, p, k, status, work);
+    } else {
+        if (!g0) g0 = persistent_grid(k_extend<false>, 128);
+        k_extend<false><<<g0, 128, 0, st>>>(s, p, k, status, nullptr);
+    }
     return cudaGetLastError();
 }
 
@@ -919,8 +793,14 @@ cudaError_t launch_shade(const SceneView& s, const WaveParams& w, const RenderPa
 
 cudaError_t launch_shadow(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
                           uint32_t k, uint32_t* status, unsigned long long* work, cudaStream_t st) {
-    if (work) k_shadow<true><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, rp, ps, k, status, work);
-    else k_shadow<false><<<grid_for(w.paths, 128, 16), 128, 0, st>>>(s, rp, ps, k, status, nullptr);
+    static unsigned g0 = 0, g1 = 0;
+    if (work) {
+        if (!g1) g1 = persistent_grid(k_shadow<true>, 128);
+        k_shadow<true><<<g1, 128, 0, st>>>(s, rp, ps, k, status, work);
+    } else {
+        if (!g0) g0 = persistent_grid(k_shadow<false>, 128);
+        k_shadow<false><<<g0, 128, 0, st>>>(s, rp, ps, k, status, nullptr);
+    }
     return cudaGetLastError();
 }
 

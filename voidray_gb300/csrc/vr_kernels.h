@@ -45,13 +45,16 @@ struct PathState {
     float4* s_dir;
     float4* s_contrib;
     uint32_t* s_path;
-    uint32_t* counts;   // queue sizes: [k] live paths at depth k, [MAX_DEPTH_SLOTS + k] shadow rays
+    uint32_t* counts;   // 4*MAX_DEPTH_SLOTS words: [k] live paths at depth k, [M + k] shadow rays,
+                        // [2M + k] extend fetch cursor, [3M + k] shadow fetch cursor
 };
 
+// Batch closest/any hit; `counter` is a device word the persistent kernel
+// uses as its ray-fetch cursor (reset by the launcher).
 cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
-                             uint32_t* status, cudaStream_t st);
-cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, bool any,
-                                   unsigned long long* counters, uint32_t* status, cudaStream_t st);
+                             uint32_t* counter, uint32_t* status, cudaStream_t st);
+cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
+                                   uint32_t* counter, unsigned long long* work, uint32_t* status, cudaStream_t st);
 // Wavefront stages, in launch order: raygen, then per depth k extend, shade
 // and (NEE) shadow, then accumulate.  `work` (optional) receives traversal
 // work counters (node visits, triangle tests) of that launch.

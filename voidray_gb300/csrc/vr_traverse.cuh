@@ -1,0 +1,228 @@
+// vr_traverse.cuh — BVH2 traversal of the sm_103a kernels (closest and any hit).
+//
+// Node layout (64 bytes, four 128-bit loads):
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (code0, code1, count0, count1); code >= 0: inner node index,
+//        code < 0: leaf ~(first << 4 | count - 1) over the leaf-ordered
+//        triangle array (3 x float4 per triangle: v0 | prim id, e1, e2).
+//
+// Traversal is the persistent "while-while" scheme of Aila & Laine (2009):
+// resident warps pull rays from a queue; each lane walks inner nodes nearest
+// child first and postpones the first leaf it reaches, so that leaves are
+// intersected when every lane of the warp holds one (the triangle tests then
+// run with the whole warp active).  When enough lanes have finished, the warp
+// stores their results and refills them from the queue.  The far child of two
+// hit children is pushed with its entry distance; popped entries beyond the
+// current closest hit are skipped.
+#pragma once
+#include "vr_device.cuh"
+
+namespace vr {
+
+struct HitOut {
+    uint32_t prim;
+    float t, u, v;
+};
+
+#ifndef VR_TRACE_MINB
+#define VR_TRACE_MINB 1  // minimum resident blocks per SM requested from ptxas for the traversal kernels
+#endif
+#ifndef VR_DYN_FETCH
+#define VR_DYN_FETCH 12  // refill a warp's lanes once at least this many have finished
+#endif
+constexpr int SENTINEL = 0x7fffffff;  // "no node": the walk is finished
+constexpr int DYN_FETCH = VR_DYN_FETCH;
+
+// Triangle::hit (mesh.rs:144-188) on the precomputed (v0, e1, e2): the same
+// operations in the same order, each rounded separately (-fmad=false), so
+// t/u/v are the values the reference computes.  The determinant test uses
+// tmin as an absolute epsilon like the reference; a hit is accepted for
+// tmin < t < best.  Returns true on the first accepted hit when ANY.
+template <bool ANY>
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, int first, int count, V3 o, V3 d,
+                                          float tmin, float& best, HitOut& h, uint32_t& ntest, bool counting) {
+    for (int k = 0; k < count; ++k) {
+        const float4* tp = tris + 3 * (first + k);
+        const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (counting) ntest++;
+        const V3 v0 = xyz(a), e1 = xyz(b), e2 = xyz(c);
+        const V3 hh = cross(d, e2);
+        const float det = dot(e1, hh);
+        if (det > -tmin && det < tmin) continue;
+        const float f = 1.0f / det;
+        const V3 s = o - v0;
+        const float u = f * dot(s, hh);
+        if (u < 0.0f || u > 1.0f) continue;
+        const V3 q = cross(s, e1);
+        const float v = f * dot(d, q);
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float t = f * dot(e2, q);
+        if (t > tmin && t < best) {
+            best = t;
+            h.prim = __float_as_uint(a.w);
+            h.t = t;
+            h.u = u;
+            h.v = v;
+            if (ANY) return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ float4 pack_hit(const HitOut& h) {
+    return make_float4(__uint_as_float(h.prim), h.t, h.u, h.v);
+}
+
+// Warp-reduced work counters (inner-node visits, triangle tests).
+__device__ __forceinline__ void add_work(unsigned long long* work, uint32_t nv, uint32_t nt) {
+    unsigned long long a = nv, b = nt;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(work, a);
+        atomicAdd(work + 1, b);
+    }
+}
+
+// Io supplies load(i, ro, rd) and store(i, hit, overflow).  `counter` is the
+// queue's fetch cursor (zero before the launch).  Every lane of the block's
+// warps must call this (warp-uniform control flow at the votes).
+template <bool ANY, bool COUNT, class Io>
+__device__ __forceinline__ void persistent_trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                 uint32_t n, uint32_t* counter, const Io& io, uint32_t* status,
+                                                 unsigned long long* work) {
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    if (nodes == nullptr) {  // scene without triangles: every ray misses
+        const HitOut h{MISS, INF_F, 0.0f, 0.0f};
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) io.store(i, h, false);
+        return;
+    }
+    int stack_node[STACK_SIZE];
+    float stack_t[STACK_SIZE];
+    V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
+    float ix = 0.0f, iy = 0.0f, iz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f, tmin = 0.0f, best = 0.0f;
+    int node = SENTINEL, leaf = 0, sp = 0;
+    HitOut h{MISS, INF_F, 0.0f, 0.0f};
+    uint32_t ray = 0, nv = 0, nt = 0;
+    bool has = false, alive = true, overflow = false;
+
+    auto pop = [&]() -> int {
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= best) return stack_node[sp];
+        }
+        return SENTINEL;
+    };
+
+    while (true) {
+        // finished lanes store their result
+        if (has && node == SENTINEL && leaf >= 0) {
+            if (overflow) atomicOr(status, ERRF_STACK);
+            io.store(ray, h, overflow);
+            has = false;
+        }
+        // and take new rays, one atomic per warp
+        const bool need = alive && !has;
+        const unsigned needm = __ballot_sync(FULL, need);
+        if (needm) {
+            const int leader = __ffs(needm) - 1;
+            uint32_t base = 0;
+            if (lane == (uint32_t)leader) base = atomicAdd(counter, (uint32_t)__popc(needm));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                ray = base + __popc(needm & ((1u << lane) - 1u));
+                if (ray < n) {
+                    float4 ro, rd;
+                    io.load(ray, ro, rd);
+                    o = xyz(ro);
+                    d = xyz(rd);
+                    const float eps = 1e-18f;
+                    ix = 1.0f / (fabsf(rd.x) > eps ? rd.x : copysignf(eps, rd.x));
+                    iy = 1.0f / (fabsf(rd.y) > eps ? rd.y : copysignf(eps, rd.y));
+                    iz = 1.0f / (fabsf(rd.z) > eps ? rd.z : copysignf(eps, rd.z));
+                    ox = ro.x * ix;
+                    oy = ro.y * iy;
+                    oz = ro.z * iz;
+                    tmin = ro.w;
+                    best = rd.w;
+                    node = 0;
+                    leaf = 0;
+                    sp = 0;
+                    overflow = false;
+                    h = HitOut{MISS, INF_F, 0.0f, 0.0f};
+                    has = true;
+                } else {
+                    alive = false;
+                }
+            }
+        }
+        if (!__any_sync(FULL, has)) break;
+
+        do {
+            // inner nodes until every lane in the loop holds a postponed leaf
+            while (node >= 0 && node != SENTINEL) {
+                const float4* np = nodes + 4 * node;
+                const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+                const int4 n3 = __ldg(reinterpret_cast<const int4*>(np) + 3);
+                if (COUNT) nv++;
+                const float a0 = fmaf(n0.x, ix, -ox), b0 = fmaf(n0.y, ix, -ox);
+                const float c0 = fmaf(n0.z, iy, -oy), d0 = fmaf(n0.w, iy, -oy);
+                const float e0 = fmaf(n2.x, iz, -oz), f0 = fmaf(n2.y, iz, -oz);
+                const float a1 = fmaf(n1.x, ix, -ox), b1 = fmaf(n1.y, ix, -ox);
+                const float c1 = fmaf(n1.z, iy, -oy), d1 = fmaf(n1.w, iy, -oy);
+                const float e1 = fmaf(n2.z, iz, -oz), f1 = fmaf(n2.w, iz, -oz);
+                const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
+                const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), best));
+                const float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
+                const float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), best));
+                const bool hit0 = tn0 <= tf0, hit1 = tn1 <= tf1;
+                if (hit0 && hit1) {
+                    const bool swap = tn1 < tn0;
+                    if (sp >= STACK_SIZE) {
+                        overflow = true;
+                        node = SENTINEL;
+                        leaf = 0;
+                        break;
+                    }
+                    stack_node[sp] = swap ? n3.x : n3.y;
+                    stack_t[sp] = swap ? tn0 : tn1;
+                    ++sp;
+                    node = swap ? n3.y : n3.x;
+                } else if (hit0) {
+                    node = n3.x;
+                } else if (hit1) {
+                    node = n3.y;
+                } else {
+                    node = pop();
+                }
+                // postpone the first leaf reached
+                if (node < 0 && leaf >= 0) {
+                    leaf = node;
+                    node = pop();
+                }
+                if (!__any_sync(__activemask(), leaf >= 0)) break;
+            }
+            // intersect the postponed leaf (and any leaf that follows it)
+            while (leaf < 0) {
+                const uint32_t code = ~(uint32_t)leaf;
+                const bool found = leaf_test<ANY>(tris, (int)(code >> 4), (int)(code & 15u) + 1, o, d, tmin, best, h,
+                                                  nt, COUNT);
+                if (ANY && found) {
+                    node = SENTINEL;
+                    leaf = 0;
+                    break;
+                }
+                leaf = node;
+                if (node < 0) node = pop();
+            }
+        } while (__popc(__ballot_sync(FULL, node == SENTINEL)) < DYN_FETCH);
+    }
+    if (COUNT) add_work(work, nv, nt);
+}
+
+}  // namespace vr
