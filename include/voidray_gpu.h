@@ -211,6 +211,26 @@ vr_status vr_render_device(vr_scene* scene, const vr_render_settings* settings,
                            uint32_t height, uint64_t seed, uint32_t first_sample,
                            void* stream);
 
+/* Same render as vr_render_device, for callers that cannot allocate device
+ * memory while they render (inside a CUDA stream capture, a real-time frame
+ * loop with a fixed memory budget, a host callback).  No counterpart in the
+ * reference.  It calls no cudaMalloc/cudaFree: the wavefront scratch (ray
+ * queues, path state, per-pixel sums) lives in one device array of
+ * VR_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads
+ * the library holds until the process exits.  The image must fit in it: 16
+ * bytes per pixel plus room for at least 1024 paths (about 4 Mpixels);
+ * larger images are rejected with VR_ERR_UNSUPPORTED, and the wavefront is
+ * sized to what remains.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the one array, so calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  The scene must
+ * have been created beforehand with vr_scene_create. */
+#define VR_NOALLOC_SCRATCH_BYTES (64u << 20)
+vr_status vr_render_device_noalloc(vr_scene* scene, const vr_render_settings* settings,
+                                   uint32_t samples, float* rgba_device, uint32_t width,
+                                   uint32_t height, uint64_t seed, uint32_t first_sample,
+                                   void* stream);
+
 typedef struct vr_render_stats {
     uint64_t paths;          /* camera paths traced                            */
     uint64_t extend_rays;    /* closest-hit rays                               */

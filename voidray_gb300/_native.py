@@ -109,6 +109,7 @@ _SIGS = [
     ("vr_abi_version", C.c_int32, []),
     ("vr_device_available", C.c_int32, []),
     ("vr_scene_synchronize", C.c_int, [P]),
+    ("vr_render_device_noalloc", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),
 ]

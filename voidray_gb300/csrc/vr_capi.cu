@@ -581,3 +581,125 @@ vr_status vr_relmse_device(const float* a, float sa, const float* ref, float sr,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Render without device allocation (no counterpart in the reference).
+//
+// Callers that cannot call cudaMalloc while they render -- a CUDA stream
+// capture in progress, a real-time frame loop with a fixed memory budget, a
+// host callback -- use vr_render_device_noalloc.  Its wavefront scratch (ray
+// queues, path state, per-pixel sums) lives in this file-scope device array
+// of VR_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
+// until the process exits.  The scene itself is still built, and its memory
+// allocated, by vr_scene_create beforehand.
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VR_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// The array's host-side name is only a stand-in; kernels need its device
+// address, looked up once per device with that device current.
+vr_status noalloc_scratch(void** out) {
+    int dev = 0;
+    VR_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(VR_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(VR_ERR_CUDA, std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return VR_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" {
+
+vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba,
+                                   uint32_t w, uint32_t h, uint64_t seed, uint32_t first_sample, void* stream) {
+    vr_status r = validate_render(s, st, w, h);
+    if (r != VR_OK) return r;
+    if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
+    if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
+    if (samples == 0) return VR_OK;
+    const uint32_t np = w * h;
+    const uint64_t total = (uint64_t)samples * np;
+    const bool need_att = st->estimator == VR_EST_REFERENCE;
+    // fixed layout: pixel sums, queue counters, then the per-path arrays
+    const size_t psum_bytes = align256((size_t)np * sizeof(float4));
+    const size_t counts_bytes = align256(4 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t));
+    const size_t per_path = 10 * sizeof(float4) + sizeof(uint64_t) + 3 * sizeof(uint32_t) +
+                            (need_att ? (size_t)st->max_bounces * 3 * sizeof(float) : 0);
+    const size_t fixed = psum_bytes + counts_bytes + 16 * 256;  // 16 arrays, each rounded up to 256 bytes
+    const uint64_t min_paths = 1024;
+    if (fixed + min_paths * per_path > (size_t)VR_NOALLOC_SCRATCH_BYTES)
+        return fail(VR_ERR_UNSUPPORTED, "image of " + std::to_string(np) + " pixels does not fit the " +
+                                            std::to_string(VR_NOALLOC_SCRATCH_BYTES >> 20) +
+                                            " MiB no-alloc scratch (16 bytes per pixel plus at least 1024 paths)");
+    uint64_t cap = ((size_t)VR_NOALLOC_SCRATCH_BYTES - fixed) / per_path;
+    if (st->wavefront_paths && st->wavefront_paths < cap) cap = st->wavefront_paths;
+    if (cap > total) cap = total;
+    void* base = nullptr;
+    if ((r = noalloc_scratch(&base)) != VR_OK) return r;
+    unsigned char* p = static_cast<unsigned char*>(base);
+    auto carve = [&](size_t bytes) {
+        void* q = p;
+        p += align256(bytes);
+        return q;
+    };
+    float4* psum = static_cast<float4*>(carve((size_t)np * sizeof(float4)));
+    vr::PathState ps{};
+    ps.counts = static_cast<uint32_t*>(carve(4 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t)));
+    ps.q_org = static_cast<float4*>(carve(2 * cap * sizeof(float4)));
+    ps.q_dir = static_cast<float4*>(carve(2 * cap * sizeof(float4)));
+    ps.hits = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.thr = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.rad = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.s_org = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.s_dir = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.s_contrib = static_cast<float4*>(carve(cap * sizeof(float4)));
+    ps.rng = static_cast<uint64_t*>(carve(cap * sizeof(uint64_t)));
+    ps.q_path = static_cast<uint32_t*>(carve(2 * cap * sizeof(uint32_t)));
+    ps.s_path = static_cast<uint32_t*>(carve(cap * sizeof(uint32_t)));
+    ps.att = need_att ? static_cast<float*>(carve((size_t)st->max_bounces * 3 * cap * sizeof(float))) : nullptr;
+    if ((size_t)(p - static_cast<unsigned char*>(base)) > (size_t)VR_NOALLOC_SCRATCH_BYTES)
+        return fail(VR_ERR_INVALID, "no-alloc scratch layout overflow");
+    ps.cap = (uint32_t)cap;
+    cudaStream_t cs = pick(s, stream);
+    // the array keeps the previous call's contents: the pixel sums must start at zero
+    // (queue counters are cleared by each wavefront's ray generation)
+    VR_CK(cudaMemsetAsync(psum, 0, (size_t)np * sizeof(float4), cs));
+    const vr::RenderParams rp{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
+    const bool nee = st->estimator == VR_EST_NEE;
+    for (uint64_t g0 = 0; g0 < total; g0 += cap) {
+        vr::WaveParams wp{};
+        wp.g0 = g0;
+        wp.seed = seed;
+        wp.paths = (uint32_t)std::min<uint64_t>(cap, total - g0);
+        wp.num_pixels = np;
+        wp.width = w;
+        wp.height = h;
+        wp.first_sample = first_sample;
+        VR_CK(vr::launch_raygen(s->view, wp, ps, cs));
+        for (uint32_t k = 0; k < st->max_bounces; ++k) {
+            VR_CK(vr::launch_extend(s->view, wp, ps, k, s->status, nullptr, cs));
+            VR_CK(vr::launch_shade(s->view, wp, rp, ps, k, cs));
+            if (nee) VR_CK(vr::launch_shadow(s->view, wp, rp, ps, k, s->status, nullptr, cs));
+        }
+        VR_CK(vr::launch_accumulate(wp, ps, rp, psum, s->totals, cs));
+    }
+    VR_CK(vr::launch_finalize(psum, reinterpret_cast<float4*>(rgba), np, 1.0f / (float)st->total_samples, cs));
+    return VR_OK;
+}
+
+}  // extern "C"
