@@ -228,8 +228,13 @@ def main():
     w, h, spp = args.width, args.height, args.spp
     npx = w * h
     cst = st.to_c()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: its handle is non-zero, so the library launches on it
+    # and the CUDA events below bracket the kernels (NULL would select the
+    # scene's own stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = C.c_void_p(stream.cuda_stream)
+    assert sh.value, "render stream handle must be non-zero"
     accum = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
     # each rank and step renders its own sample range
     base = rank * (args.warmup + args.steps + 2) * spp
@@ -343,7 +348,7 @@ def main():
                           f"accumulation {npx * 16 / 1e6:.0f} MB",
                     "bvh": {"nodes": int(info.num_nodes), "max_depth": int(info.max_depth),
                             "sah_cost": round(info.sah_cost, 2), "build_s": round(build_s, 2)},
-                    "wavefront_paths": st.wavefront_paths or (1 << 22),
+                    "wavefront_paths": st.wavefront_paths or (1 << 26),
                     "parallelism": f"replicas x{world}, disjoint sample ranges"})
         line = {
             "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,

@@ -379,8 +379,11 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
     cudaStream_t cs = pick(s, stream);
     const uint32_t np = w * h;
     const uint64_t total = (uint64_t)samples * np;
-    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 22);
-    if (cap > (1ull << 26)) cap = 1ull << 26;
+    // default wavefront: 2^26 paths (about 12 GB of path state with the NEE
+    // estimator, 21 GB with the reference estimator at depth 12); deep
+    // bounces then still hold enough rays to fill the GPU
+    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
+    if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
     const bool need_att = st->estimator == VR_EST_REFERENCE;
     if ((r = ensure_scratch(s, (uint32_t)cap, st->max_bounces, need_att)) != VR_OK) return r;
