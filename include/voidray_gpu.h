@@ -231,6 +231,36 @@ vr_status vr_render_device_noalloc(vr_scene* scene, const vr_render_settings* se
                                    uint32_t height, uint64_t seed, uint32_t first_sample,
                                    void* stream);
 
+/* ------------------------------------------------------------- batch -- */
+
+/* Multi-scene rendering (no reference counterpart): many render jobs -- each
+ * a scene with its own settings, image, seed and sample range -- share one
+ * wavefront launch per stage.  Every job owns a segment of the path state and
+ * of each ray queue with its own counters; paths of all jobs are traced by
+ * the same persistent kernels.  A job's image is bit-identical to rendering
+ * it alone with vr_render_device (same sample streams, same per-pixel
+ * summation order). */
+typedef struct vr_render_job {
+    vr_scene* scene;
+    vr_render_settings settings;
+    uint32_t samples;
+    uint32_t width;
+    uint32_t height;
+    uint32_t first_sample;
+    uint64_t seed;
+    float* rgba_device;       /* RGBA f32 accumulation buffer, += like vr_render */
+} vr_render_job;
+
+typedef struct vr_batch vr_batch;
+/* max_wave_paths: paths per wavefront over all jobs (0 = 2^26). */
+vr_status vr_batch_create(uint64_t max_wave_paths, vr_batch** out);
+vr_status vr_batch_destroy(vr_batch* batch);
+/* Enqueues all jobs on `stream` (NULL = legacy default stream); scenes must
+ * live on the batch's device.  Returns before the GPU finishes. */
+vr_status vr_batch_render(vr_batch* batch, const vr_render_job* jobs, uint32_t count, void* stream);
+/* Waits for `stream` and reports kernel-side errors. */
+vr_status vr_batch_synchronize(vr_batch* batch, void* stream);
+
 typedef struct vr_render_stats {
     uint64_t paths;          /* camera paths traced                            */
     uint64_t extend_rays;    /* closest-hit rays                               */
@@ -241,6 +271,8 @@ typedef struct vr_render_stats {
     uint32_t pad_;
 } vr_render_stats;
 vr_status vr_render_stats_get(const vr_scene* scene, vr_render_stats* stats);
+/* Totals over every vr_batch_render call of the batch (synchronises the device). */
+vr_status vr_batch_stats_get(vr_batch* batch, vr_render_stats* stats);
 
 /* Instrumentation (no reference counterpart).  VR_INSTR_STAGE_TIMES brackets
  * every wavefront stage launch with CUDA events on the render stream;

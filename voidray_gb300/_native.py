@@ -69,6 +69,12 @@ class vr_render_settings(C.Structure):
                 ("rr_depth", C.c_uint32), ("wavefront_paths", C.c_uint32)]
 
 
+class vr_render_job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("settings", vr_render_settings), ("samples", C.c_uint32),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("first_sample", C.c_uint32), ("seed", C.c_uint64),
+                ("rgba_device", C.c_void_p)]
+
+
 class vr_color_management(C.Structure):
     _fields_ = [("tonemap", C.c_int32), ("gamma", C.c_float), ("exposure", C.c_float), ("transparent", C.c_int32)]
 
@@ -110,6 +116,11 @@ _SIGS = [
     ("vr_device_available", C.c_int32, []),
     ("vr_scene_synchronize", C.c_int, [P]),
     ("vr_render_device_noalloc", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, P]),
+    ("vr_batch_create", C.c_int, [C.c_uint64, P]),
+    ("vr_batch_destroy", C.c_int, [P]),
+    ("vr_batch_render", C.c_int, [P, P, C.c_uint32, P]),
+    ("vr_batch_synchronize", C.c_int, [P, P]),
+    ("vr_batch_stats_get", C.c_int, [P, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),
 ]

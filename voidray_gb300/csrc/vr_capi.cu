@@ -1,14 +1,17 @@
 // vr_capi.cu — implementation of the C ABI declared in include/voidray_gpu.h.
 //
 // Ownership: a vr_scene owns its device memory and one non-blocking CUDA
-// stream.  Render scratch (path state, ray queues, pixel sums) is allocated
-// lazily per scene and grown when a larger wavefront is requested.  Errors are
-// returned as vr_status with a thread-local message; kernel-side faults that
-// can be detected (traversal stack overflow) are recorded in a per-scene
-// device status word and reported by the next synchronising call.
+// stream; a vr_batch owns the scratch of multi-scene renders.  Render scratch
+// (path state, ray queues, per-job counters and pixel sums) is allocated
+// lazily and grown when a larger wavefront is requested.  Errors are returned
+// as vr_status with a thread-local message; kernel-side faults that can be
+// detected (traversal stack overflow) are recorded in a device status word
+// and reported by the next synchronising call.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -49,6 +52,123 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+vr_status ensure_buf(DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes) return VR_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    VR_CK(cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return VR_OK;
+}
+
+// Wavefront scratch: per-slot path state and queues for `cap` slots, per-job
+// counters, fetch cursors and a device table of Job entries.
+struct Engine {
+    vr::PathState ps{};
+    uint32_t cap = 0, bounces = 0;
+    std::vector<void*> allocs;
+    uint64_t bytes = 0;
+    vr::Job* table = nullptr;  // device Job entries (waves x jobs of one chunk)
+    size_t table_cap = 0;
+
+    void release() {
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        ps = vr::PathState{};
+        cap = bounces = 0;
+        bytes = 0;
+        table = nullptr;
+        table_cap = 0;
+    }
+    template <class T>
+    vr_status alloc(T** out, size_t count) {
+        void* p = nullptr;
+        const size_t b = std::max<size_t>(count * sizeof(T), 16);
+        VR_CK(cudaMalloc(&p, b));
+        allocs.push_back(p);
+        bytes += b;
+        *out = static_cast<T*>(p);
+        return VR_OK;
+    }
+    // (re)allocates for `c` slots and reference-estimator attenuation of depth `b`
+    vr_status ensure(uint32_t c, uint32_t b, cudaStream_t sync_stream) {
+        if (cap >= c && bounces >= b && table) return VR_OK;
+        if (sync_stream) VR_CK(cudaStreamSynchronize(sync_stream));
+        c = std::max(c, cap);
+        b = std::max(b, bounces);
+        release();
+        vr_status st;
+#define EA(field, n)                                  \
+    if ((st = alloc(&ps.field, (n))) != VR_OK) {      \
+        release();                                    \
+        return st;                                    \
+    }
+        EA(q_org, 2 * (size_t)c);
+        EA(q_dir, 2 * (size_t)c);
+        EA(q_path, 2 * (size_t)c);
+        EA(hits, (size_t)c);
+        EA(rng, (size_t)c);
+        EA(thr, (size_t)c);
+        EA(rad, (size_t)c);
+        EA(att, (size_t)std::max<uint32_t>(b, 1) * 3 * c);
+        EA(s_org, (size_t)c);
+        EA(s_dir, (size_t)c);
+        EA(s_contrib, (size_t)c);
+        EA(s_path, (size_t)c);
+        EA(counts, (size_t)vr::MAX_JOBS * vr::JOB_COUNTERS);
+        EA(cursors, 2 * (size_t)vr::MAX_DEPTH_SLOTS);
+#undef EA
+        table_cap = 4096;
+        if ((st = alloc(&table, table_cap)) != VR_OK) {
+            release();
+            return st;
+        }
+        ps.cap = c;
+        cap = c;
+        bounces = b;
+        return VR_OK;
+    }
+};
+
+// Stage-event instrumentation of one scene.
+struct Instr {
+    uint32_t flags = 0;
+    std::vector<cudaEvent_t> events;  // pool, reused across calls
+    std::vector<int> event_stage;     // stage of the launch that ends at events[i] (i >= 1)
+    size_t used = 0;
+    double stage_ms[8] = {0};
+    uint64_t stage_launches[8] = {0};
+    unsigned long long* work = nullptr;  // device: extend visits, tests, shadow visits, tests
+
+    vr_status mark(int stage, cudaStream_t cs) {
+        if (!(flags & VR_INSTR_STAGE_TIMES)) return VR_OK;
+        if (used == events.size()) {
+            cudaEvent_t e;
+            VR_CK(cudaEventCreate(&e));
+            events.push_back(e);
+            event_stage.push_back(-1);
+        }
+        event_stage[used] = stage;
+        VR_CK(cudaEventRecord(events[used], cs));
+        used++;
+        return VR_OK;
+    }
+    // folds recorded events into the per-stage totals (after a synchronisation)
+    vr_status collect() {
+        for (size_t i = 1; i < used; ++i) {
+            const int st = event_stage[i];
+            if (st < 0) continue;
+            float ms = 0.0f;
+            VR_CK(cudaEventElapsedTime(&ms, events[i - 1], events[i]));
+            stage_ms[st] += ms;
+            stage_launches[st] += 1;
+        }
+        used = 0;
+        return VR_OK;
+    }
+};
+
 }  // namespace
 
 struct vr_scene {
@@ -59,27 +179,24 @@ struct vr_scene {
     uint64_t scene_bytes = 0;
     vr_scene_info info{};
     vr_render_stats stats{};
-    uint32_t* status = nullptr;               // device status word
-    uint32_t* fetch = nullptr;                // ray-fetch cursor of the batch intersection kernel
-    unsigned long long* totals = nullptr;     // device: paths, extend, shadow, counters x2
-    double* dres = nullptr;                   // device scratch for reductions
-    // render scratch
-    vr::PathState ps{};
-    uint32_t ps_cap = 0, ps_bounces = 0;
-    std::vector<void*> ps_allocs;
-    uint64_t ps_bytes = 0;
+    uint32_t* status = nullptr;            // device status word
+    uint32_t* fetch = nullptr;             // ray-fetch cursor of the batch intersection kernel
+    unsigned long long* totals = nullptr;  // device: paths, extend, shadow, counters x2
+    Engine eng;                            // render scratch
     float4* psum = nullptr;
     uint32_t psum_cap = 0;
-    // host-call staging
-    DevBuf stage_a, stage_b;
-    // instrumentation
-    uint32_t instr = 0;
-    std::vector<cudaEvent_t> events;   // pool, reused across calls
-    std::vector<int> event_stage;      // stage of the launch that ends at events[i] (i >= 1)
-    size_t events_used = 0;
-    double stage_ms[8] = {0};
-    uint64_t stage_launches[8] = {0};
-    unsigned long long* work = nullptr; // device: extend visits, tests, shadow visits, tests
+    DevBuf stage_a, stage_b;               // host-call staging
+    Instr instr;
+};
+
+struct vr_batch {
+    int device = 0;
+    uint64_t max_wave_paths = 0;
+    Engine eng;
+    DevBuf psum;       // pixel sums of all jobs of a call
+    uint32_t* status = nullptr;
+    unsigned long long* totals = nullptr;
+    vr_render_stats stats{};
 };
 
 namespace {
@@ -98,115 +215,23 @@ vr_status upload(vr_scene* s, const std::vector<T>& v, const T** out) {
     return VR_OK;
 }
 
-void free_scratch(vr_scene* s) {
-    for (void* p : s->ps_allocs) cudaFree(p);
-    s->ps_allocs.clear();
-    s->ps = vr::PathState{};
-    s->ps_cap = 0;
-    s->ps_bounces = 0;
-    s->ps_bytes = 0;
-}
-
-template <class T>
-vr_status scratch_alloc(vr_scene* s, T** out, size_t count) {
-    void* p = nullptr;
-    size_t bytes = count * sizeof(T);
-    VR_CK(cudaMalloc(&p, bytes == 0 ? 16 : bytes));
-    s->ps_allocs.push_back(p);
-    s->ps_bytes += bytes;
-    *out = static_cast<T*>(p);
-    return VR_OK;
-}
-
-vr_status ensure_scratch(vr_scene* s, uint32_t cap, uint32_t bounces, bool need_att) {
-    uint32_t need_b = need_att ? bounces : 0;
-    if (s->ps_cap >= cap && s->ps_bounces >= need_b) return VR_OK;
-    VR_CK(cudaStreamSynchronize(s->stream));
-    free_scratch(s);
-    vr::PathState& ps = s->ps;
-    vr_status st;
-#define SA(field, n)                                            \
-    if ((st = scratch_alloc(s, &ps.field, (n))) != VR_OK) {     \
-        free_scratch(s);                                        \
-        return st;                                              \
-    }
-    SA(q_org, 2 * (size_t)cap);
-    SA(q_dir, 2 * (size_t)cap);
-    SA(q_path, 2 * (size_t)cap);
-    SA(hits, (size_t)cap);
-    SA(rng, (size_t)cap);
-    SA(thr, (size_t)cap);
-    SA(rad, (size_t)cap);
-    SA(att, (size_t)std::max<uint32_t>(need_b, 1) * 3 * cap);
-    SA(s_org, (size_t)cap);
-    SA(s_dir, (size_t)cap);
-    SA(s_contrib, (size_t)cap);
-    SA(s_path, (size_t)cap);
-    SA(counts, 4 * (size_t)vr::MAX_DEPTH_SLOTS);
-#undef SA
-    ps.cap = cap;
-    s->ps_cap = cap;
-    s->ps_bounces = need_b;
-    return VR_OK;
-}
-
-vr_status ensure_buf(DevBuf& b, size_t bytes) {
-    if (b.bytes >= bytes) return VR_OK;
-    if (b.p) cudaFree(b.p);
-    b.p = nullptr;
-    b.bytes = 0;
-    VR_CK(cudaMalloc(&b.p, bytes));
-    b.bytes = bytes;
-    return VR_OK;
-}
-
 cudaStream_t pick(vr_scene* s, void* stream) { return stream ? static_cast<cudaStream_t>(stream) : s->stream; }
 
-vr_status check_status(vr_scene* s) {
+vr_status check_flags(uint32_t* status_dev, vr_render_stats& stats) {
     uint32_t flags = 0;
-    VR_CK(cudaMemcpy(&flags, s->status, 4, cudaMemcpyDeviceToHost));
-    s->stats.error_flags |= flags;
+    VR_CK(cudaMemcpy(&flags, status_dev, 4, cudaMemcpyDeviceToHost));
+    stats.error_flags |= flags;
     if (flags) {
-        VR_CK(cudaMemset(s->status, 0, 4));
+        VR_CK(cudaMemset(status_dev, 0, 4));
         if (flags & vr::ERRF_STACK) return fail(VR_ERR_STACK, "traversal stack overflow in a kernel");
         return fail(VR_ERR_CUDA, "kernel reported error flags " + std::to_string(flags));
     }
     return VR_OK;
 }
+vr_status check_status(vr_scene* s) { return check_flags(s->status, s->stats); }
 
-// Records the event that closes a launch of `stage` (the previous event opened it).
-vr_status mark(vr_scene* s, int stage, cudaStream_t cs) {
-    if (!(s->instr & VR_INSTR_STAGE_TIMES)) return VR_OK;
-    if (s->events_used == s->events.size()) {
-        cudaEvent_t e;
-        VR_CK(cudaEventCreate(&e));
-        s->events.push_back(e);
-        s->event_stage.push_back(-1);
-    }
-    s->event_stage[s->events_used] = stage;
-    VR_CK(cudaEventRecord(s->events[s->events_used], cs));
-    s->events_used++;
-    return VR_OK;
-}
-
-// Folds recorded events into the per-stage totals (after a synchronisation).
-vr_status collect_events(vr_scene* s) {
-    for (size_t i = 1; i < s->events_used; ++i) {
-        int st = s->event_stage[i];
-        if (st < 0) continue;
-        float ms = 0.0f;
-        VR_CK(cudaEventElapsedTime(&ms, s->events[i - 1], s->events[i]));
-        s->stage_ms[st] += ms;
-        s->stage_launches[st] += 1;
-    }
-    s->events_used = 0;
-    return VR_OK;
-}
-
-vr_status validate_render(const vr_scene* scene, const vr_render_settings* st, uint32_t w, uint32_t h) {
-    if (!scene || !st) return fail(VR_ERR_INVALID, "null scene or settings");
-    if (w == 0 || h == 0) return fail(VR_ERR_INVALID, "empty image");
-    if ((uint64_t)w * h >= (1ull << 31)) return fail(VR_ERR_INVALID, "image too large");
+vr_status validate_settings(const vr_render_settings* st) {
+    if (!st) return fail(VR_ERR_INVALID, "null settings");
     if (st->total_samples == 0) return fail(VR_ERR_INVALID, "total_samples must be > 0");
     if (st->max_bounces >= vr::MAX_DEPTH_SLOTS)
         return fail(VR_ERR_UNSUPPORTED, "max_bounces must be below " + std::to_string(vr::MAX_DEPTH_SLOTS));
@@ -214,6 +239,135 @@ vr_status validate_render(const vr_scene* scene, const vr_render_settings* st, u
         return fail(VR_ERR_INVALID, "render_mode");
     if (st->estimator != VR_EST_REFERENCE && st->estimator != VR_EST_NEE) return fail(VR_ERR_INVALID, "estimator");
     return VR_OK;
+}
+
+vr_status validate_render(const vr_scene* scene, const vr_render_settings* st, uint32_t w, uint32_t h) {
+    if (!scene || !st) return fail(VR_ERR_INVALID, "null scene or settings");
+    if (w == 0 || h == 0) return fail(VR_ERR_INVALID, "empty image");
+    if ((uint64_t)w * h >= (1ull << 31)) return fail(VR_ERR_INVALID, "image too large");
+    return validate_settings(st);
+}
+
+// One render job on the host side of the wave planner.
+struct HostJob {
+    vr::Job tmpl;      // view, rp, seed, num_pixels, width, height, first_sample, psum
+    uint64_t total;    // paths = samples * pixels
+    uint64_t done = 0;
+    float4* rgba;
+    float inv_total;
+};
+
+// Plans waves of at most `cap` slots over the jobs (each wave takes, in job
+// order, as many of every unfinished job's next paths as fit), uploads the
+// Job entries of up to `table_cap` entries at a time, and launches the stage
+// sequence of every wave.  A job whose last paths ran in a wave is finalised
+// right after it.  `instr` (optional) brackets every launch with events.
+vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_t cap, vr::Job* table,
+                    size_t table_cap, uint32_t* status, unsigned long long* totals, Instr* instr, cudaStream_t cs,
+                    uint64_t* waves_out) {
+    vr_status r;
+    unsigned long long* wk = (instr && (instr->flags & VR_INSTR_WORK)) ? instr->work : nullptr;
+    if (instr && (instr->flags & VR_INSTR_STAGE_TIMES) && instr->used > 0) {
+        VR_CK(cudaStreamSynchronize(cs));
+        if ((r = instr->collect()) != VR_OK) return r;
+    }
+    if (instr && (r = instr->mark(-1, cs)) != VR_OK) return r;
+    uint64_t waves = 0;
+    std::vector<vr::Job> chunk;
+    struct WaveHost {
+        size_t first, njobs;
+        uint32_t total, max_bounces, max_pixels;
+        bool any_nee;
+        std::vector<size_t> finishing;
+    };
+    std::vector<WaveHost> plan;
+    auto pending = [&]() {
+        for (const HostJob& j : jobs)
+            if (j.done < j.total) return true;
+        return false;
+    };
+    std::vector<size_t> entry_job;  // job index of every chunk entry
+    while (pending()) {
+        // plan a chunk of waves whose entries fit the device table
+        chunk.clear();
+        entry_job.clear();
+        plan.clear();
+        while (pending()) {
+            WaveHost wh{chunk.size(), 0, 0, 0, 0, false, {}};
+            uint32_t left = cap;
+            for (size_t i = 0; i < jobs.size() && left > 0 && wh.njobs < vr::MAX_JOBS; ++i) {
+                HostJob& j = jobs[i];
+                if (j.done >= j.total) continue;
+                const uint32_t take = (uint32_t)std::min<uint64_t>(left, j.total - j.done);
+                vr::Job e = j.tmpl;
+                e.g0 = j.done;
+                e.paths = take;
+                e.base = cap - left;
+                chunk.push_back(e);
+                entry_job.push_back(i);
+                wh.njobs++;
+                wh.total += take;
+                wh.max_bounces = std::max(wh.max_bounces, e.rp.max_bounces);
+                wh.max_pixels = std::max(wh.max_pixels, e.num_pixels);
+                wh.any_nee = wh.any_nee || e.rp.estimator == VR_EST_NEE;
+                left -= take;
+                j.done += take;
+                if (j.done == j.total) wh.finishing.push_back(i);
+            }
+            if (chunk.size() > table_cap) {  // does not fit this chunk: undo and run what is planned
+                for (size_t k = wh.first; k < chunk.size(); ++k) jobs[entry_job[k]].done -= chunk[k].paths;
+                chunk.resize(wh.first);
+                entry_job.resize(wh.first);
+                break;
+            }
+            plan.push_back(std::move(wh));
+        }
+        if (plan.empty()) return fail(VR_ERR_INVALID, "wave table too small for one wave");
+        // pageable host -> device: the host vector may be reused once the call returns
+        VR_CK(cudaMemcpyAsync(table, chunk.data(), chunk.size() * sizeof(vr::Job), cudaMemcpyHostToDevice, cs));
+        for (const WaveHost& wh : plan) {
+            const vr::Wave wv{table + wh.first, (uint32_t)wh.njobs, wh.total, wh.max_bounces, wh.any_nee ? 1u : 0u,
+                              chunk[wh.first]};
+            VR_CK(vr::launch_raygen(wv, ps, cs));
+            if (instr && (r = instr->mark(VR_STAGE_RAYGEN, cs)) != VR_OK) return r;
+            for (uint32_t k = 0; k < wv.max_bounces; ++k) {
+                VR_CK(vr::launch_extend(wv, ps, k, status, wk, cs));
+                if (instr && (r = instr->mark(VR_STAGE_EXTEND, cs)) != VR_OK) return r;
+                VR_CK(vr::launch_shade(wv, ps, k, cs));
+                if (instr && (r = instr->mark(VR_STAGE_SHADE, cs)) != VR_OK) return r;
+                if (wv.any_nee) {
+                    VR_CK(vr::launch_shadow(wv, ps, k, status, wk ? wk + 2 : nullptr, cs));
+                    if (instr && (r = instr->mark(VR_STAGE_SHADOW, cs)) != VR_OK) return r;
+                }
+            }
+            VR_CK(vr::launch_accumulate(wv, ps, wh.max_pixels, totals, cs));
+            if (instr && (r = instr->mark(VR_STAGE_ACCUMULATE, cs)) != VR_OK) return r;
+            for (size_t i : wh.finishing) {
+                const HostJob& j = jobs[i];
+                VR_CK(vr::launch_finalize(j.tmpl.psum, j.rgba, j.tmpl.num_pixels, j.inv_total, cs));
+            }
+            ++waves;
+        }
+    }
+    if (waves_out) *waves_out += waves;
+    return VR_OK;
+}
+
+HostJob make_job(const vr::SceneView& view, const vr_render_settings* st, uint32_t samples, float* rgba, uint32_t w,
+                 uint32_t h, uint64_t seed, uint32_t first_sample, float4* psum) {
+    HostJob j{};
+    j.tmpl.view = view;
+    j.tmpl.rp = vr::RenderParams{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
+    j.tmpl.seed = seed;
+    j.tmpl.num_pixels = w * h;
+    j.tmpl.width = w;
+    j.tmpl.height = h;
+    j.tmpl.first_sample = first_sample;
+    j.tmpl.psum = psum;
+    j.total = (uint64_t)samples * w * h;
+    j.rgba = reinterpret_cast<float4*>(rgba);
+    j.inv_total = 1.0f / (float)st->total_samples;
+    return j;
 }
 
 }  // namespace
@@ -262,9 +416,6 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if (cudaMalloc(&p, 8 * sizeof(unsigned long long)) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "totals alloc"));
     s->allocs.push_back(p);
     s->totals = static_cast<unsigned long long*>(p);
-    if (cudaMalloc(&p, 8 * sizeof(double)) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "result alloc"));
-    s->allocs.push_back(p);
-    s->dres = static_cast<double*>(p);
     if (cudaMemset(s->status, 0, 64) != cudaSuccess || cudaMemset(s->totals, 0, 64) != cudaSuccess)
         return cleanup(fail(VR_ERR_CUDA, "memset"));
     s->info.num_triangles = hs.num_prims;
@@ -275,56 +426,6 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     s->info.sah_cost = hs.sah_cost;
     s->info.build_ms = hs.build_ms;
     *out = s;
-    return VR_OK;
-}
-
-vr_status vr_scene_instrument(vr_scene* s, uint32_t flags) {
-    if (!s) return fail(VR_ERR_INVALID, "null scene");
-    VR_CK(cudaStreamSynchronize(s->stream));
-    if (!s->work) VR_CK(cudaMalloc(&s->work, 4 * sizeof(unsigned long long)));
-    VR_CK(cudaMemset(s->work, 0, 4 * sizeof(unsigned long long)));
-    s->instr = flags;
-    s->events_used = 0;
-    for (int i = 0; i < 8; ++i) {
-        s->stage_ms[i] = 0.0;
-        s->stage_launches[i] = 0;
-    }
-    return VR_OK;
-}
-
-vr_status vr_scene_instrument_get(vr_scene* s, vr_instrument* out) {
-    if (!s || !out) return fail(VR_ERR_INVALID, "null argument");
-    VR_CK(cudaDeviceSynchronize());
-    vr_status r = collect_events(s);
-    if (r != VR_OK) return r;
-    *out = vr_instrument{};
-    for (int i = 0; i < 8; ++i) {
-        out->stage_ms[i] = s->stage_ms[i];
-        out->stage_launches[i] = s->stage_launches[i];
-    }
-    if (s->work) {
-        unsigned long long w[4];
-        VR_CK(cudaMemcpy(w, s->work, sizeof w, cudaMemcpyDeviceToHost));
-        out->extend_node_visits = w[0];
-        out->extend_tri_tests = w[1];
-        out->shadow_node_visits = w[2];
-        out->shadow_tri_tests = w[3];
-    }
-    return VR_OK;
-}
-
-vr_status vr_scene_destroy(vr_scene* s) {
-    if (!s) return VR_OK;
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
-    if (s->work) cudaFree(s->work);
-    free_scratch(s);
-    if (s->psum) cudaFree(s->psum);
-    if (s->stage_a.p) cudaFree(s->stage_a.p);
-    if (s->stage_b.p) cudaFree(s->stage_b.p);
-    for (void* p : s->allocs) cudaFree(p);
-    if (s->stream) cudaStreamDestroy(s->stream);
-    delete s;
     return VR_OK;
 }
 
@@ -347,6 +448,56 @@ vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
         info->sah_cost = hs.sah_cost;
         info->build_ms = hs.build_ms;
     }
+    return VR_OK;
+}
+
+vr_status vr_scene_instrument(vr_scene* s, uint32_t flags) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    VR_CK(cudaStreamSynchronize(s->stream));
+    if (!s->instr.work) VR_CK(cudaMalloc(&s->instr.work, 4 * sizeof(unsigned long long)));
+    VR_CK(cudaMemset(s->instr.work, 0, 4 * sizeof(unsigned long long)));
+    s->instr.flags = flags;
+    s->instr.used = 0;
+    for (int i = 0; i < 8; ++i) {
+        s->instr.stage_ms[i] = 0.0;
+        s->instr.stage_launches[i] = 0;
+    }
+    return VR_OK;
+}
+
+vr_status vr_scene_instrument_get(vr_scene* s, vr_instrument* out) {
+    if (!s || !out) return fail(VR_ERR_INVALID, "null argument");
+    VR_CK(cudaDeviceSynchronize());
+    vr_status r = s->instr.collect();
+    if (r != VR_OK) return r;
+    *out = vr_instrument{};
+    for (int i = 0; i < 8; ++i) {
+        out->stage_ms[i] = s->instr.stage_ms[i];
+        out->stage_launches[i] = s->instr.stage_launches[i];
+    }
+    if (s->instr.work) {
+        unsigned long long w[4];
+        VR_CK(cudaMemcpy(w, s->instr.work, sizeof w, cudaMemcpyDeviceToHost));
+        out->extend_node_visits = w[0];
+        out->extend_tri_tests = w[1];
+        out->shadow_node_visits = w[2];
+        out->shadow_tri_tests = w[3];
+    }
+    return VR_OK;
+}
+
+vr_status vr_scene_destroy(vr_scene* s) {
+    if (!s) return VR_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (cudaEvent_t e : s->instr.events) cudaEventDestroy(e);
+    if (s->instr.work) cudaFree(s->instr.work);
+    s->eng.release();
+    if (s->psum) cudaFree(s->psum);
+    if (s->stage_a.p) cudaFree(s->stage_a.p);
+    if (s->stage_b.p) cudaFree(s->stage_b.p);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
     return VR_OK;
 }
 
@@ -385,8 +536,8 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
     uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
     if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
-    const bool need_att = st->estimator == VR_EST_REFERENCE;
-    if ((r = ensure_scratch(s, (uint32_t)cap, st->max_bounces, need_att)) != VR_OK) return r;
+    const uint32_t att_depth = st->estimator == VR_EST_REFERENCE ? st->max_bounces : 0;
+    if ((r = s->eng.ensure((uint32_t)cap, att_depth, s->stream)) != VR_OK) return r;
     if (s->psum_cap < np) {
         VR_CK(cudaStreamSynchronize(s->stream));
         if (s->psum) cudaFree(s->psum);
@@ -396,43 +547,11 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
         s->psum_cap = np;
     }
     VR_CK(cudaMemsetAsync(s->psum, 0, (size_t)np * sizeof(float4), cs));
-    vr::RenderParams rp{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
+    std::vector<HostJob> jobs{make_job(s->view, st, samples, rgba, w, h, seed, first_sample, s->psum)};
     auto t0 = std::chrono::steady_clock::now();
-    uint64_t waves = 0;
-    const bool nee = st->estimator == VR_EST_NEE;
-    unsigned long long* wk = (s->instr & VR_INSTR_WORK) ? s->work : nullptr;
-    if ((s->instr & VR_INSTR_STAGE_TIMES) && s->events_used > 0) {
-        VR_CK(cudaStreamSynchronize(cs));
-        if ((r = collect_events(s)) != VR_OK) return r;
-    }
-    if ((r = mark(s, -1, cs)) != VR_OK) return r;
-    for (uint64_t g0 = 0; g0 < total; g0 += cap) {
-        vr::WaveParams wp{};
-        wp.g0 = g0;
-        wp.seed = seed;
-        wp.paths = (uint32_t)std::min<uint64_t>(cap, total - g0);
-        wp.num_pixels = np;
-        wp.width = w;
-        wp.height = h;
-        wp.first_sample = first_sample;
-        VR_CK(vr::launch_raygen(s->view, wp, s->ps, cs));
-        if ((r = mark(s, VR_STAGE_RAYGEN, cs)) != VR_OK) return r;
-        for (uint32_t k = 0; k < st->max_bounces; ++k) {
-            VR_CK(vr::launch_extend(s->view, wp, s->ps, k, s->status, wk, cs));
-            if ((r = mark(s, VR_STAGE_EXTEND, cs)) != VR_OK) return r;
-            VR_CK(vr::launch_shade(s->view, wp, rp, s->ps, k, cs));
-            if ((r = mark(s, VR_STAGE_SHADE, cs)) != VR_OK) return r;
-            if (nee) {
-                VR_CK(vr::launch_shadow(s->view, wp, rp, s->ps, k, s->status, wk ? wk + 2 : nullptr, cs));
-                if ((r = mark(s, VR_STAGE_SHADOW, cs)) != VR_OK) return r;
-            }
-        }
-        VR_CK(vr::launch_accumulate(wp, s->ps, rp, s->psum, s->totals, cs));
-        if ((r = mark(s, VR_STAGE_ACCUMULATE, cs)) != VR_OK) return r;
-        ++waves;
-    }
-    VR_CK(vr::launch_finalize(s->psum, reinterpret_cast<float4*>(rgba), np, 1.0f / (float)st->total_samples, cs));
-    s->stats.wavefronts += waves;
+    if ((r = run_waves(jobs, s->eng.ps, (uint32_t)cap, s->eng.table, s->eng.table_cap, s->status, s->totals, &s->instr,
+                       cs, &s->stats.wavefronts)) != VR_OK)
+        return r;
     s->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return VR_OK;
 }
@@ -470,6 +589,109 @@ vr_status vr_render_stats_get(const vr_scene* cs, vr_render_stats* out) {
     out->error_flags |= flags;
     return VR_OK;
 }
+
+// ------------------------------------------------------------------ batch --
+
+vr_status vr_batch_create(uint64_t max_wave_paths, vr_batch** out) {
+    if (!out) return fail(VR_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    vr_batch* b = new vr_batch();
+    cudaGetDevice(&b->device);
+    b->max_wave_paths = max_wave_paths ? std::min<uint64_t>(max_wave_paths, 1ull << 28) : (1ull << 26);
+    void* p = nullptr;
+    if (cudaMalloc(&p, 64) != cudaSuccess) {
+        delete b;
+        return fail(VR_ERR_OOM, "status alloc");
+    }
+    b->status = static_cast<uint32_t*>(p);
+    if (cudaMalloc(&p, 64) != cudaSuccess) {
+        cudaFree(b->status);
+        delete b;
+        return fail(VR_ERR_OOM, "totals alloc");
+    }
+    b->totals = static_cast<unsigned long long*>(p);
+    cudaMemset(b->status, 0, 64);
+    cudaMemset(b->totals, 0, 64);
+    *out = b;
+    return VR_OK;
+}
+
+vr_status vr_batch_destroy(vr_batch* b) {
+    if (!b) return VR_OK;
+    cudaDeviceSynchronize();
+    b->eng.release();
+    if (b->psum.p) cudaFree(b->psum.p);
+    if (b->status) cudaFree(b->status);
+    if (b->totals) cudaFree(b->totals);
+    delete b;
+    return VR_OK;
+}
+
+vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count, void* stream) {
+    if (!b) return fail(VR_ERR_INVALID, "null batch");
+    if (count && !jobs) return fail(VR_ERR_INVALID, "null jobs");
+    vr_status r;
+    uint64_t total = 0, pixels = 0;
+    uint32_t att_depth = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const vr_render_job& j = jobs[i];
+        if ((r = validate_render(j.scene, &j.settings, j.width, j.height)) != VR_OK)
+            return fail(r, "job " + std::to_string(i) + ": " + g_err);
+        if (!j.rgba_device) return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": rgba is NULL");
+        if ((uint64_t)j.first_sample + j.samples >= (1ull << 31))
+            return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": sample index out of range");
+        if (j.scene->device != b->device) return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": other device");
+        total += (uint64_t)j.samples * j.width * j.height;
+        pixels += (uint64_t)j.width * j.height;
+        if (j.settings.estimator == VR_EST_REFERENCE) att_depth = std::max(att_depth, j.settings.max_bounces);
+    }
+    if (total == 0) return VR_OK;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    const uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
+    if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs)) != VR_OK) return r;
+    if (b->psum.bytes < pixels * sizeof(float4)) {
+        VR_CK(cudaStreamSynchronize(cs));
+        if ((r = ensure_buf(b->psum, pixels * sizeof(float4))) != VR_OK) return r;
+    }
+    VR_CK(cudaMemsetAsync(b->psum.p, 0, pixels * sizeof(float4), cs));
+    std::vector<HostJob> hj;
+    hj.reserve(count);
+    float4* ps = static_cast<float4*>(b->psum.p);
+    for (uint32_t i = 0; i < count; ++i) {
+        const vr_render_job& j = jobs[i];
+        if (j.samples == 0) continue;
+        hj.push_back(make_job(j.scene->view, &j.settings, j.samples, j.rgba_device, j.width, j.height, j.seed,
+                              j.first_sample, ps));
+        ps += (size_t)j.width * j.height;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    if ((r = run_waves(hj, b->eng.ps, (uint32_t)cap, b->eng.table, b->eng.table_cap, b->status, b->totals, nullptr, cs,
+                       &b->stats.wavefronts)) != VR_OK)
+        return r;
+    b->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return VR_OK;
+}
+
+vr_status vr_batch_synchronize(vr_batch* b, void* stream) {
+    if (!b) return fail(VR_ERR_INVALID, "null batch");
+    VR_CK(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    return check_flags(b->status, b->stats);
+}
+
+vr_status vr_batch_stats_get(vr_batch* b, vr_render_stats* out) {
+    if (!b || !out) return fail(VR_ERR_INVALID, "null argument");
+    VR_CK(cudaDeviceSynchronize());
+    unsigned long long t[3] = {0, 0, 0};
+    VR_CK(cudaMemcpy(t, b->totals, sizeof t, cudaMemcpyDeviceToHost));
+    *out = b->stats;
+    out->paths = t[0];
+    out->extend_rays = t[1];
+    out->shadow_rays = t[2];
+    return VR_OK;
+}
+
+// -------------------------------------------------------------- intersect --
 
 vr_status vr_intersect_device(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hit* hits, int32_t any_hit,
                               void* stream) {
@@ -529,6 +751,8 @@ vr_status vr_intersect_count_device(vr_scene* s, const vr_ray* rays, uint64_t n,
     *tri_tests = hc[1];
     return check_status(s);
 }
+
+// ---------------------------------------------------------------- colour --
 
 vr_status vr_tonemap_device(const float* in, float* out, uint32_t w, uint32_t h, const vr_color_management* cm,
                             float scale, void* stream) {
@@ -638,12 +862,15 @@ vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, ui
     const uint32_t np = w * h;
     const uint64_t total = (uint64_t)samples * np;
     const bool need_att = st->estimator == VR_EST_REFERENCE;
-    // fixed layout: pixel sums, queue counters, then the per-path arrays
+    // fixed layout: pixel sums, counters, wave table, then the per-path arrays
+    const size_t table_entries = 2048;
     const size_t psum_bytes = align256((size_t)np * sizeof(float4));
-    const size_t counts_bytes = align256(4 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t));
+    const size_t counts_bytes = align256((size_t)vr::MAX_JOBS * vr::JOB_COUNTERS * sizeof(uint32_t)) +
+                                align256(2 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t));
+    const size_t table_bytes = align256(table_entries * sizeof(vr::Job));
     const size_t per_path = 10 * sizeof(float4) + sizeof(uint64_t) + 3 * sizeof(uint32_t) +
                             (need_att ? (size_t)st->max_bounces * 3 * sizeof(float) : 0);
-    const size_t fixed = psum_bytes + counts_bytes + 16 * 256;  // 16 arrays, each rounded up to 256 bytes
+    const size_t fixed = psum_bytes + counts_bytes + table_bytes + 16 * 256;  // 16 arrays rounded up to 256 bytes
     const uint64_t min_paths = 1024;
     if (fixed + min_paths * per_path > (size_t)VR_NOALLOC_SCRATCH_BYTES)
         return fail(VR_ERR_UNSUPPORTED, "image of " + std::to_string(np) + " pixels does not fit the " +
@@ -662,7 +889,9 @@ vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, ui
     };
     float4* psum = static_cast<float4*>(carve((size_t)np * sizeof(float4)));
     vr::PathState ps{};
-    ps.counts = static_cast<uint32_t*>(carve(4 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t)));
+    ps.counts = static_cast<uint32_t*>(carve((size_t)vr::MAX_JOBS * vr::JOB_COUNTERS * sizeof(uint32_t)));
+    ps.cursors = static_cast<uint32_t*>(carve(2 * (size_t)vr::MAX_DEPTH_SLOTS * sizeof(uint32_t)));
+    vr::Job* table = static_cast<vr::Job*>(carve(table_entries * sizeof(vr::Job)));
     ps.q_org = static_cast<float4*>(carve(2 * cap * sizeof(float4)));
     ps.q_dir = static_cast<float4*>(carve(2 * cap * sizeof(float4)));
     ps.hits = static_cast<float4*>(carve(cap * sizeof(float4)));
@@ -679,30 +908,11 @@ vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, ui
         return fail(VR_ERR_INVALID, "no-alloc scratch layout overflow");
     ps.cap = (uint32_t)cap;
     cudaStream_t cs = pick(s, stream);
-    // the array keeps the previous call's contents: the pixel sums must start at zero
-    // (queue counters are cleared by each wavefront's ray generation)
+    // the array keeps the previous call's contents: the pixel sums must start
+    // at zero (queue counters are cleared at the start of every wavefront)
     VR_CK(cudaMemsetAsync(psum, 0, (size_t)np * sizeof(float4), cs));
-    const vr::RenderParams rp{st->firefly_clamp, st->max_bounces, st->render_mode, st->estimator, st->rr_depth};
-    const bool nee = st->estimator == VR_EST_NEE;
-    for (uint64_t g0 = 0; g0 < total; g0 += cap) {
-        vr::WaveParams wp{};
-        wp.g0 = g0;
-        wp.seed = seed;
-        wp.paths = (uint32_t)std::min<uint64_t>(cap, total - g0);
-        wp.num_pixels = np;
-        wp.width = w;
-        wp.height = h;
-        wp.first_sample = first_sample;
-        VR_CK(vr::launch_raygen(s->view, wp, ps, cs));
-        for (uint32_t k = 0; k < st->max_bounces; ++k) {
-            VR_CK(vr::launch_extend(s->view, wp, ps, k, s->status, nullptr, cs));
-            VR_CK(vr::launch_shade(s->view, wp, rp, ps, k, cs));
-            if (nee) VR_CK(vr::launch_shadow(s->view, wp, rp, ps, k, s->status, nullptr, cs));
-        }
-        VR_CK(vr::launch_accumulate(wp, ps, rp, psum, s->totals, cs));
-    }
-    VR_CK(vr::launch_finalize(psum, reinterpret_cast<float4*>(rgba), np, 1.0f / (float)st->total_samples, cs));
-    return VR_OK;
+    std::vector<HostJob> jobs{make_job(s->view, st, samples, rgba, w, h, seed, first_sample, psum)};
+    return run_waves(jobs, ps, (uint32_t)cap, table, table_entries, s->status, s->totals, nullptr, cs, nullptr);
 }
 
 }  // extern "C"

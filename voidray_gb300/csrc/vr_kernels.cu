@@ -33,9 +33,13 @@ namespace vr {
 struct BatchIo {
     const float4* rays;
     float4* hits;
-    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
+    const float4* nodes;
+    const float4* tris;
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd, const float4*& n, const float4*& t) const {
         ro = __ldg(rays + 2 * (size_t)i);
         rd = __ldg(rays + 2 * (size_t)i + 1);
+        n = nodes;
+        t = tris;
     }
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
         HitOut o = h;
@@ -45,10 +49,9 @@ struct BatchIo {
 };
 
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_intersect(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                   BatchIo io, uint32_t n, uint32_t* counter, uint32_t* status,
-                                                   unsigned long long* work) {
-    persistent_trace<ANY, COUNT>(nodes, tris, n, counter, io, status, work);
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_intersect(BatchIo io, uint32_t n, uint32_t* counter,
+                                                                  uint32_t* status, unsigned long long* work) {
+    persistent_trace<ANY, COUNT>(n, counter, io, status, work);
 }
 
 // ----------------------------------------------------------------------------
@@ -319,29 +322,88 @@ __device__ bool scatter(const Material& m, V3 ro, V3 rd, const SurfHit& hit, Rng
 // ----------------------------------------------------------------------------
 // Wavefront stages
 // ----------------------------------------------------------------------------
-// Path index p of a wavefront maps to global sample-major index g = g0 + p,
-// pixel = g % NP, sample = first_sample + g / NP.
-__device__ __forceinline__ void path_coords(const WaveParams& w, uint32_t p, uint32_t& pixel, uint32_t& sample) {
-    uint64_t g = w.g0 + p;
-    pixel = (uint32_t)(g % w.num_pixels);
-    sample = w.first_sample + (uint32_t)(g / w.num_pixels);
+// ----------------------------------------------------------------------------
+// Jobs.  A wavefront holds the paths of one or more render jobs (scenes with
+// their own settings, image and sample range).  Job r owns the slots
+// [base, base + paths) of every per-path array and of each ray queue half;
+// its queue sizes live in its own counters, counts[r * JOB_COUNTERS + ...].
+// Path slot p of job r is its global sample-major path g = g0 + (p - base):
+// pixel = g % num_pixels, sample = first_sample + g / num_pixels.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void path_coords(const Job& j, uint32_t p, uint32_t& pixel, uint32_t& sample) {
+    const uint64_t g = j.g0 + (p - j.base);
+    pixel = (uint32_t)(g % j.num_pixels);
+    sample = j.first_sample + (uint32_t)(g / j.num_pixels);
 }
 
-__global__ void k_raygen(SceneView s, WaveParams w, PathState ps) {
+// Block-wide exclusive prefix over the jobs of one per-job counter into
+// shared memory: pre[r] = sum of counter over jobs < r, pre[njobs] = total.
+__device__ __forceinline__ void job_prefix(const uint32_t* counts, uint32_t which, uint32_t njobs, uint32_t* pre) {
+    if (threadIdx.x < 32) {
+        const uint32_t lane = threadIdx.x;
+        uint32_t carry = 0;
+        for (uint32_t r0 = 0; r0 < njobs; r0 += 32) {
+            const uint32_t r = r0 + lane;
+            const uint32_t v = (r < njobs) ? counts[r * JOB_COUNTERS + which] : 0u;
+            uint32_t x = v;
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+                if (lane >= (uint32_t)off) x += y;
+            }
+            if (r < njobs) pre[r] = carry + x - v;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (lane == 0) pre[njobs] = carry;
+    }
+    __syncthreads();
+}
+
+// Largest r with pre[r] <= i.
+__device__ __forceinline__ uint32_t find_job(const uint32_t* pre, uint32_t njobs, uint32_t i) {
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pre[mid] <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Clears the wave's counters and fetch cursors; depth-0 queue size = paths.
+__global__ void k_wave_begin(Wave w, PathState ps) {
+    const uint32_t n = w.njobs * JOB_COUNTERS;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i / JOB_COUNTERS, c = i % JOB_COUNTERS;
+        ps.counts[i] = (c == 0) ? w.jobs[r].paths : 0u;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * MAX_DEPTH_SLOTS; i += gridDim.x * blockDim.x)
+        ps.cursors[i] = 0u;
+}
+
+// ONE: a single-job wave, whose job is read from the kernel parameters.
+template <bool ONE>
+__global__ void k_raygen(Wave w, PathState ps) {
+    __shared__ uint32_t pre[MAX_JOBS + 1];
+    if (!ONE) {
+        if (threadIdx.x == 0)
+            for (uint32_t r = 0; r <= w.njobs; ++r) pre[r] = (r < w.njobs) ? w.jobs[r].base : w.total_paths;
+        __syncthreads();
+    }
     const uint32_t stride = gridDim.x * blockDim.x;
-    if (blockIdx.x == 0 && threadIdx.x < MAX_DEPTH_SLOTS * 4) ps.counts[threadIdx.x] = 0;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.paths; p += stride) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.total_paths; p += stride) {
+        const uint32_t r = ONE ? 0u : find_job(pre, w.njobs, p);
+        const Job& j = ONE ? w.first : w.jobs[r];
+        const SceneView& s = j.view;
         uint32_t pixel, sample;
-        path_coords(w, p, pixel, sample);
+        path_coords(j, p, pixel, sample);
         // iterative.rs:25-40 (row = pixel / width)
-        const uint32_t W = w.width, H = w.height;
+        const uint32_t W = j.width, H = j.height;
         const uint32_t x = pixel % W, y = pixel / W;
         const float dmax = (float)max(W, H);
         const float fx = ((float)(2 * x + 1) - (float)W) / dmax;
         const float fy = ((float)(2 * (H - y) - 1) - (float)H) / dmax;
         Rng rng;
         rng.inc = pcg_inc(sample, pixel);
-        rng.state = pcg_init(w.seed, rng.inc);
+        rng.state = pcg_init(j.seed, rng.inc);
         const float lo = -1.0f / dmax, hi = 1.0f / dmax;
         const float jx = rng.range(lo, hi);
         const float jy = rng.range(lo, hi);
@@ -366,30 +428,58 @@ __global__ void k_raygen(SceneView s, WaveParams w, PathState ps) {
     }
 }
 
-// Closest hit of the live queue of depth k.
-// Closest hit of the live queue of depth k (persistent, dynamic fetch).
+// Closest hit of every job's live queue of depth k (persistent, dynamic fetch).
+// Concatenated index i -> job r, entry l = i - pre[r] of r's queue segment.
+template <bool ONE>
 struct ExtendIo {
-    const float4* org;
+    const float4* org;  // queue half of depth k
     const float4* dir;
     float4* hits;
-    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
-        ro = org[i];
-        rd = dir[i];
+    const Job* jobs;
+    const uint32_t* pre;
+    uint32_t njobs;
+    const float4* nodes1;  // ONE: the single job's BVH
+    const float4* tris1;
+    __device__ __forceinline__ uint32_t slot(uint32_t i, uint32_t& r) const {
+        if (ONE) {  // a single job's segment starts at slot 0
+            r = 0;
+            return i;
+        }
+        r = find_job(pre, njobs, i);
+        return jobs[r].base + (i - pre[r]);
+    }
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd, const float4*& n, const float4*& t) const {
+        uint32_t r;
+        const uint32_t q = slot(i, r);
+        ro = org[q];
+        rd = dir[q];
+        n = ONE ? nodes1 : jobs[r].view.nodes;
+        t = ONE ? tris1 : jobs[r].view.tris;
     }
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
+        uint32_t r;
+        const uint32_t q = slot(i, r);
         HitOut o = h;
         if (overflow) o.prim = MISS;
-        hits[i] = pack_hit(o);
+        hits[q] = pack_hit(o);
     }
 };
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_extend(SceneView s, PathState ps, uint32_t k, uint32_t* status,
-                                                unsigned long long* work) {
-    const uint32_t n = (k == 0) ? ps.first_count : ps.counts[k];
-    const uint32_t base = (k & 1) ? ps.cap : 0;
-    ExtendIo io{ps.q_org + base, ps.q_dir + base, ps.hits};
-    persistent_trace<false, COUNT>(s.nodes, s.tris, n, &ps.counts[2 * MAX_DEPTH_SLOTS + k], io, status, work);
+template <bool COUNT, bool ONE>
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_extend(Wave w, PathState ps, uint32_t k, uint32_t* status,
+                                                               unsigned long long* work) {
+    __shared__ uint32_t pre[MAX_JOBS + 1];
+    uint32_t n;
+    if (ONE) {
+        n = ps.counts[k];
+    } else {
+        job_prefix(ps.counts, k, w.njobs, pre);
+        n = pre[w.njobs];
+    }
+    const uint32_t half = (k & 1) ? ps.cap : 0;
+    ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, w.jobs, pre, w.njobs, w.first.view.nodes,
+                     w.first.view.tris};
+    persistent_trace<false, COUNT>(n, &ps.cursors[k], io, status, work);
 }
 
 // Reference estimator: the path's radiance is the recursion of
@@ -410,28 +500,60 @@ __device__ __forceinline__ void rad_add(const PathState& ps, uint32_t p, V3 c) {
     ps.rad[p] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
 }
 
-__global__ void __launch_bounds__(256) k_shade(SceneView s, WaveParams w, RenderParams rp, PathState ps, uint32_t k) {
-    const uint32_t n = (k == 0) ? ps.first_count : ps.counts[k];
-    const uint32_t in_base = (k & 1) ? ps.cap : 0;
-    const uint32_t out_base = (k & 1) ? 0 : ps.cap;
+// Appends the active lanes with `want` to job r's queue segment: one atomic
+// per group of lanes of the same job; returns this lane's slot in the segment.
+__device__ __forceinline__ uint32_t queue_append(bool want, uint32_t r, uint32_t* counter_of_job, uint32_t lane) {
+    const uint32_t active = __activemask();
+    const uint32_t wm = __ballot_sync(active, want);
+    uint32_t slot = 0;
+    if (want) {
+        const uint32_t grp = __match_any_sync(wm, r);
+        const uint32_t leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(counter_of_job, __popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        slot = base + __popc(grp & ((1u << lane) - 1u));
+    }
+    return slot;
+}
+
+template <bool ONE>
+__global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k) {
+    __shared__ uint32_t pre[MAX_JOBS + 1];
+    uint32_t n;
+    if (ONE) {
+        if (threadIdx.x == 0) pre[0] = 0;
+        __syncthreads();
+        n = ps.counts[k];
+    } else {
+        job_prefix(ps.counts, k, w.njobs, pre);
+        n = pre[w.njobs];
+    }
+    const uint32_t in_half = (k & 1) ? ps.cap : 0;
+    const uint32_t out_half = (k & 1) ? 0 : ps.cap;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const float fc = rp.firefly_clamp;
-    const bool nee_mode = rp.estimator == 1;
-    const bool last = (k + 1 >= rp.max_bounces);
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         const uint32_t i = i0 + threadIdx.x;
         bool cont = false, want_shadow = false;
         V3 new_o, new_d, sh_dir, sh_c;
-        uint32_t p = 0;
+        uint32_t p = 0, r = 0;
         if (i < n) {
-            p = ps.q_path[in_base + i];
-            const float4 ro4 = ps.q_org[in_base + i], rd4 = ps.q_dir[in_base + i];
+            r = ONE ? 0u : find_job(pre, w.njobs, i);
+            const Job& j = ONE ? w.first : w.jobs[r];
+            const SceneView& s = j.view;
+            const RenderParams& rp = j.rp;
+            const float fc = rp.firefly_clamp;
+            const bool nee_mode = rp.estimator == 1;
+            const bool last = (k + 1 >= rp.max_bounces);
+            const uint32_t q = in_half + j.base + (i - pre[r]);
+            p = ps.q_path[q];
+            const float4 ro4 = ps.q_org[q], rd4 = ps.q_dir[q];
             const V3 ro = xyz(ro4), rd = xyz(rd4);
-            const float4 hh = ps.hits[i];
+            const float4 hh = ps.hits[q - in_half];
             const uint32_t prim = __float_as_uint(hh.x);
             uint32_t pixel, sample;
-            path_coords(w, p, pixel, sample);
+            path_coords(j, p, pixel, sample);
             Rng rng;
             rng.inc = pcg_inc(sample, pixel);
             rng.state = ps.rng[p];
@@ -501,13 +623,13 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, WaveParams w, Render
                         if (nee_mode) prev_pdf = lamb ? dot(hit.normal, nd) / PI_F : -1.0f;
                         bool alive = true;
                         if (rp.rr_depth != 0 && k >= rp.rr_depth) {
-                            const float q = fminf(max3(tn), 0.95f);
+                            const float qq = fminf(max3(tn), 0.95f);
                             const float ur = rng.uniform();
-                            if (!(ur < q)) {
+                            if (!(ur < qq)) {
                                 alive = false;
                             } else {
-                                att = att / q;
-                                tn = tn / q;
+                                att = att / qq;
+                                tn = tn / qq;
                             }
                         }
                         if (!nee_mode) {
@@ -534,92 +656,110 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, WaveParams w, Render
             }
             ps.rng[p] = rng.state;
         }
-        // warp-aggregated compaction into the next queue and the shadow queue
-        const uint32_t active = __activemask();
-        const uint32_t cm = __ballot_sync(active, cont);
-        if (cm) {
-            const uint32_t leader = __ffs(cm) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&ps.counts[k + 1], __popc(cm));
-            base = __shfl_sync(active, base, leader);
-            if (cont) {
-                const uint32_t slot = base + __popc(cm & ((1u << lane) - 1u));
-                ps.q_org[out_base + slot] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
-                ps.q_dir[out_base + slot] = make_float4(new_d.x, new_d.y, new_d.z, INF_F);
-                ps.q_path[out_base + slot] = p;
-            }
+        // warp-aggregated compaction into the job's next queue segment and shadow segment
+        const uint32_t base_r = (ONE || i >= n) ? 0u : w.jobs[r].base;
+        const uint32_t cs = queue_append(cont, r, &ps.counts[r * JOB_COUNTERS + k + 1], lane);
+        if (cont) {
+            const uint32_t q = out_half + base_r + cs;
+            ps.q_org[q] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
+            ps.q_dir[q] = make_float4(new_d.x, new_d.y, new_d.z, INF_F);
+            ps.q_path[q] = p;
         }
-        const uint32_t sm = __ballot_sync(active, want_shadow);
-        if (sm) {
-            const uint32_t leader = __ffs(sm) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&ps.counts[MAX_DEPTH_SLOTS + k], __popc(sm));
-            base = __shfl_sync(active, base, leader);
-            if (want_shadow) {
-                const uint32_t slot = base + __popc(sm & ((1u << lane) - 1u));
-                ps.s_org[slot] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
-                ps.s_dir[slot] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, INF_F);
-                ps.s_path[slot] = p;
-                ps.s_contrib[slot] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
-            }
+        const uint32_t ss = queue_append(want_shadow, r, &ps.counts[r * JOB_COUNTERS + MAX_DEPTH_SLOTS + k], lane);
+        if (want_shadow) {
+            const uint32_t q = base_r + ss;
+            ps.s_org[q] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
+            ps.s_dir[q] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, INF_F);
+            ps.s_path[q] = p;
+            ps.s_contrib[q] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
         }
     }
 }
 
 // NEE visibility: adds the (clamped) contribution when nothing is hit
 // (persistent any-hit traversal).  A stack overflow counts as occluded.
+template <bool ONE>
 struct ShadowIo {
-    const float4* org;
-    const float4* dir;
-    const uint32_t* path;
-    const float4* contrib;
     PathState ps;
-    float fc;
-    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd) const {
-        ro = org[i];
-        rd = dir[i];
+    const Job* jobs;
+    const uint32_t* pre;
+    uint32_t njobs;
+    const float4* nodes1;  // ONE: the single job's BVH and clamp
+    const float4* tris1;
+    float fc1;
+    __device__ __forceinline__ uint32_t slot(uint32_t i, uint32_t& r) const {
+        if (ONE) {
+            r = 0;
+            return i;
+        }
+        r = find_job(pre, njobs, i);
+        return jobs[r].base + (i - pre[r]);
+    }
+    __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd, const float4*& n, const float4*& t) const {
+        uint32_t r;
+        const uint32_t q = slot(i, r);
+        ro = ps.s_org[q];
+        rd = ps.s_dir[q];
+        n = ONE ? nodes1 : jobs[r].view.nodes;
+        t = ONE ? tris1 : jobs[r].view.tris;
     }
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
-        if (!overflow && h.prim == MISS) rad_add(ps, path[i], clampc(xyz(contrib[i]), fc));
+        uint32_t r;
+        const uint32_t q = slot(i, r);
+        if (!overflow && h.prim == MISS)
+            rad_add(ps, ps.s_path[q], clampc(xyz(ps.s_contrib[q]), ONE ? fc1 : jobs[r].rp.firefly_clamp));
     }
 };
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(SceneView s, RenderParams rp, PathState ps, uint32_t k,
-                                                uint32_t* status, unsigned long long* work) {
-    const uint32_t n = ps.counts[MAX_DEPTH_SLOTS + k];
-    ShadowIo io{ps.s_org, ps.s_dir, ps.s_path, ps.s_contrib, ps, rp.firefly_clamp};
-    persistent_trace<true, COUNT>(s.nodes, s.tris, n, &ps.counts[3 * MAX_DEPTH_SLOTS + k], io, status, work);
+template <bool COUNT, bool ONE>
+__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(Wave w, PathState ps, uint32_t k, uint32_t* status,
+                                                               unsigned long long* work) {
+    __shared__ uint32_t pre[MAX_JOBS + 1];
+    uint32_t n;
+    if (ONE) {
+        n = ps.counts[MAX_DEPTH_SLOTS + k];
+    } else {
+        job_prefix(ps.counts, MAX_DEPTH_SLOTS + k, w.njobs, pre);
+        n = pre[w.njobs];
+    }
+    ShadowIo<ONE> io{ps, w.jobs, pre, w.njobs, w.first.view.nodes, w.first.view.tris, w.first.rp.firefly_clamp};
+    persistent_trace<true, COUNT>(n, &ps.cursors[MAX_DEPTH_SLOTS + k], io, status, work);
 }
 
-// Per-pixel running sum in sample order over this wavefront's paths.
-__global__ void k_accumulate(WaveParams w, PathState ps, float4* __restrict__ psum) {
-    const uint32_t NP = w.num_pixels;
+// Per-pixel running sum, in sample order, of each job's paths of this wave
+// (blockIdx.y = job).
+template <bool ONE>
+__global__ void k_accumulate(Wave w, PathState ps) {
+    const Job& j = ONE ? w.first : w.jobs[blockIdx.y];
+    const uint32_t NP = j.num_pixels;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < NP; px += stride) {
         // global indices g = s*NP + px inside [g0, g0 + paths)
-        uint64_t g0 = w.g0, g1 = w.g0 + w.paths;
-        uint64_t s_begin = (g0 > px) ? (g0 - px + NP - 1) / NP : 0;
+        const uint64_t g0 = j.g0, g1 = j.g0 + j.paths;
+        const uint64_t s_begin = (g0 > px) ? (g0 - px + NP - 1) / NP : 0;
         if (s_begin * NP + px >= g1) continue;
-        float4 acc = psum[px];
+        float4 acc = j.psum[px];
         for (uint64_t g = s_begin * NP + px; g < g1; g += NP) {
-            const float4 r = ps.rad[g - g0];
-            acc.x = acc.x + r.x;
-            acc.y = acc.y + r.y;
-            acc.z = acc.z + r.z;
+            const float4 rr = ps.rad[j.base + (uint32_t)(g - g0)];
+            acc.x = acc.x + rr.x;
+            acc.y = acc.y + rr.y;
+            acc.z = acc.z + rr.z;
         }
-        psum[px] = acc;
+        j.psum[px] = acc;
     }
 }
 
-// Adds this wavefront's queue sizes to the running totals
+// Adds this wave's queue sizes to the running totals
 // (totals[0] camera paths, [1] extend rays, [2] shadow rays).
-__global__ void k_wave_stats(PathState ps, uint32_t paths, uint32_t bounces, unsigned long long* totals) {
+__global__ void k_wave_stats(Wave w, PathState ps, uint32_t bounces, unsigned long long* totals) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    unsigned long long ext = bounces > 0 ? paths : 0, shd = 0;
-    for (uint32_t k = 1; k < bounces; ++k) ext += ps.counts[k];
-    for (uint32_t k = 0; k < bounces; ++k) shd += ps.counts[MAX_DEPTH_SLOTS + k];
-    totals[0] += paths;
+    unsigned long long ext = 0, shd = 0;
+    for (uint32_t r = 0; r < w.njobs; ++r) {
+        const uint32_t* c = ps.counts + r * JOB_COUNTERS;
+        for (uint32_t k = 0; k < bounces; ++k) ext += c[k];
+        for (uint32_t k = 0; k < bounces; ++k) shd += c[MAX_DEPTH_SLOTS + k];
+    }
+    totals[0] += w.total_paths;
     totals[1] += ext;
     totals[2] += shd;
 }
@@ -744,7 +884,7 @@ static cudaError_t intersect_impl(const SceneView& s, const float4* rays, uint64
     if (!grid) grid = persistent_grid(k_intersect<ANY, COUNT>, 128);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(s.nodes, s.tris, BatchIo{rays, hits}, (uint32_t)n, counter, status,
+    k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(BatchIo{rays, hits, s.nodes, s.tris}, (uint32_t)n, counter, status,
                                                    work);
     return cudaGetLastError();
 }
@@ -763,51 +903,57 @@ cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint6
                : intersect_impl<false, true>(s, rays, n, hits, counter, status, work, st);
 }
 
-cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathState& ps, cudaStream_t st) {
-    k_raygen<<<grid_for(w.paths, 256, 8), 256, 0, st>>>(s, w, ps);
+cudaError_t launch_raygen(const Wave& w, const PathState& ps, cudaStream_t st) {
+    k_wave_begin<<<grid_for((uint64_t)w.njobs * JOB_COUNTERS, 256, 1), 256, 0, st>>>(w, ps);
+    if (w.njobs == 1) k_raygen<true><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps);
+    else k_raygen<false><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps);
     return cudaGetLastError();
 }
 
-cudaError_t launch_extend(const SceneView& s, const WaveParams& w, const PathState& ps, uint32_t k, uint32_t* status,
-                          unsigned long long* work, cudaStream_t st) {
-    static unsigned g0 = 0, g1 = 0;
-    PathState p = ps;
-    p.first_count = w.paths;
-    if (work) {
-        if (!g1) g1 = persistent_grid(k_extend<true>, 128);
-        k_extend<true><<<g1, 128, 0, st>>>(s, p, k, status, work);
-    } else {
-        if (!g0) g0 = persistent_grid(k_extend<false>, 128);
-        k_extend<false><<<g0, 128, 0, st>>>(s, p, k, status, nullptr);
-    }
+template <bool COUNT, bool ONE>
+static void extend_impl(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                        cudaStream_t st) {
+    static unsigned g = 0;
+    if (!g) g = persistent_grid(k_extend<COUNT, ONE>, 128);
+    k_extend<COUNT, ONE><<<g, 128, 0, st>>>(w, ps, k, status, work);
+}
+
+cudaError_t launch_extend(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                          cudaStream_t st) {
+    const bool one = w.njobs == 1;
+    if (work) one ? extend_impl<true, true>(w, ps, k, status, work, st) : extend_impl<true, false>(w, ps, k, status, work, st);
+    else one ? extend_impl<false, true>(w, ps, k, status, nullptr, st) : extend_impl<false, false>(w, ps, k, status, nullptr, st);
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                         uint32_t k, cudaStream_t st) {
-    PathState p = ps;
-    p.first_count = w.paths;
-    k_shade<<<grid_for(w.paths, 256, 8), 256, 0, st>>>(s, w, rp, p, k);
+cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, cudaStream_t st) {
+    if (w.njobs == 1) k_shade<true><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps, k);
+    else k_shade<false><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps, k);
     return cudaGetLastError();
 }
 
-cudaError_t launch_shadow(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                          uint32_t k, uint32_t* status, unsigned long long* work, cudaStream_t st) {
-    static unsigned g0 = 0, g1 = 0;
-    if (work) {
-        if (!g1) g1 = persistent_grid(k_shadow<true>, 128);
-        k_shadow<true><<<g1, 128, 0, st>>>(s, rp, ps, k, status, work);
-    } else {
-        if (!g0) g0 = persistent_grid(k_shadow<false>, 128);
-        k_shadow<false><<<g0, 128, 0, st>>>(s, rp, ps, k, status, nullptr);
-    }
+template <bool COUNT, bool ONE>
+static void shadow_impl(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                        cudaStream_t st) {
+    static unsigned g = 0;
+    if (!g) g = persistent_grid(k_shadow<COUNT, ONE>, 128);
+    k_shadow<COUNT, ONE><<<g, 128, 0, st>>>(w, ps, k, status, work);
+}
+
+cudaError_t launch_shadow(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                          cudaStream_t st) {
+    const bool one = w.njobs == 1;
+    if (work) one ? shadow_impl<true, true>(w, ps, k, status, work, st) : shadow_impl<true, false>(w, ps, k, status, work, st);
+    else one ? shadow_impl<false, true>(w, ps, k, status, nullptr, st) : shadow_impl<false, false>(w, ps, k, status, nullptr, st);
     return cudaGetLastError();
 }
 
-cudaError_t launch_accumulate(const WaveParams& w, const PathState& ps, const RenderParams& rp, float4* psum,
-                              unsigned long long* totals, cudaStream_t st) {
-    k_accumulate<<<grid_for(w.num_pixels, 256, 8), 256, 0, st>>>(w, ps, psum);
-    if (totals) k_wave_stats<<<1, 32, 0, st>>>(ps, w.paths, rp.max_bounces, totals);
+cudaError_t launch_accumulate(const Wave& w, const PathState& ps, uint32_t max_pixels, unsigned long long* totals,
+                              cudaStream_t st) {
+    dim3 grid(grid_for(max_pixels, 256, 8), w.njobs);
+    if (w.njobs == 1) k_accumulate<true><<<grid, 256, 0, st>>>(w, ps);
+    else k_accumulate<false><<<grid, 256, 0, st>>>(w, ps);
+    if (totals) k_wave_stats<<<1, 32, 0, st>>>(w, ps, w.max_bounces, totals);
     return cudaGetLastError();
 }
 

@@ -9,17 +9,6 @@ namespace vr {
 
 constexpr uint32_t MAX_DEPTH_SLOTS = 32;  // max_bounces must stay below this
 
-// One wavefront: global sample-major path indices [g0, g0 + paths).
-struct WaveParams {
-    uint64_t g0;
-    uint64_t seed;
-    uint32_t paths;
-    uint32_t num_pixels;
-    uint32_t width, height;
-    uint32_t first_sample;
-    uint32_t pad_;
-};
-
 struct RenderParams {
     float firefly_clamp;
     uint32_t max_bounces;
@@ -28,11 +17,36 @@ struct RenderParams {
     uint32_t rr_depth;
 };
 
+// One render job's part of a wavefront (device memory, one per job per wave).
+struct Job {
+    SceneView view;
+    RenderParams rp;
+    uint64_t seed;
+    uint64_t g0;            // first global sample-major path of this wave
+    uint32_t paths;         // paths of the job in this wave
+    uint32_t base;          // first slot of the job's segment in every per-path array
+    uint32_t num_pixels, width, height, first_sample;
+    float4* psum;           // per-pixel running sums (float4 per pixel)
+};
+
+constexpr uint32_t MAX_JOBS = 256;                       // jobs per wavefront
+constexpr uint32_t JOB_COUNTERS = 2 * MAX_DEPTH_SLOTS;   // [k] queue size, [M + k] shadow queue size
+
+// A wavefront: jobs[0..njobs) in device memory, their segments packed from slot 0.
+struct Wave {
+    const Job* jobs;
+    uint32_t njobs;
+    uint32_t total_paths;
+    uint32_t max_bounces;   // over the jobs
+    uint32_t any_nee;       // some job uses the NEE estimator
+    Job first;              // copy of jobs[0]: single-job waves read it from kernel parameters
+};
+
 // Device scratch of the wavefront integrator (structure of arrays, `cap`
 // paths).  Ray queues are double buffered (2*cap entries).
 struct PathState {
     uint32_t cap;
-    uint32_t first_count;
+    uint32_t pad_;
     float4* q_org;      // (origin, tmin)    2*cap
     float4* q_dir;      // (direction, tmax) 2*cap
     uint32_t* q_path;   // path index        2*cap
@@ -45,8 +59,8 @@ struct PathState {
     float4* s_dir;
     float4* s_contrib;
     uint32_t* s_path;
-    uint32_t* counts;   // 4*MAX_DEPTH_SLOTS words: [k] live paths at depth k, [M + k] shadow rays,
-                        // [2M + k] extend fetch cursor, [3M + k] shadow fetch cursor
+    uint32_t* counts;   // MAX_JOBS * JOB_COUNTERS per-job queue sizes
+    uint32_t* cursors;  // 2 * MAX_DEPTH_SLOTS fetch cursors: [k] extend, [M + k] shadow
 };
 
 // Batch closest/any hit; `counter` is a device word the persistent kernel
@@ -55,18 +69,17 @@ cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n,
                              uint32_t* counter, uint32_t* status, cudaStream_t st);
 cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
                                    uint32_t* counter, unsigned long long* work, uint32_t* status, cudaStream_t st);
-// Wavefront stages, in launch order: raygen, then per depth k extend, shade
-// and (NEE) shadow, then accumulate.  `work` (optional) receives traversal
-// work counters (node visits, triangle tests) of that launch.
-cudaError_t launch_raygen(const SceneView& s, const WaveParams& w, const PathState& ps, cudaStream_t st);
-cudaError_t launch_extend(const SceneView& s, const WaveParams& w, const PathState& ps, uint32_t k, uint32_t* status,
-                          unsigned long long* work, cudaStream_t st);
-cudaError_t launch_shade(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                         uint32_t k, cudaStream_t st);
-cudaError_t launch_shadow(const SceneView& s, const WaveParams& w, const RenderParams& rp, const PathState& ps,
-                          uint32_t k, uint32_t* status, unsigned long long* work, cudaStream_t st);
-cudaError_t launch_accumulate(const WaveParams& w, const PathState& ps, const RenderParams& rp, float4* psum,
-                              unsigned long long* totals, cudaStream_t st);
+// Wavefront stages, in launch order: raygen (clears the wave's counters),
+// then per depth k extend, shade and (NEE) shadow, then accumulate.  `work`
+// (optional) receives traversal work counters (node visits, triangle tests).
+cudaError_t launch_raygen(const Wave& w, const PathState& ps, cudaStream_t st);
+cudaError_t launch_extend(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                          cudaStream_t st);
+cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, cudaStream_t st);
+cudaError_t launch_shadow(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
+                          cudaStream_t st);
+cudaError_t launch_accumulate(const Wave& w, const PathState& ps, uint32_t max_pixels, unsigned long long* totals,
+                              cudaStream_t st);
 cudaError_t launch_finalize(const float4* psum, float4* rgba, uint32_t np, float inv_total, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, float4* out, uint32_t np, int32_t tonemap, float inv_gamma, float ex,
                            float scale, cudaStream_t st);

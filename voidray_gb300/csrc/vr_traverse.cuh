@@ -27,7 +27,7 @@ struct HitOut {
 };
 
 #ifndef VR_TRACE_MINB
-#define VR_TRACE_MINB 1  // minimum resident blocks per SM requested from ptxas for the traversal kernels
+#define VR_TRACE_MINB 8  // minimum resident blocks per SM requested from ptxas (64 registers, no spills)
 #endif
 #ifndef VR_DYN_FETCH
 #define VR_DYN_FETCH 12  // refill a warp's lanes once at least this many have finished
@@ -88,20 +88,18 @@ __device__ __forceinline__ void add_work(unsigned long long* work, uint32_t nv, 
     }
 }
 
-// Io supplies load(i, ro, rd) and store(i, hit, overflow).  `counter` is the
-// queue's fetch cursor (zero before the launch).  Every lane of the block's
-// warps must call this (warp-uniform control flow at the votes).
+// Io supplies load(i, ro, rd, nodes, tris) -- the ray and the BVH of its
+// scene, so that rays of different scenes can share a launch -- and
+// store(i, hit, overflow).  `counter` is the queue's fetch cursor (zero
+// before the launch).  Every lane of the block's warps must call this
+// (warp-uniform control flow at the votes).
 template <bool ANY, bool COUNT, class Io>
-__device__ __forceinline__ void persistent_trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                 uint32_t n, uint32_t* counter, const Io& io, uint32_t* status,
+__device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, const Io& io, uint32_t* status,
                                                  unsigned long long* work) {
     const uint32_t lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
-    if (nodes == nullptr) {  // scene without triangles: every ray misses
-        const HitOut h{MISS, INF_F, 0.0f, 0.0f};
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) io.store(i, h, false);
-        return;
-    }
+    const float4* nodes = nullptr;  // BVH of the current ray's scene
+    const float4* tris = nullptr;
     int stack_node[STACK_SIZE];
     float stack_t[STACK_SIZE];
     V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
@@ -138,7 +136,7 @@ __device__ __forceinline__ void persistent_trace(const float4* __restrict__ node
                 ray = base + __popc(needm & ((1u << lane) - 1u));
                 if (ray < n) {
                     float4 ro, rd;
-                    io.load(ray, ro, rd);
+                    io.load(ray, ro, rd, nodes, tris);
                     o = xyz(ro);
                     d = xyz(rd);
                     const float eps = 1e-18f;
@@ -150,7 +148,7 @@ __device__ __forceinline__ void persistent_trace(const float4* __restrict__ node
                     oz = ro.z * iz;
                     tmin = ro.w;
                     best = rd.w;
-                    node = 0;
+                    node = nodes ? 0 : SENTINEL;  // a scene without triangles: the ray misses
                     leaf = 0;
                     sp = 0;
                     overflow = false;
