@@ -54,6 +54,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-work-count", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-size", type=int, default=256, help="job image side")
+    ap.add_argument("--serve-target", type=float, default=1e-3, help="target relMSE")
     return ap.parse_args()
 
 
@@ -153,6 +158,85 @@ def cpu_baseline(scene, st, args, budget_s):
             "sample": f"1 spp over {n} pixels (rows {start // w}-{(start + n) // w - 1}) of the "
                       f"{w}x{h} frame, {dt:.1f} s; {int(rays[0])} extend + {int(rays[1])} shadow rays",
             "mrays_per_s": (int(rays[0]) + int(rays[1])) / dt / 1e6}
+
+
+def serving_benchmark(args):
+    """Poisson stream of render jobs drawn like the plain render scene (four
+    resident displaced icospheres of 18k-800k triangles with the sky HDRI),
+    each to a target relative MSE (estimated from the job's two half-buffers,
+    checked against a 4096-spp reference after the run).  Served: continuous
+    batching of every admitted job in one launch per pass.  Plain: the same
+    requests rendered one at a time (one active job)."""
+    import numpy as np
+
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.scene import Estimator, RenderSettings
+    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig, poisson_arrivals
+
+    size = args.serve_size
+    hdri = vr.Environments.hdri_image(W.sky_hdri(1024, 512))
+    pool = []
+    for k, freq in enumerate((30, 60, 120, 200)):
+        s, _ = W.displaced_icosphere_scene(freq=freq, seed=10 + k, hdri_size=None)
+        s.environment = hdri
+        acc = s.build_acceleration()
+        # the reference's default firefly clamp (3.0): the sun seen through
+        # metal / dielectric patches would otherwise keep every job far from
+        # the target error
+        st = RenderSettings(total_samples=1, max_bounces=8 + k, rr_depth=3, estimator=Estimator.NEE,
+                            firefly_clamp=3.0)
+        pool.append((acc, st, int(acc.info().device_bytes), s.num_triangles()))
+    rng = np.random.default_rng(5)
+    arrivals = poisson_arrivals(args.serve_rate, args.serve_jobs, seed=5)
+    requests = []
+    for i, t in enumerate(arrivals):
+        acc, st, nbytes, _ = pool[int(rng.integers(0, len(pool)))]
+        requests.append((float(t), JobRequest(acc, st, size, size, max_samples=2048, target_relmse=args.serve_target,
+                                              seed=1000 + i, scene_bytes=nbytes)))
+    out = {"jobs": args.serve_jobs, "rate_per_s": args.serve_rate, "image": f"{size}x{size}",
+           "target_relmse": args.serve_target, "scenes_triangles": [p[3] for p in pool],
+           "error_estimate": "half-buffer variance of the mean / (m^2 + 1e-2)"}
+    backend = GpuBackend()
+    results = {}
+    # served: as many active jobs as fill a ~16M-path wavefront per pass, so
+    # that jobs complete in admission order instead of all at the end
+    spp_pass = 32
+    fill = max(1, (1 << 24) // (size * size * spp_pass))
+    out["served_max_active"] = fill
+    for name, active in (("served", fill), ("plain", 1)):
+        srv = Server(backend, ServerConfig(memory_budget=150 * 10**9, max_active=active, spp_per_pass=32,
+                                           min_samples=64))
+        t0 = time.perf_counter()
+        srv.run([(t, r) for t, r in requests])
+        wall = time.perf_counter() - t0
+        lat = srv.latencies()
+        samples = sum(j.samples * j.req.width * j.req.height for j in srv.jobs.values())
+        out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                     "jobs_per_s": len(lat) / wall, "samples_per_s": samples / wall, "wall_s": wall,
+                     "passes": srv.passes,
+                     "mean_spp": float(np.mean([j.samples for j in srv.jobs.values()]))}
+        results[name] = srv
+    # true error of the served results against a 4096-spp reference per scene
+    refs = {}
+    errs = []
+    for j in results["served"].jobs.values():
+        key = id(j.req.scene)
+        if key not in refs:
+            t = vr.CpuRenderTarget(size, size)
+            st = RenderSettings(**{**j.req.settings.__dict__, "total_samples": 4096})
+            vr.iterative_render(t, j.req.scene, st, 4096, seed=99)
+            refs[key] = t.buffer[..., :3].astype(np.float64)
+        r = refs[key]
+        x = j.result.astype(np.float64)
+        errs.append(float(np.mean((x - r) ** 2 / (r * r + 1e-2))))
+    out["served"]["true_relmse_p50"] = float(np.median(errs))
+    out["served"]["true_relmse_p99"] = float(np.percentile(errs, 99))
+    out["p50_speedup"] = out["plain"]["p50_s"] / out["served"]["p50_s"]
+    out["throughput_ratio"] = out["served"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
+    for acc, *_ in pool:
+        acc.destroy()
+    return out
 
 
 def run_reference(args):
@@ -340,6 +424,10 @@ def main():
     out_img = host.numpy()
     finite = bool(np.isfinite(out_img).all())
 
+    acc.destroy()
+    serve = None
+    if rank == 0 and world == 1 and not args.no_serve:
+        serve = serving_benchmark(args)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, st, args, args.cpu_seconds)
@@ -357,7 +445,7 @@ def main():
             "mrays_per_s": (ext_rays + shd_rays) / (ms / 1e3) / 1e6,
             "rays": {"extend": int(ext_rays), "shadow": int(shd_rays)},
             "stages": stage, "gpu_launches": gpu_launches, "clocks": clk, "e2e": e2e, "roofline": roofline,
-            "cpu_baseline": cpu, "image_finite": finite,
+            "cpu_baseline": cpu, "image_finite": finite, "serving": serve,
         }
         print(json.dumps(line), flush=True)
     acc.destroy()

@@ -1,0 +1,318 @@
+"""Serving layer: a continuous-batching request loop over the batched renderer.
+
+No reference counterpart: the reference renders one scene at a time on its
+render thread (voidray_renderer/src/render/renderer.rs:35-125), progressively
+in chunks sized by `update_frequency`, with cancel and progress statistics.
+Here many progressive renders run at once:
+
+* A request names a resident scene (built once with vr_scene_create), its
+  settings, image size, a sample cap and a target relative MSE.
+* Admission: a waiting request is admitted when an active slot is free and its
+  device footprint (two accumulation half-buffers, plus its scene if that scene
+  is not resident yet) fits the memory budget; otherwise it waits (FIFO).
+* Every pass renders `spp_per_pass` further samples of every active job in one
+  batched launch (vr_batch_render); passes alternate between a job's two
+  half-buffers A and B.  Requests that arrive meanwhile are admitted at the
+  next pass, so their work overlaps on the device with the running jobs.
+* After each pass a job's error is estimated from its half-buffers: with means
+  a, b over nA, nB samples, the variance of the combined mean is about
+  (a - b)^2 nA nB / (nA + nB)^2, and the estimate is its mean ratio to
+  (m^2 + 1e-2) over pixels and channels (the relMSE definition).  A job
+  finishes when the estimate reaches the target or its sample cap.
+* A job's result depends only on its own sample streams and pass schedule,
+  so it is the same alone and in any mix.
+
+Backends: GpuBackend (torch device buffers + vr_batch) and FakeBackend (a
+deterministic CPU stand-in used by the scheduler tests).
+"""
+from __future__ import annotations
+
+import itertools
+import time
+from dataclasses import dataclass, field
+from typing import Any, Callable, Optional
+
+import numpy as np
+
+EPS_REL = 1e-2  # relMSE denominator offset
+
+
+@dataclass
+class JobRequest:
+    scene: Any                 # backend scene handle (SceneAcceleration for the GPU backend)
+    settings: Any              # RenderSettings (total_samples is managed by the server)
+    width: int
+    height: int
+    max_samples: int = 4096
+    target_relmse: float = 1e-3
+    seed: int = 0
+    scene_bytes: int = 0       # device bytes of the scene (counted once while resident)
+
+
+@dataclass
+class JobState:
+    job_id: int
+    req: JobRequest
+    arrival: float
+    state: str = "waiting"     # waiting, active, done, cancelled, failed
+    admitted: Optional[float] = None
+    finished: Optional[float] = None
+    samples: int = 0
+    n_a: int = 0
+    n_b: int = 0
+    passes: int = 0
+    estimate: float = float("inf")
+    bufs: Any = None
+    result: Optional[np.ndarray] = None
+    error: str = ""
+
+    @property
+    def latency(self) -> Optional[float]:
+        return None if self.finished is None else self.finished - self.arrival
+
+    def footprint(self) -> int:
+        return 2 * self.req.width * self.req.height * 16
+
+
+@dataclass
+class ServerConfig:
+    memory_budget: int = 150 * 10**9
+    max_active: int = 64
+    spp_per_pass: int = 16
+    min_samples: int = 32      # no error estimate before this many samples
+
+
+class FakeBackend:
+    """CPU stand-in: a job's pixel value for sample s is a deterministic
+    function of (seed, pixel, s), so results are reproducible and independent
+    of the mix.  `fail_alloc` makes allocation fail for chosen job ids."""
+
+    def __init__(self, fail_alloc: Callable[[int], bool] = lambda job_id: False, noise: float = 0.5):
+        self.fail_alloc = fail_alloc
+        self.noise = noise
+        self.calls = []
+
+    def alloc(self, job: JobState):
+        if self.fail_alloc(job.job_id):
+            raise MemoryError(f"allocation refused for job {job.job_id}")
+        n = job.req.width * job.req.height
+        return [np.zeros((n, 3)), np.zeros((n, 3))]
+
+    def free(self, job: JobState) -> None:
+        job.bufs = None
+
+    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        """work: (job, buffer index, first sample, samples)."""
+        self.calls.append([(j.job_id, b, f, s) for j, b, f, s in work])
+        for job, b, first, n in work:
+            npx = job.req.width * job.req.height
+            base = 0.2 + (np.arange(npx) % 17) / 20.0
+            for k in range(first, first + n):
+                rng = np.random.default_rng([job.req.seed, k])
+                job.bufs[b] += (base + self.noise * rng.standard_normal(npx))[:, None]
+
+    def means(self, job: JobState):
+        a, b = job.bufs
+        return a / max(job.n_a, 1), b / max(job.n_b, 1)
+
+    def estimate(self, job: JobState) -> float:
+        a, b = self.means(job)
+        return _estimate(a, b, job.n_a, job.n_b)
+
+    def result(self, job: JobState) -> np.ndarray:
+        a, b = job.bufs
+        return (a + b) / (job.n_a + job.n_b)
+
+
+def _estimate(a, b, na: int, nb: int, xp=np) -> float:
+    n = na + nb
+    m = (a * na + b * nb) / n
+    var = (a - b) ** 2 * (na * nb) / (n * n)
+    return float(xp.mean(var / (m * m + EPS_REL)))
+
+
+class GpuBackend:
+    """Device accumulation buffers (torch) and one vr_batch for every pass."""
+
+    def __init__(self, max_wave_paths: int = 0):
+        import torch
+
+        from .batch import Batch
+
+        self.torch = torch
+        self.batch = Batch(max_wave_paths)
+        self.stream = torch.cuda.Stream()
+
+    def alloc(self, job: JobState):
+        t = self.torch
+        h, w = job.req.height, job.req.width
+        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda"), t.zeros((h, w, 4), dtype=t.float32, device="cuda")]
+
+    def free(self, job: JobState) -> None:
+        job.bufs = None
+
+    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        from dataclasses import replace
+
+        from .batch import RenderJob
+
+        jobs = []
+        for job, b, first, n in work:
+            # buffers accumulate raw sums: total_samples = 1
+            st = replace(job.req.settings, total_samples=1)
+            jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
+                                  job.req.seed, first))
+        self.batch.render(jobs, self.stream.cuda_stream)
+        self.batch.synchronize(self.stream.cuda_stream)
+
+    def estimate(self, job: JobState) -> float:
+        t = self.torch
+        a = job.bufs[0][..., :3].double() / max(job.n_a, 1)
+        b = job.bufs[1][..., :3].double() / max(job.n_b, 1)
+        return _estimate(a, b, job.n_a, job.n_b, xp=t)
+
+    def result(self, job: JobState) -> np.ndarray:
+        a, b = job.bufs
+        return ((a[..., :3] + b[..., :3]) / (job.n_a + job.n_b)).cpu().numpy()
+
+
+class Server:
+    def __init__(self, backend, config: ServerConfig = ServerConfig(), clock: Callable[[], float] = time.perf_counter):
+        self.backend = backend
+        self.cfg = config
+        self.clock = clock
+        self.jobs: dict[int, JobState] = {}
+        self.waiting: list[int] = []
+        self.active: list[int] = []
+        self._ids = itertools.count()
+        self.resident_scenes: dict[int, int] = {}  # id(scene) -> active users
+        self.used = 0
+        self.passes = 0
+
+    # -- requests --------------------------------------------------------
+    def submit(self, req: JobRequest, arrival: Optional[float] = None) -> int:
+        jid = next(self._ids)
+        self.jobs[jid] = JobState(jid, req, self.clock() if arrival is None else arrival)
+        self.waiting.append(jid)
+        return jid
+
+    def cancel(self, job_id: int) -> None:
+        job = self.jobs[job_id]
+        if job.state == "waiting":
+            self.waiting.remove(job_id)
+        elif job.state == "active":
+            self._release(job)
+            self.active.remove(job_id)
+        job.state = "cancelled"
+        job.finished = self.clock()
+
+    def status(self, job_id: int) -> JobState:
+        return self.jobs[job_id]
+
+    # -- admission ---------------------------------------------------------
+    def _scene_cost(self, req: JobRequest) -> int:
+        return 0 if id(req.scene) in self.resident_scenes else req.scene_bytes
+
+    def _admit(self) -> None:
+        still = []
+        for jid in self.waiting:
+            job = self.jobs[jid]
+            need = job.footprint() + self._scene_cost(job.req)
+            if len(self.active) < self.cfg.max_active and self.used + need <= self.cfg.memory_budget:
+                try:
+                    job.bufs = self.backend.alloc(job)
+                except Exception as e:  # an allocation failure fails this job only
+                    job.state, job.error, job.finished = "failed", str(e), self.clock()
+                    continue
+                self.used += need
+                key = id(job.req.scene)
+                self.resident_scenes[key] = self.resident_scenes.get(key, 0) + 1
+                job.state, job.admitted = "active", self.clock()
+                self.active.append(jid)
+            else:
+                still.append(jid)
+        self.waiting = still
+
+    def _release(self, job: JobState) -> None:
+        key = id(job.req.scene)
+        n = self.resident_scenes.get(key, 1) - 1
+        freed = job.footprint()
+        if n <= 0:
+            self.resident_scenes.pop(key, None)
+            freed += job.req.scene_bytes
+        else:
+            self.resident_scenes[key] = n
+        self.used -= freed
+        self.backend.free(job)
+
+    # -- passes ------------------------------------------------------------
+    def step(self) -> int:
+        """Admits what fits, renders one pass of every active job, retires
+        finished jobs.  Returns the number of jobs rendered."""
+        self._admit()
+        if not self.active:
+            return 0
+        work = []
+        for jid in self.active:
+            job = self.jobs[jid]
+            n = min(self.cfg.spp_per_pass, job.req.max_samples - job.samples)
+            work.append((job, job.passes % 2, job.samples, n))
+        try:
+            self.backend.render(work)
+        except Exception as e:
+            for job, *_ in work:
+                job.state, job.error, job.finished = "failed", str(e), self.clock()
+                self._release(job)
+            self.active = []
+            return 0
+        self.passes += 1
+        done = []
+        for job, b, first, n in work:
+            job.samples += n
+            if b == 0:
+                job.n_a += n
+            else:
+                job.n_b += n
+            job.passes += 1
+            if job.n_a and job.n_b and job.samples >= self.cfg.min_samples:
+                job.estimate = self.backend.estimate(job)
+            if job.estimate <= job.req.target_relmse or job.samples >= job.req.max_samples:
+                job.result = self.backend.result(job)
+                job.state, job.finished = "done", self.clock()
+                done.append(job.job_id)
+        for jid in done:
+            self._release(self.jobs[jid])
+            self.active.remove(jid)
+        return len(work)
+
+    def idle(self) -> bool:
+        return not self.waiting and not self.active
+
+    def run(self, arrivals: list[tuple[float, JobRequest]] = (), until_idle: bool = True) -> None:
+        """Replays `arrivals` (offset seconds, request) against the clock while
+        stepping; returns when every request has finished."""
+        start = self.clock()
+        pending = sorted(arrivals, key=lambda x: x[0])
+        i = 0
+        while True:
+            now = self.clock() - start
+            while i < len(pending) and pending[i][0] <= now:
+                self.submit(pending[i][1], arrival=start + pending[i][0])
+                i += 1
+            if self.idle():
+                if i >= len(pending):
+                    break
+                time.sleep(max(0.0, min(pending[i][0] - now, 0.001)))
+                continue
+            self.step()
+            if not until_idle and i >= len(pending):
+                break
+
+    def latencies(self, state: str = "done") -> np.ndarray:
+        return np.array([j.latency for j in self.jobs.values() if j.state == state and j.latency is not None])
+
+
+def poisson_arrivals(rate: float, count: int, seed: int = 0) -> np.ndarray:
+    """Arrival offsets (seconds) of a Poisson stream."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, count))

@@ -277,7 +277,8 @@ def displaced_icosphere_scene(freq: int = 316, seed: int = 2, patch: int = 64, h
     q = np.array([(-g, gy, -g), (-g, gy, g), (g, gy, g), (g, gy, -g)], f32)
     s.add_object(ground, s.add_mesh(Mesh(q, np.array([0, 1, 2, 2, 0, 3], np.uint32),
                                          np.array([(0, 1, 0)] * 4, f32))))
-    s.environment = Environments.hdri_image(sky_hdri(*hdri_size), importance_sample=True)
+    if hdri_size is not None:  # None: the caller sets a (shared) environment
+        s.environment = Environments.hdri_image(sky_hdri(*hdri_size), importance_sample=True)
     s.camera = Camera.look_at((0.0, 0.35, 3.4), (0.0, -0.15, 0.0), (0.0, 1.0, 0.0), degrees_to_radians(50.0))
     st = RenderSettings(total_samples=256, max_bounces=12, rr_depth=3, estimator=Estimator.NEE,
                         firefly_clamp=float("inf"))
