@@ -211,6 +211,20 @@ vr_status vr_render_device(vr_scene* scene, const vr_render_settings* settings,
                            uint32_t height, uint64_t seed, uint32_t first_sample,
                            void* stream);
 
+/* vr_render_device plus first-hit feature buffers (AOVs) for the denoiser;
+ * no counterpart in the reference.  rgba_device receives exactly what
+ * vr_render_device writes for the same arguments.  albedo_device and
+ * normal_device (RGBA f32, width*height*4, device memory) receive, summed
+ * over the same samples and scaled by 1/settings.total_samples like the
+ * radiance: the first hit's surface colour clamped to 1 (1 for dielectrics;
+ * the environment colour clamped to 1 for rays that miss) and the first
+ * hit's shading normal facing the camera ray (0 for misses); alpha gains 1.0
+ * per call. */
+vr_status vr_render_aov_device(vr_scene* scene, const vr_render_settings* settings,
+                               uint32_t samples, float* rgba_device, float* albedo_device,
+                               float* normal_device, uint32_t width, uint32_t height,
+                               uint64_t seed, uint32_t first_sample, void* stream);
+
 /* Same render as vr_render_device, for callers that cannot allocate device
  * memory while they render (inside a CUDA stream capture, a real-time frame
  * loop with a fixed memory budget, a host callback).  No counterpart in the
@@ -249,6 +263,8 @@ typedef struct vr_render_job {
     uint32_t first_sample;
     uint64_t seed;
     float* rgba_device;       /* RGBA f32 accumulation buffer, += like vr_render */
+    float* albedo_device;     /* optional first-hit AOV buffers, += like          */
+    float* normal_device;     /* vr_render_aov_device (both set or both NULL)     */
 } vr_render_job;
 
 typedef struct vr_batch vr_batch;

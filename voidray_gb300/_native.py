@@ -72,7 +72,7 @@ class vr_render_settings(C.Structure):
 class vr_render_job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("settings", vr_render_settings), ("samples", C.c_uint32),
                 ("width", C.c_uint32), ("height", C.c_uint32), ("first_sample", C.c_uint32), ("seed", C.c_uint64),
-                ("rgba_device", C.c_void_p)]
+                ("rgba_device", C.c_void_p), ("albedo_device", C.c_void_p), ("normal_device", C.c_void_p)]
 
 
 class vr_color_management(C.Structure):
@@ -104,6 +104,8 @@ _SIGS = [
     ("vr_scene_set_camera", C.c_int, [P, P]),
     ("vr_render", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32]),
     ("vr_render_device", C.c_int, [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, P]),
+    ("vr_render_aov_device", C.c_int,
+     [P, P, C.c_uint32, P, P, P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, P]),
     ("vr_render_stats_get", C.c_int, [P, P]),
     ("vr_tonemap", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float]),
     ("vr_tonemap_device", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float, P]),

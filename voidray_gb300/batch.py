@@ -23,10 +23,13 @@ class RenderJob:
     height: int
     seed: int = 0
     first_sample: int = 0
+    albedo_device: int = 0    # optional first-hit AOV buffers (both or neither), same layout as rgba
+    normal_device: int = 0
 
     def to_c(self) -> N.vr_render_job:
         return N.vr_render_job(self.scene.handle.value, self.settings.to_c(), int(self.samples), int(self.width),
-                               int(self.height), int(self.first_sample), int(self.seed), int(self.rgba_device))
+                               int(self.height), int(self.first_sample), int(self.seed), int(self.rgba_device),
+                               int(self.albedo_device) or None, int(self.normal_device) or None)
 
 
 class Batch:

@@ -67,6 +67,7 @@ vr_status ensure_buf(DevBuf& b, size_t bytes) {
 struct Engine {
     vr::PathState ps{};
     uint32_t cap = 0, bounces = 0;
+    bool aov = false;
     std::vector<void*> allocs;
     uint64_t bytes = 0;
     vr::Job* table = nullptr;  // device Job entries (waves x jobs of one chunk)
@@ -77,6 +78,7 @@ struct Engine {
         allocs.clear();
         ps = vr::PathState{};
         cap = bounces = 0;
+        aov = false;
         bytes = 0;
         table = nullptr;
         table_cap = 0;
@@ -92,11 +94,12 @@ struct Engine {
         return VR_OK;
     }
     // (re)allocates for `c` slots and reference-estimator attenuation of depth `b`
-    vr_status ensure(uint32_t c, uint32_t b, cudaStream_t sync_stream) {
-        if (cap >= c && bounces >= b && table) return VR_OK;
+    vr_status ensure(uint32_t c, uint32_t b, cudaStream_t sync_stream, bool want_aov = false) {
+        if (cap >= c && bounces >= b && table && (aov || !want_aov)) return VR_OK;
         if (sync_stream) VR_CK(cudaStreamSynchronize(sync_stream));
         c = std::max(c, cap);
         b = std::max(b, bounces);
+        want_aov = want_aov || aov;
         release();
         vr_status st;
 #define EA(field, n)                                  \
@@ -118,6 +121,7 @@ struct Engine {
         EA(s_path, (size_t)c);
         EA(counts, (size_t)vr::MAX_JOBS * vr::JOB_COUNTERS);
         EA(cursors, 2 * (size_t)vr::MAX_DEPTH_SLOTS);
+        if (want_aov) EA(aov, 2 * (size_t)c);
 #undef EA
         table_cap = 4096;
         if ((st = alloc(&table, table_cap)) != VR_OK) {
@@ -127,6 +131,7 @@ struct Engine {
         ps.cap = c;
         cap = c;
         bounces = b;
+        aov = want_aov;
         return VR_OK;
     }
 };
@@ -185,6 +190,7 @@ struct vr_scene {
     Engine eng;                            // render scratch
     float4* psum = nullptr;
     uint32_t psum_cap = 0;
+    DevBuf aov_psum;                       // first-hit AOV sums (2 float4 per pixel)
     DevBuf stage_a, stage_b;               // host-call staging
     Instr instr;
 };
@@ -255,6 +261,8 @@ struct HostJob {
     uint64_t done = 0;
     float4* rgba;
     float inv_total;
+    float4* albedo = nullptr;  // optional AOV outputs (accumulated like rgba)
+    float4* normal = nullptr;
 };
 
 // Plans waves of at most `cap` slots over the jobs (each wave takes, in job
@@ -345,6 +353,11 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
             for (size_t i : wh.finishing) {
                 const HostJob& j = jobs[i];
                 VR_CK(vr::launch_finalize(j.tmpl.psum, j.rgba, j.tmpl.num_pixels, j.inv_total, cs));
+                if (j.tmpl.aov_psum) {
+                    VR_CK(vr::launch_finalize(j.tmpl.aov_psum, j.albedo, j.tmpl.num_pixels, j.inv_total, cs));
+                    VR_CK(vr::launch_finalize(j.tmpl.aov_psum + j.tmpl.num_pixels, j.normal, j.tmpl.num_pixels,
+                                              j.inv_total, cs));
+                }
             }
             ++waves;
         }
@@ -493,6 +506,7 @@ vr_status vr_scene_destroy(vr_scene* s) {
     if (s->instr.work) cudaFree(s->instr.work);
     s->eng.release();
     if (s->psum) cudaFree(s->psum);
+    if (s->aov_psum.p) cudaFree(s->aov_psum.p);
     if (s->stage_a.p) cudaFree(s->stage_a.p);
     if (s->stage_b.p) cudaFree(s->stage_b.p);
     for (void* p : s->allocs) cudaFree(p);
@@ -554,6 +568,45 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
         return r;
     s->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return VR_OK;
+}
+
+vr_status vr_render_aov_device(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba,
+                               float* albedo, float* normal, uint32_t w, uint32_t h, uint64_t seed,
+                               uint32_t first_sample, void* stream) {
+    vr_status r = validate_render(s, st, w, h);
+    if (r != VR_OK) return r;
+    if (!rgba || !albedo || !normal) return fail(VR_ERR_INVALID, "rgba, albedo and normal must be set");
+    if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
+    if (samples == 0) return VR_OK;
+    cudaStream_t cs = pick(s, stream);
+    const uint32_t np = w * h;
+    const uint64_t total = (uint64_t)samples * np;
+    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
+    if (cap > (1ull << 28)) cap = 1ull << 28;
+    if (cap > total) cap = total;
+    const uint32_t att_depth = st->estimator == VR_EST_REFERENCE ? st->max_bounces : 0;
+    if ((r = s->eng.ensure((uint32_t)cap, att_depth, s->stream, true)) != VR_OK) return r;
+    if (s->psum_cap < np) {
+        VR_CK(cudaStreamSynchronize(s->stream));
+        if (s->psum) cudaFree(s->psum);
+        s->psum = nullptr;
+        s->psum_cap = 0;
+        VR_CK(cudaMalloc(&s->psum, (size_t)np * sizeof(float4)));
+        s->psum_cap = np;
+    }
+    if (s->aov_psum.bytes < 2 * (size_t)np * sizeof(float4)) {
+        VR_CK(cudaStreamSynchronize(s->stream));
+        if ((r = ensure_buf(s->aov_psum, 2 * (size_t)np * sizeof(float4))) != VR_OK) return r;
+    }
+    VR_CK(cudaMemsetAsync(s->psum, 0, (size_t)np * sizeof(float4), cs));
+    VR_CK(cudaMemsetAsync(s->aov_psum.p, 0, 2 * (size_t)np * sizeof(float4), cs));
+    HostJob j = make_job(s->view, st, samples, rgba, w, h, seed, first_sample, s->psum);
+    j.tmpl.aov_psum = static_cast<float4*>(s->aov_psum.p);
+    j.albedo = reinterpret_cast<float4*>(albedo);
+    j.normal = reinterpret_cast<float4*>(normal);
+    std::vector<HostJob> jobs{j};
+    return run_waves(jobs, s->eng.ps, (uint32_t)cap, s->eng.table, s->eng.table_cap, s->status, s->totals, &s->instr, cs,
+                     &s->stats.wavefronts);
 }
 
 vr_status vr_render(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba, uint32_t w, uint32_t h,
@@ -634,22 +687,27 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
     vr_status r;
     uint64_t total = 0, pixels = 0;
     uint32_t att_depth = 0;
+    bool want_aov = false;
     for (uint32_t i = 0; i < count; ++i) {
         const vr_render_job& j = jobs[i];
         if ((r = validate_render(j.scene, &j.settings, j.width, j.height)) != VR_OK)
             return fail(r, "job " + std::to_string(i) + ": " + g_err);
         if (!j.rgba_device) return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": rgba is NULL");
+        if (!j.albedo_device != !j.normal_device)
+            return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": set both AOV buffers or neither");
+        const bool aov = j.albedo_device && j.samples;
+        want_aov = want_aov || aov;
         if ((uint64_t)j.first_sample + j.samples >= (1ull << 31))
             return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": sample index out of range");
         if (j.scene->device != b->device) return fail(VR_ERR_INVALID, "job " + std::to_string(i) + ": other device");
         total += (uint64_t)j.samples * j.width * j.height;
-        pixels += (uint64_t)j.width * j.height;
+        pixels += (uint64_t)j.width * j.height * (aov ? 3 : 1);
         if (j.settings.estimator == VR_EST_REFERENCE) att_depth = std::max(att_depth, j.settings.max_bounces);
     }
     if (total == 0) return VR_OK;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     const uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
-    if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs)) != VR_OK) return r;
+    if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs, want_aov)) != VR_OK) return r;
     if (b->psum.bytes < pixels * sizeof(float4)) {
         VR_CK(cudaStreamSynchronize(cs));
         if ((r = ensure_buf(b->psum, pixels * sizeof(float4))) != VR_OK) return r;
@@ -664,6 +722,12 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
         hj.push_back(make_job(j.scene->view, &j.settings, j.samples, j.rgba_device, j.width, j.height, j.seed,
                               j.first_sample, ps));
         ps += (size_t)j.width * j.height;
+        if (j.albedo_device) {
+            hj.back().tmpl.aov_psum = ps;
+            hj.back().albedo = reinterpret_cast<float4*>(j.albedo_device);
+            hj.back().normal = reinterpret_cast<float4*>(j.normal_device);
+            ps += 2 * (size_t)j.width * j.height;
+        }
     }
     auto t0 = std::chrono::steady_clock::now();
     if ((r = run_waves(hj, b->eng.ps, (uint32_t)cap, b->eng.table, b->eng.table_cap, b->status, b->totals, nullptr, cs,

@@ -562,6 +562,10 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k)
             float prev_pdf = thr4.w;
             if (prim == MISS) {
                 const V3 le = env_eval(s, rd);
+                if (k == 0 && j.aov_psum) {  // first-hit AOVs of a miss: environment (clamped), no normal
+                    ps.aov[p] = make_float4(fminf(le.x, 1.0f), fminf(le.y, 1.0f), fminf(le.z, 1.0f), 0.0f);
+                    ps.aov[ps.cap + p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
                 if (nee_mode) {
                     float wgt = 1.0f;
                     if (prev_pdf >= 0.0f && s.env_is) {
@@ -589,6 +593,13 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k)
                 hit.t = t;
                 hit.front = dot(rd, normal) < 0.0f;
                 hit.normal = hit.front ? normal : -normal;
+                if (k == 0 && j.aov_psum) {  // first-hit AOVs: surface colour (1 for glass), shading normal
+                    const V3 al = (m.kind == M_DIEL) ? v3(1.0f, 1.0f, 1.0f)
+                                                     : v3(fminf(m.color[0], 1.0f), fminf(m.color[1], 1.0f),
+                                                          fminf(m.color[2], 1.0f));
+                    ps.aov[p] = make_float4(al.x, al.y, al.z, 0.0f);
+                    ps.aov[ps.cap + p] = make_float4(hit.normal.x, hit.normal.y, hit.normal.z, 0.0f);
+                }
                 if (rp.render_mode != 1) {
                     const V3 nn = normalize(hit.normal);
                     const V3 c = (0.5f * nn) + v3(1.0f, 1.0f, 1.0f) * 0.5f;
@@ -746,6 +757,21 @@ __global__ void k_accumulate(Wave w, PathState ps) {
             acc.z = acc.z + rr.z;
         }
         j.psum[px] = acc;
+        if (j.aov_psum) {
+            float4 aa = j.aov_psum[px], an = j.aov_psum[NP + px];
+            for (uint64_t g = s_begin * NP + px; g < g1; g += NP) {
+                const uint32_t q = j.base + (uint32_t)(g - g0);
+                const float4 a = ps.aov[q], nn = ps.aov[ps.cap + q];
+                aa.x += a.x;
+                aa.y += a.y;
+                aa.z += a.z;
+                an.x += nn.x;
+                an.y += nn.y;
+                an.z += nn.z;
+            }
+            j.aov_psum[px] = aa;
+            j.aov_psum[NP + px] = an;
+        }
     }
 }
 

@@ -27,6 +27,7 @@ struct Job {
     uint32_t base;          // first slot of the job's segment in every per-path array
     uint32_t num_pixels, width, height, first_sample;
     float4* psum;           // per-pixel running sums (float4 per pixel)
+    float4* aov_psum;       // optional: first-hit albedo sums [0, np), normal sums [np, 2 np)
 };
 
 constexpr uint32_t MAX_JOBS = 256;                       // jobs per wavefront
@@ -61,6 +62,7 @@ struct PathState {
     uint32_t* s_path;
     uint32_t* counts;   // MAX_JOBS * JOB_COUNTERS per-job queue sizes
     uint32_t* cursors;  // 2 * MAX_DEPTH_SLOTS fetch cursors: [k] extend, [M + k] shadow
+    float4* aov;        // 2*cap, when some job wants AOVs: first-hit albedo [0, cap), normal [cap, 2 cap)
 };
 
 // Batch closest/any hit; `counter` is a device word the persistent kernel

@@ -507,6 +507,22 @@ def iterative_render(target: CpuRenderTarget, scene: SceneAcceleration, settings
     check(lib().vr_render(scene.handle, C.byref(st), int(samples), ptr(buf), w, h, int(seed), int(first_sample)))
 
 
+def render_device(scene: SceneAcceleration, settings: RenderSettings, samples: int, rgba_device: int, width: int,
+                  height: int, seed: int = 0, first_sample: int = 0, stream: int = 0, albedo_device: int = 0,
+                  normal_device: int = 0) -> None:
+    """iterative_render into device buffers (raw CUDA pointers, RGBA f32), enqueued on `stream`.
+    With albedo_device/normal_device set, also accumulates the first-hit feature buffers."""
+    st = settings.to_c()
+    s = C.c_void_p(stream or None)
+    if albedo_device or normal_device:
+        check(lib().vr_render_aov_device(scene.handle, C.byref(st), int(samples), C.c_void_p(rgba_device),
+                                         C.c_void_p(albedo_device), C.c_void_p(normal_device), int(width),
+                                         int(height), int(seed), int(first_sample), s))
+    else:
+        check(lib().vr_render_device(scene.handle, C.byref(st), int(samples), C.c_void_p(rgba_device), int(width),
+                                     int(height), int(seed), int(first_sample), s))
+
+
 def tonemap(rgba: np.ndarray, cm: ColorManagementSettings, scale: float) -> np.ndarray:
     """post_process.glsl:23-49 on the GPU."""
     rgba = np.ascontiguousarray(rgba, dtype=np.float32)
