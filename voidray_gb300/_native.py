@@ -1,4 +1,4 @@
-"""ctypes binding of ``include/voidray_gpu.h`` (libvoidray_gb300.so).
+"""ctypes binding of ``include/voidray_gpu.h`` and ``include/voidray_denoise.h`` (libvoidray_gb300.so).
 
 The library is the only compute path: if it is missing, importing anything
 that renders raises immediately; nothing falls back to the CPU.
@@ -84,6 +84,16 @@ class vr_render_stats(C.Structure):
                 ("wavefronts", C.c_uint64), ("ms", C.c_double), ("error_flags", C.c_uint32), ("pad_", C.c_uint32)]
 
 
+class vr_denoiser_info(C.Structure):
+    _fields_ = [("param_count", C.c_uint64), ("steps", C.c_uint64), ("workspace_bytes", C.c_uint64),
+                ("flops_per_pixel", C.c_double), ("num_layers", C.c_uint32), ("input_channels", C.c_uint32)]
+
+
+class vr_denoiser_layer(C.Structure):
+    _fields_ = [("c1", C.c_uint32), ("c2", C.c_uint32), ("up1", C.c_uint32), ("cout", C.c_uint32),
+                ("relu", C.c_uint32), ("level", C.c_uint32), ("w_offset", C.c_uint64), ("b_offset", C.c_uint64)]
+
+
 class vr_instrument(C.Structure):
     _fields_ = [("stage_ms", C.c_double * 8), ("stage_launches", C.c_uint64 * 8),
                 ("extend_node_visits", C.c_uint64), ("extend_tri_tests", C.c_uint64),
@@ -125,6 +135,24 @@ _SIGS = [
     ("vr_batch_stats_get", C.c_int, [P, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),
+    # include/voidray_denoise.h
+    ("vr_denoiser_create", C.c_int, [C.c_uint64, P]),
+    ("vr_denoiser_destroy", C.c_int, [P]),
+    ("vr_denoiser_info_get", C.c_int, [P, P]),
+    ("vr_denoiser_layer_get", C.c_int, [C.c_uint32, P]),
+    ("vr_denoiser_set_loss", C.c_int, [P, C.c_int32]),
+    ("vr_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
+    ("vr_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
+    ("vr_denoise_device", C.c_int, [P, P, P, P, C.c_float, P, C.c_uint32, C.c_uint32, P]),
+    ("vr_denoiser_gradients_device", C.c_int,
+     [P, P, P, P, P, C.c_float, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]),
+    ("vr_denoiser_train_step_device", C.c_int,
+     [P, P, P, P, P, C.c_float, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, P, P]),
+    ("vr_dn_conv3x3_device", C.c_int,
+     [P, C.c_uint32, C.c_int32, P, C.c_uint32, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+      C.c_int32, P]),
+    ("vr_dn_conv3x3_wgrad_device", C.c_int,
+     [P, P, C.c_uint32, C.c_int32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P]),
 ]
 EXPORTED = [name for name, _, _ in _SIGS]
 

@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libvoidray_gb300.so"
 
-SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu"]
+SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "dn_kernels.cu", "dn_unet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -51,7 +51,7 @@ def _stale(obj: Path, deps: list[Path]) -> bool:
 def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "voidray_gpu.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((PKG.parent / "include").glob("*.h"))
     procs = []
     objs = []
     for src in SOURCES:

@@ -176,6 +176,11 @@ struct Instr {
 
 }  // namespace
 
+namespace vr {
+vr_status set_error(vr_status s, const std::string& message) { return fail(s, message); }
+bool device_usable() { return device_ok(); }
+}  // namespace vr
+
 struct vr_scene {
     int device = 0;
     cudaStream_t stream = nullptr;

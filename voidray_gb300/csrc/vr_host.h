@@ -9,6 +9,11 @@
 
 namespace vr {
 
+// Sets the thread-local message vr_last_error() returns; returns s.
+vr_status set_error(vr_status s, const std::string& message);
+// True when a CUDA device is usable (clears the error a failed probe leaves).
+bool device_usable();
+
 // Environment importance-sampling tables (no reference counterpart).
 struct EnvTables {
     uint32_t W = 0, H = 0;
