@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-work-count", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="library default launch shapes")
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-size", type=int, default=256, help="job image side")
@@ -163,14 +164,19 @@ def cpu_baseline(scene, st, args, budget_s):
 def serving_benchmark(args):
     """Poisson stream of render jobs drawn like the plain render scene (four
     resident displaced icospheres of 18k-800k triangles with the sky HDRI),
-    each to a target relative MSE (estimated from the job's two half-buffers,
-    checked against a 4096-spp reference after the run).  Served: continuous
-    batching of every admitted job in one launch per pass.  Plain: the same
-    requests rendered one at a time (one active job)."""
+    each to a target relative MSE (estimated from the job's two half-buffers
+    without a reference, checked against a 4096-spp reference after the run).
+    plain: the requests rendered one at a time (one active job, the plain
+    single-scene GPU path); served: continuous batching of every admitted job
+    in one launch per pass; served_denoised: the same with AOVs and the
+    learned denoiser, each job returning the plain mean or the denoised blend,
+    whichever is predicted to be better."""
     import numpy as np
+    import torch
 
     import voidray_gb300 as vr
     from voidray_gb300 import workloads as W
+    from voidray_gb300.denoise import Denoiser
     from voidray_gb300.scene import Estimator, RenderSettings
     from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig, poisson_arrivals
 
@@ -187,56 +193,123 @@ def serving_benchmark(args):
         st = RenderSettings(total_samples=1, max_bounces=8 + k, rr_depth=3, estimator=Estimator.NEE,
                             firefly_clamp=3.0)
         pool.append((acc, st, int(acc.info().device_bytes), s.num_triangles()))
+    # 4096-spp references, one per scene (all jobs of a scene share its camera)
+    refs = {}
+    for acc, st, *_ in pool:
+        t = vr.CpuRenderTarget(size, size)
+        vr.iterative_render(t, acc, RenderSettings(**{**st.__dict__, "total_samples": 4096}), 4096, seed=99)
+        refs[id(acc)] = t.buffer[..., :3].astype(np.float64)
+
+    def relmse(x, r):
+        return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
     rng = np.random.default_rng(5)
     arrivals = poisson_arrivals(args.serve_rate, args.serve_jobs, seed=5)
-    requests = []
-    for i, t in enumerate(arrivals):
-        acc, st, nbytes, _ = pool[int(rng.integers(0, len(pool)))]
-        requests.append((float(t), JobRequest(acc, st, size, size, max_samples=2048, target_relmse=args.serve_target,
-                                              seed=1000 + i, scene_bytes=nbytes)))
+    picks = [int(rng.integers(0, len(pool))) for _ in arrivals]
+    net = Denoiser.pretrained()
     out = {"jobs": args.serve_jobs, "rate_per_s": args.serve_rate, "image": f"{size}x{size}",
            "target_relmse": args.serve_target, "scenes_triangles": [p[3] for p in pool],
-           "error_estimate": "half-buffer variance of the mean / (m^2 + 1e-2)"}
-    backend = GpuBackend()
-    results = {}
+           "error_estimate": "half-buffer variance of the mean / (m^2 + 1e-2); denoised: reference-free "
+                             "prediction of the blend's error from the halves",
+           "reference": "4096 spp per scene", "denoiser": "U-Net 32/64/128/256, bf16, shipped weights"}
+    spp_pass = 32
     # served: as many active jobs as fill a ~16M-path wavefront per pass, so
     # that jobs complete in admission order instead of all at the end
-    spp_pass = 32
     fill = max(1, (1 << 24) // (size * size * spp_pass))
     out["served_max_active"] = fill
-    for name, active in (("served", fill), ("plain", 1)):
-        srv = Server(backend, ServerConfig(memory_budget=150 * 10**9, max_active=active, spp_per_pass=32,
+    modes = (("plain", 1, False), ("served", fill, False), ("served_denoised", fill, True))
+    for name, active, dn in modes:
+        backend = GpuBackend(denoiser=net if dn else None)
+        requests = []
+        for i, t in enumerate(arrivals):
+            acc, st, nbytes, _ = pool[picks[i]]
+            requests.append((float(t), JobRequest(acc, st, size, size, max_samples=2048,
+                                                  target_relmse=args.serve_target, seed=1000 + i,
+                                                  scene_bytes=nbytes, denoise=dn)))
+        srv = Server(backend, ServerConfig(memory_budget=150 * 10**9, max_active=active, spp_per_pass=spp_pass,
                                            min_samples=64))
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        srv.run([(t, r) for t, r in requests])
+        srv.run(requests)
         wall = time.perf_counter() - t0
         lat = srv.latencies()
-        samples = sum(j.samples * j.req.width * j.req.height for j in srv.jobs.values())
+        jobs = list(srv.jobs.values())
+        samples = sum(j.samples * j.req.width * j.req.height for j in jobs)
+        errs = [relmse(j.result.astype(np.float64), refs[id(j.req.scene)]) for j in jobs]
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "jobs_per_s": len(lat) / wall, "samples_per_s": samples / wall, "wall_s": wall,
-                     "passes": srv.passes,
-                     "mean_spp": float(np.mean([j.samples for j in srv.jobs.values()]))}
-        results[name] = srv
-    # true error of the served results against a 4096-spp reference per scene
-    refs = {}
-    errs = []
-    for j in results["served"].jobs.values():
-        key = id(j.req.scene)
-        if key not in refs:
-            t = vr.CpuRenderTarget(size, size)
-            st = RenderSettings(**{**j.req.settings.__dict__, "total_samples": 4096})
-            vr.iterative_render(t, j.req.scene, st, 4096, seed=99)
-            refs[key] = t.buffer[..., :3].astype(np.float64)
-        r = refs[key]
-        x = j.result.astype(np.float64)
-        errs.append(float(np.mean((x - r) ** 2 / (r * r + 1e-2))))
-    out["served"]["true_relmse_p50"] = float(np.median(errs))
-    out["served"]["true_relmse_p99"] = float(np.percentile(errs, 99))
-    out["p50_speedup"] = out["plain"]["p50_s"] / out["served"]["p50_s"]
-    out["throughput_ratio"] = out["served"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
+                     "passes": srv.passes, "max_active": active,
+                     "mean_spp": float(np.mean([j.samples for j in jobs])),
+                     "true_relmse_p50": float(np.median(errs)), "true_relmse_p99": float(np.percentile(errs, 99)),
+                     "true_relmse_max": float(np.max(errs))}
+        if dn:
+            out[name]["denoised_jobs"] = int(sum(j.alpha > 0 for j in jobs))
+            out[name]["mean_alpha"] = float(np.mean([j.alpha for j in jobs]))
+            out[name]["denoiser_calls"] = backend.denoise_calls
+        backend.batch.destroy()
+    out["p50_speedup_served"] = out["plain"]["p50_s"] / out["served"]["p50_s"]
+    out["p50_speedup_served_denoised"] = out["plain"]["p50_s"] / out["served_denoised"]["p50_s"]
+    out["throughput_ratio_served"] = out["served"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
+    out["throughput_ratio_served_denoised"] = out["served_denoised"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
+    out["equal_time"] = denoiser_equal_time(pool, refs, net, size)
+    net.destroy()
     for acc, *_ in pool:
         acc.destroy()
     return out
+
+
+def denoiser_equal_time(pool, refs, net, size):
+    """Acceptance rule of the denoiser: a denoised frame must beat the plain
+    frame rendered in the same time.  For each scene and input spp: time the
+    AOV render plus the denoiser (CUDA events), render the plain frame with
+    as many samples as fit in that time, and compare both with the 4096-spp
+    reference."""
+    import numpy as np
+    import torch
+
+    from voidray_gb300.scene import render_device
+
+    stream = torch.cuda.Stream()
+    h = stream.cuda_stream
+    rows = []
+    bufs = [torch.zeros((size, size, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    for k, (acc, st, *_) in enumerate(pool):
+        # warm-up: scratch allocation of the AOV render and the denoiser workspace
+        render_device(acc, st, 1, bufs[0].data_ptr(), size, size, seed=6, stream=h,
+                      albedo_device=bufs[1].data_ptr(), normal_device=bufs[2].data_ptr())
+        net.denoise(bufs[0], bufs[1], bufs[2], 1.0, bufs[3], size, size, stream=h)
+        render_device(acc, st, 1, bufs[0].data_ptr(), size, size, seed=6, stream=h)
+        for spp in (4, 16, 64, 256):
+            for b in bufs:
+                b.zero_()
+            torch.cuda.synchronize()
+            t_r = timed(lambda: render_device(acc, st, spp, bufs[0].data_ptr(), size, size, seed=7, stream=h,
+                                              albedo_device=bufs[1].data_ptr(), normal_device=bufs[2].data_ptr()))
+            t_d = timed(lambda: net.denoise(bufs[0], bufs[1], bufs[2], 1.0 / spp, bufs[3], size, size, stream=h))
+            den = bufs[3][..., :3].double().cpu().numpy()
+            # plain frame in the same time: samples scale with the time budget
+            t_plain_1 = timed(lambda: render_device(acc, st, spp, bufs[0].data_ptr(), size, size, seed=8, stream=h))
+            spp_eq = max(spp, int(spp * (t_r + t_d) / max(t_plain_1, 1e-3)))
+            bufs[0].zero_()
+            t_eq = timed(lambda: render_device(acc, st, spp_eq, bufs[0].data_ptr(), size, size, seed=8, stream=h))
+            plain = (bufs[0][..., :3].double() / spp_eq).cpu().numpy()
+            r = refs[id(acc)]
+            e_d = float(np.mean((den - r) ** 2 / (r * r + 1e-2)))
+            e_p = float(np.mean((plain - r) ** 2 / (r * r + 1e-2)))
+            rows.append({"scene": k, "spp": spp, "render_ms": t_r, "denoise_ms": t_d, "plain_spp": spp_eq,
+                         "plain_ms": t_eq, "denoised_relmse": e_d, "plain_relmse": e_p,
+                         "denoised_wins": e_d < e_p})
+    return rows
 
 
 def run_reference(args):
@@ -311,6 +384,13 @@ def main():
     info = acc.info()
     w, h, spp = args.width, args.height, args.spp
     npx = w * h
+    tuning = None
+    if not args.no_autotune and not args.wavefront:
+        # launch shapes for this workload class (cached per GPU / scene / image / spp bucket)
+        from voidray_gb300 import autotune
+
+        tuning = autotune.tune(acc, st, w, h, spp)
+        st = autotune.apply(tuning, st)
     cst = st.to_c()
     # a dedicated stream: its handle is non-zero, so the library launches on it
     # and the CUDA events below bracket the kernels (NULL would select the
@@ -437,7 +517,8 @@ def main():
                     "bvh": {"nodes": int(info.num_nodes), "max_depth": int(info.max_depth),
                             "sah_cost": round(info.sah_cost, 2), "build_s": round(build_s, 2)},
                     "wavefront_paths": st.wavefront_paths or (1 << 26),
-                    "parallelism": f"replicas x{world}, disjoint sample ranges"})
+                    "parallelism": f"replicas x{world}, disjoint sample ranges",
+                    "tuning": tuning})
         line = {
             "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",

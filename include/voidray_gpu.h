@@ -276,6 +276,25 @@ vr_status vr_batch_destroy(vr_batch* batch);
 vr_status vr_batch_render(vr_batch* batch, const vr_render_job* jobs, uint32_t count, void* stream);
 /* Waits for `stream` and reports kernel-side errors. */
 vr_status vr_batch_synchronize(vr_batch* batch, void* stream);
+/* Launch shapes of the shade and raygen stages (process-wide; the autotuner
+ * in voidray_gb300/autotune.py sets them).  Results do not depend on them. */
+typedef struct vr_tuning {
+    uint32_t shade_block;          /* 64, 128 or 256 threads (default 256)   */
+    uint32_t shade_blocks_per_sm;  /* resident blocks per SM, 1-32 (8)       */
+    uint32_t raygen_block;         /* 64, 128 or 256 threads (256)           */
+    uint32_t generation;           /* out: bumped by every set                */
+} vr_tuning;
+vr_status vr_tuning_get(vr_tuning* tuning);
+vr_status vr_tuning_set(const vr_tuning* tuning);
+
+/* With graphs enabled, every wavefront's stage sequence (raygen, each depth's
+ * extend / shade / shadow, accumulate) is captured once as a CUDA graph and
+ * replayed on later calls with the same job-set shape (job count, paths,
+ * depth); the per-call data (sample offsets, seeds, scenes) is read from the
+ * device job table, so results are identical to direct launches.  Needs a
+ * non-NULL stream; off by default.  No counterpart in the reference. */
+vr_status vr_batch_set_graphs(vr_batch* batch, int32_t enable);
+vr_status vr_batch_graph_stats(vr_batch* batch, uint64_t* captures, uint64_t* replays);
 
 typedef struct vr_render_stats {
     uint64_t paths;          /* camera paths traced                            */

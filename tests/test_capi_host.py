@@ -113,3 +113,31 @@ def test_settings_defaults_match_reference(native):
            (100, 0.1, vr.RenderMode.Full, 3.0, 10)
     cm = vr.ColorManagementSettings()
     assert (cm.tonemap, cm.gamma, cm.exposure, cm.transparent) == (vr.Tonemap.NONE, 2.2, 0.0, True)
+
+
+def test_tuning_knobs_roundtrip_and_validation(native):
+    from voidray_gb300 import autotune as T
+
+    before = T.get_tuning()
+    try:
+        T.set_tuning({"shade_block": 128, "shade_blocks_per_sm": 16, "raygen_block": 64})
+        assert T.get_tuning() == {"shade_block": 128, "shade_blocks_per_sm": 16, "raygen_block": 64}
+        for bad in ({"shade_block": 96, "shade_blocks_per_sm": 8, "raygen_block": 256},
+                    {"shade_block": 256, "shade_blocks_per_sm": 0, "raygen_block": 256},
+                    {"shade_block": 256, "shade_blocks_per_sm": 8, "raygen_block": 512}):
+            with pytest.raises(native.VoidrayError):
+                T.set_tuning(bad)
+        assert T.get_tuning()["shade_block"] == 128
+    finally:
+        T.set_tuning(before)
+
+
+def test_tuning_cache_keys(tmp_path, monkeypatch):
+    from voidray_gb300 import autotune as T
+
+    monkeypatch.setenv("VOIDRAY_TUNING_CACHE", str(tmp_path / "t.json"))
+    k1 = T.bucket_key("GB300", 2_000_000, 1920 * 1080, 256, 1)
+    assert k1 == T.bucket_key("GB300", 1_500_000, 1900 * 1080, 300, 1)   # same buckets
+    assert k1 != T.bucket_key("GB300", 2_000_000, 1920 * 1080, 256, 0)
+    T.save_cache({k1: {"wavefront_paths": 1 << 25}})
+    assert T.load_cache()[k1]["wavefront_paths"] == 1 << 25

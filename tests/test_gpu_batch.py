@@ -81,3 +81,39 @@ def test_batch_validation(gpu):
     b = Batch()
     with pytest.raises(vr.VoidrayError):
         b.render([RenderJob(acc, st, 1, 0, 8, 8)])
+
+
+@pytest.mark.parametrize("max_wave", [0, 5000])
+def test_graph_replays_equal_direct_launches(gpu, max_wave):
+    """Progressive passes of one job set: with graphs the first pass captures
+    each distinct wave shape and later passes replay them; every pass's
+    images equal the direct launches bit for bit (the jobs change their
+    sample offsets and seeds between passes through the device job table)."""
+    import torch
+
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.batch import Batch, RenderJob
+
+    jobs = _jobs(vr, W)
+    stream = torch.cuda.Stream()
+    results = {}
+    for graphs in (False, True):
+        batch = Batch(max_wave)
+        batch.set_graphs(graphs)
+        outs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, _, _, w, h, _, _ in jobs]
+        passes = 4
+        for p in range(passes):
+            rj = [RenderJob(acc, st, 2, o.data_ptr(), w, h, seed, first + 2 * p)
+                  for (acc, st, spp, w, h, seed, first), o in zip(jobs, outs)]
+            batch.render(rj, stream.cuda_stream)
+            batch.synchronize(stream.cuda_stream)
+        results[graphs] = [o.cpu().numpy() for o in outs]
+        caps, reps = batch.graph_stats()
+        if graphs:
+            assert caps >= 1 and reps >= caps * (passes - 1)
+        else:
+            assert caps == 0 and reps == 0
+        batch.destroy()
+    for a, b in zip(results[False], results[True]):
+        assert np.array_equal(a, b)

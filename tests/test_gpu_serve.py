@@ -47,3 +47,39 @@ def test_served_same_alone_and_in_mix(gpu):
     assert r0[1:] == r1[1:]
     assert np.array_equal(r0[0], r1[0])
     assert r0[1] < 256  # stopped on the error estimate
+
+
+def test_denoised_serving_same_alone_and_in_mix(gpu):
+    """With the denoiser in the loop (AOV buffers, blended output) a job's
+    stopping point, blend weight and image still depend only on the job."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.denoise import Denoiser
+    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig
+
+    scenes = _scenes(vr, W)
+    cfg = ServerConfig(spp_per_pass=8, min_samples=16)
+    net = Denoiser.pretrained()
+
+    def run(mix):
+        backend = GpuBackend(denoiser=net, denoise_below=1e9)
+        srv = Server(backend, cfg)
+        acc, st = scenes[1]
+        jid = srv.submit(JobRequest(acc, st, 40, 32, max_samples=128, target_relmse=2e-2, seed=5, denoise=True))
+        for k in range(mix):
+            a2, s2 = scenes[k % 2]
+            srv.submit(JobRequest(a2, s2, 24 + 8 * k, 16, max_samples=64, target_relmse=1e-4, seed=10 + k,
+                                  denoise=bool(k % 2)))
+        while not srv.idle():
+            srv.step()
+        j = srv.status(jid)
+        assert backend.denoise_calls > 0
+        return j.result, j.samples, j.alpha, j.estimate
+
+    try:
+        r0 = run(0)
+        r1 = run(3)
+        assert r0[1:] == r1[1:]
+        assert np.array_equal(r0[0], r1[0])
+    finally:
+        net.destroy()

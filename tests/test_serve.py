@@ -131,3 +131,62 @@ def test_poisson_replay():
     s.run([(float(t), req(seed=i, target=5e-3, max_samples=128)) for i, t in enumerate(arr)])
     lat = s.latencies()
     assert len(lat) == 12 and np.all(lat > 0)
+
+
+def _box(x, r=2):
+    """(2r+1)^2 box filter with edge clamping (a linear stand-in denoiser)."""
+    pad = np.pad(x, ((r, r), (r, r), (0, 0)), mode="edge")
+    out = np.zeros_like(x)
+    for dy in range(2 * r + 1):
+        for dx in range(2 * r + 1):
+            out += pad[dy:dy + x.shape[0], dx:dx + x.shape[1]]
+    return out / (2 * r + 1) ** 2
+
+
+def _halves(truth, sigma, na, nb, seed):
+    rng = np.random.default_rng(seed)
+    a = truth + sigma * rng.standard_normal(truth.shape) / np.sqrt(na)
+    b = truth + sigma * rng.standard_normal(truth.shape) / np.sqrt(nb)
+    return a, b, (a * na + b * nb) / (na + nb)
+
+
+def _relmse(x, r):
+    return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
+
+@pytest.mark.parametrize("na,nb", [(64, 64), (96, 64)])
+def test_blend_prediction_tracks_the_true_error(na, nb):
+    """The reference-free prediction of the blended output's error (module
+    docstring of serve.py) against the error measured with the known truth,
+    for a linear smoothing 'denoiser' whose bias and noise are both sizeable."""
+    from voidray_gb300.serve import blend_prediction
+
+    yy, xx = np.mgrid[0:96, 0:96] / 96.0
+    truth = np.stack([0.2 + 0.6 * (xx > 0.5) + 0.2 * yy, 0.5 + 0.3 * np.sin(6 * xx), 0.3 + 0.0 * yy], -1)
+    sigma = 0.8 * (0.3 + truth)
+    pred_p, pred_y, true_p, true_y = [], [], [], []
+    for seed in range(6):
+        a, b, p = _halves(truth, sigma, na, nb, seed)
+        vp, blend, alpha = blend_prediction(a, b, p, _box(a), _box(b), na, nb)
+        assert 0.0 < alpha < 1.0
+        pred_p.append(vp)
+        pred_y.append(blend)
+        true_p.append(_relmse(p, truth))
+        true_y.append(_relmse(alpha * _box(p) + (1 - alpha) * p, truth))
+    assert np.mean(pred_p) == pytest.approx(np.mean(true_p), rel=0.15)
+    assert np.mean(true_y) < 0.8 * np.mean(true_p)          # the blend helps here
+    # normalising by the noisy plain mean makes the blend prediction err on
+    # the safe side (jobs stop late, not early), by well under 2x
+    assert 0.95 * np.mean(true_y) <= np.mean(pred_y) <= 1.6 * np.mean(true_y)
+
+
+def test_blend_prediction_limits():
+    from voidray_gb300.serve import blend_prediction
+
+    truth = np.full((32, 32, 3), 0.5)
+    a, b, p = _halves(truth, 0.5, 32, 32, 1)
+    # a perfect denoiser takes the whole weight, a uselessly biased one none
+    vp, blend, alpha = blend_prediction(a, b, p, truth, truth, 32, 32)
+    assert alpha == pytest.approx(1.0, abs=0.05) and blend < 0.1 * vp
+    vp, blend, alpha = blend_prediction(a, b, p, a + 0.5, b + 0.5, 32, 32)
+    assert alpha < 0.05 and blend == pytest.approx(vp, rel=0.1)

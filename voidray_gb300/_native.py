@@ -94,6 +94,11 @@ class vr_denoiser_layer(C.Structure):
                 ("relu", C.c_uint32), ("level", C.c_uint32), ("w_offset", C.c_uint64), ("b_offset", C.c_uint64)]
 
 
+class vr_tuning(C.Structure):
+    _fields_ = [("shade_block", C.c_uint32), ("shade_blocks_per_sm", C.c_uint32), ("raygen_block", C.c_uint32),
+                ("generation", C.c_uint32)]
+
+
 class vr_instrument(C.Structure):
     _fields_ = [("stage_ms", C.c_double * 8), ("stage_launches", C.c_uint64 * 8),
                 ("extend_node_visits", C.c_uint64), ("extend_tri_tests", C.c_uint64),
@@ -132,6 +137,10 @@ _SIGS = [
     ("vr_batch_destroy", C.c_int, [P]),
     ("vr_batch_render", C.c_int, [P, P, C.c_uint32, P]),
     ("vr_batch_synchronize", C.c_int, [P, P]),
+    ("vr_tuning_get", C.c_int, [P]),
+    ("vr_tuning_set", C.c_int, [P]),
+    ("vr_batch_set_graphs", C.c_int, [P, C.c_int32]),
+    ("vr_batch_graph_stats", C.c_int, [P, P, P]),
     ("vr_batch_stats_get", C.c_int, [P, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),

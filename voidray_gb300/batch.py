@@ -44,6 +44,16 @@ class Batch:
         arr = (N.vr_render_job * max(1, len(jobs)))(*[j.to_c() for j in jobs])
         check(lib().vr_batch_render(self._h, arr, len(jobs), C.c_void_p(stream or None)))
 
+    def set_graphs(self, enable: bool = True) -> None:
+        """Replay each wavefront's stage sequence as a cached CUDA graph."""
+        check(lib().vr_batch_set_graphs(self._h, int(enable)))
+
+    def graph_stats(self) -> tuple[int, int]:
+        """(captures, replays)"""
+        c, r = C.c_uint64(), C.c_uint64()
+        check(lib().vr_batch_graph_stats(self._h, C.byref(c), C.byref(r)))
+        return c.value, r.value
+
     def synchronize(self, stream: int = 0) -> None:
         check(lib().vr_batch_synchronize(self._h, C.c_void_p(stream or None)))
 

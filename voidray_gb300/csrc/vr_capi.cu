@@ -174,6 +174,53 @@ struct Instr {
     }
 };
 
+// Instantiated CUDA graphs of whole waves (wave begin, raygen, every depth's
+// extend / shade / shadow, accumulate), keyed by everything the launches bake
+// in.  The per-pass data (the Job entries: sample offsets, seeds, scenes) is
+// read from the device table, which is uploaded before each replay, so one
+// graph serves every pass of an unchanged job set.
+struct GraphKey {
+    const void* table;
+    const void* ps_tag;
+    const void* status;
+    const void* totals;
+    uint32_t njobs, total, max_bounces, any_nee, max_pixels, cap, tuning_generation, pad_;
+};
+
+struct GraphCache {
+    struct Entry {
+        GraphKey key;
+        cudaGraphExec_t exec;
+        uint64_t used;
+    };
+    std::vector<Entry> entries;
+    uint64_t tick = 0, captures = 0, replays = 0;
+    bool broken = false;  // capture failed once: launch directly from then on
+
+    void clear() {
+        for (Entry& e : entries) cudaGraphExecDestroy(e.exec);
+        entries.clear();
+    }
+    cudaGraphExec_t find(const GraphKey& k) {
+        for (Entry& e : entries)
+            if (std::memcmp(&e.key, &k, sizeof k) == 0) {
+                e.used = ++tick;
+                return e.exec;
+            }
+        return nullptr;
+    }
+    void insert(const GraphKey& k, cudaGraphExec_t x) {
+        if (entries.size() >= 16) {
+            size_t lru = 0;
+            for (size_t i = 1; i < entries.size(); ++i)
+                if (entries[i].used < entries[lru].used) lru = i;
+            cudaGraphExecDestroy(entries[lru].exec);
+            entries.erase(entries.begin() + lru);
+        }
+        entries.push_back({k, x, ++tick});
+    }
+};
+
 }  // namespace
 
 namespace vr {
@@ -203,6 +250,8 @@ struct vr_scene {
 struct vr_batch {
     int device = 0;
     uint64_t max_wave_paths = 0;
+    bool use_graphs = false;
+    GraphCache graphs;
     Engine eng;
     DevBuf psum;       // pixel sums of all jobs of a call
     uint32_t* status = nullptr;
@@ -275,9 +324,11 @@ struct HostJob {
 // Job entries of up to `table_cap` entries at a time, and launches the stage
 // sequence of every wave.  A job whose last paths ran in a wave is finalised
 // right after it.  `instr` (optional) brackets every launch with events.
+// With `graphs` (and a capturable stream) every wave runs as a replay of a
+// cached CUDA graph of its stage sequence.
 vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_t cap, vr::Job* table,
                     size_t table_cap, uint32_t* status, unsigned long long* totals, Instr* instr, cudaStream_t cs,
-                    uint64_t* waves_out) {
+                    uint64_t* waves_out, GraphCache* graphs = nullptr) {
     vr_status r;
     unsigned long long* wk = (instr && (instr->flags & VR_INSTR_WORK)) ? instr->work : nullptr;
     if (instr && (instr->flags & VR_INSTR_STAGE_TIMES) && instr->used > 0) {
@@ -338,23 +389,70 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
         if (plan.empty()) return fail(VR_ERR_INVALID, "wave table too small for one wave");
         // pageable host -> device: the host vector may be reused once the call returns
         VR_CK(cudaMemcpyAsync(table, chunk.data(), chunk.size() * sizeof(vr::Job), cudaMemcpyHostToDevice, cs));
+        const bool use_graphs = graphs && !graphs->broken && cs && !instr;
         for (const WaveHost& wh : plan) {
-            const vr::Wave wv{table + wh.first, (uint32_t)wh.njobs, wh.total, wh.max_bounces, wh.any_nee ? 1u : 0u,
-                              chunk[wh.first]};
-            VR_CK(vr::launch_raygen(wv, ps, cs));
-            if (instr && (r = instr->mark(VR_STAGE_RAYGEN, cs)) != VR_OK) return r;
-            for (uint32_t k = 0; k < wv.max_bounces; ++k) {
-                VR_CK(vr::launch_extend(wv, ps, k, status, wk, cs));
-                if (instr && (r = instr->mark(VR_STAGE_EXTEND, cs)) != VR_OK) return r;
-                VR_CK(vr::launch_shade(wv, ps, k, cs));
-                if (instr && (r = instr->mark(VR_STAGE_SHADE, cs)) != VR_OK) return r;
-                if (wv.any_nee) {
-                    VR_CK(vr::launch_shadow(wv, ps, k, status, wk ? wk + 2 : nullptr, cs));
-                    if (instr && (r = instr->mark(VR_STAGE_SHADOW, cs)) != VR_OK) return r;
+            const vr::Wave wv{table + wh.first, (uint32_t)wh.njobs, wh.total,         wh.max_bounces,
+                              wh.any_nee ? 1u : 0u, use_graphs ? 1u : 0u, chunk[wh.first]};
+            auto stages = [&]() -> vr_status {
+                VR_CK(vr::launch_raygen(wv, ps, cs));
+                if (instr && (r = instr->mark(VR_STAGE_RAYGEN, cs)) != VR_OK) return r;
+                for (uint32_t k = 0; k < wv.max_bounces; ++k) {
+                    VR_CK(vr::launch_extend(wv, ps, k, status, wk, cs));
+                    if (instr && (r = instr->mark(VR_STAGE_EXTEND, cs)) != VR_OK) return r;
+                    VR_CK(vr::launch_shade(wv, ps, k, cs));
+                    if (instr && (r = instr->mark(VR_STAGE_SHADE, cs)) != VR_OK) return r;
+                    if (wv.any_nee) {
+                        VR_CK(vr::launch_shadow(wv, ps, k, status, wk ? wk + 2 : nullptr, cs));
+                        if (instr && (r = instr->mark(VR_STAGE_SHADOW, cs)) != VR_OK) return r;
+                    }
                 }
+                VR_CK(vr::launch_accumulate(wv, ps, wh.max_pixels, totals, cs));
+                if (instr && (r = instr->mark(VR_STAGE_ACCUMULATE, cs)) != VR_OK) return r;
+                return VR_OK;
+            };
+            if (use_graphs) {
+                GraphKey key;
+                std::memset(&key, 0, sizeof key);
+                key.table = wv.jobs;
+                key.ps_tag = ps.q_org;
+                key.status = status;
+                key.totals = totals;
+                key.njobs = wv.njobs;
+                key.total = wv.total_paths;
+                key.max_bounces = wv.max_bounces;
+                key.any_nee = wv.any_nee;
+                key.max_pixels = wh.max_pixels;
+                key.cap = ps.cap;
+                key.tuning_generation = vr::get_tuning().generation;
+                cudaGraphExec_t ex = graphs->find(key);
+                if (!ex) {
+                    VR_CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+                    const vr_status sr = stages();
+                    cudaGraph_t g = nullptr;
+                    const cudaError_t ee = cudaStreamEndCapture(cs, &g);
+                    cudaError_t ie = cudaErrorUnknown;
+                    if (sr == VR_OK && ee == cudaSuccess && g) ie = cudaGraphInstantiate(&ex, g, 0);
+                    if (g) cudaGraphDestroy(g);
+                    if (ie != cudaSuccess) {
+                        // capture not possible here: run the stages directly from now on
+                        cudaGetLastError();
+                        graphs->broken = true;
+                        ex = nullptr;
+                    } else {
+                        graphs->insert(key, ex);
+                        graphs->captures++;
+                    }
+                } else {
+                    graphs->replays++;
+                }
+                if (ex) {
+                    VR_CK(cudaGraphLaunch(ex, cs));
+                } else if ((r = stages()) != VR_OK) {  // from_table stays set: same results
+                    return r;
+                }
+            } else if ((r = stages()) != VR_OK) {
+                return r;
             }
-            VR_CK(vr::launch_accumulate(wv, ps, wh.max_pixels, totals, cs));
-            if (instr && (r = instr->mark(VR_STAGE_ACCUMULATE, cs)) != VR_OK) return r;
             for (size_t i : wh.finishing) {
                 const HostJob& j = jobs[i];
                 VR_CK(vr::launch_finalize(j.tmpl.psum, j.rgba, j.tmpl.num_pixels, j.inv_total, cs));
@@ -678,6 +776,7 @@ vr_status vr_batch_create(uint64_t max_wave_paths, vr_batch** out) {
 vr_status vr_batch_destroy(vr_batch* b) {
     if (!b) return VR_OK;
     cudaDeviceSynchronize();
+    b->graphs.clear();
     b->eng.release();
     if (b->psum.p) cudaFree(b->psum.p);
     if (b->status) cudaFree(b->status);
@@ -712,7 +811,9 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
     if (total == 0) return VR_OK;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     const uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
+    const void* before = b->eng.ps.q_org;
     if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs, want_aov)) != VR_OK) return r;
+    if (b->eng.ps.q_org != before) b->graphs.clear();  // graphs bake in the old scratch pointers
     if (b->psum.bytes < pixels * sizeof(float4)) {
         VR_CK(cudaStreamSynchronize(cs));
         if ((r = ensure_buf(b->psum, pixels * sizeof(float4))) != VR_OK) return r;
@@ -736,9 +837,43 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
     }
     auto t0 = std::chrono::steady_clock::now();
     if ((r = run_waves(hj, b->eng.ps, (uint32_t)cap, b->eng.table, b->eng.table_cap, b->status, b->totals, nullptr, cs,
-                       &b->stats.wavefronts)) != VR_OK)
+                       &b->stats.wavefronts, b->use_graphs ? &b->graphs : nullptr)) != VR_OK)
         return r;
     b->stats.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return VR_OK;
+}
+
+vr_status vr_tuning_get(vr_tuning* out) {
+    if (!out) return fail(VR_ERR_INVALID, "null argument");
+    const vr::Tuning t = vr::get_tuning();
+    out->shade_block = t.shade_block;
+    out->shade_blocks_per_sm = t.shade_blocks_per_sm;
+    out->raygen_block = t.raygen_block;
+    out->generation = t.generation;
+    return VR_OK;
+}
+
+vr_status vr_tuning_set(const vr_tuning* in) {
+    if (!in) return fail(VR_ERR_INVALID, "null argument");
+    vr::Tuning t;
+    t.shade_block = in->shade_block;
+    t.shade_blocks_per_sm = in->shade_blocks_per_sm;
+    t.raygen_block = in->raygen_block;
+    if (!vr::set_tuning(t))
+        return fail(VR_ERR_INVALID, "blocks must be 64, 128 or 256 threads, 1-32 shade blocks per SM");
+    return VR_OK;
+}
+
+vr_status vr_batch_set_graphs(vr_batch* b, int32_t enable) {
+    if (!b) return fail(VR_ERR_INVALID, "null batch");
+    b->use_graphs = enable != 0;
+    return VR_OK;
+}
+
+vr_status vr_batch_graph_stats(vr_batch* b, uint64_t* captures, uint64_t* replays) {
+    if (!b || !captures || !replays) return fail(VR_ERR_INVALID, "null argument");
+    *captures = b->graphs.captures;
+    *replays = b->graphs.replays;
     return VR_OK;
 }
 

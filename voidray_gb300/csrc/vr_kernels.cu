@@ -886,6 +886,21 @@ static int num_sms() {
     }
     return g_num_sms;
 }
+static Tuning g_tuning;
+
+Tuning get_tuning() { return g_tuning; }
+
+bool set_tuning(const Tuning& t) {
+    auto ok_block = [](uint32_t b) { return b == 64 || b == 128 || b == 256; };
+    if (!ok_block(t.shade_block) || !ok_block(t.raygen_block) || t.shade_blocks_per_sm < 1 ||
+        t.shade_blocks_per_sm > 32)
+        return false;
+    const uint32_t gen = g_tuning.generation + 1;
+    g_tuning = t;
+    g_tuning.generation = gen;
+    return true;
+}
+
 static unsigned grid_for(uint64_t n, int block, int per_sm) {
     uint64_t want = (n + block - 1) / block;
     uint64_t cap = (uint64_t)num_sms() * per_sm;
@@ -931,8 +946,9 @@ cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint6
 
 cudaError_t launch_raygen(const Wave& w, const PathState& ps, cudaStream_t st) {
     k_wave_begin<<<grid_for((uint64_t)w.njobs * JOB_COUNTERS, 256, 1), 256, 0, st>>>(w, ps);
-    if (w.njobs == 1) k_raygen<true><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps);
-    else k_raygen<false><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps);
+    const int rb = (int)g_tuning.raygen_block;
+    if (w.njobs == 1 && !w.from_table) k_raygen<true><<<grid_for(w.total_paths, rb, 2048 / rb), rb, 0, st>>>(w, ps);
+    else k_raygen<false><<<grid_for(w.total_paths, rb, 2048 / rb), rb, 0, st>>>(w, ps);
     return cudaGetLastError();
 }
 
@@ -946,15 +962,16 @@ static void extend_impl(const Wave& w, const PathState& ps, uint32_t k, uint32_t
 
 cudaError_t launch_extend(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
                           cudaStream_t st) {
-    const bool one = w.njobs == 1;
+    const bool one = w.njobs == 1 && !w.from_table;
     if (work) one ? extend_impl<true, true>(w, ps, k, status, work, st) : extend_impl<true, false>(w, ps, k, status, work, st);
     else one ? extend_impl<false, true>(w, ps, k, status, nullptr, st) : extend_impl<false, false>(w, ps, k, status, nullptr, st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, cudaStream_t st) {
-    if (w.njobs == 1) k_shade<true><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps, k);
-    else k_shade<false><<<grid_for(w.total_paths, 256, 8), 256, 0, st>>>(w, ps, k);
+    const int sb = (int)g_tuning.shade_block, per_sm = (int)g_tuning.shade_blocks_per_sm;
+    if (w.njobs == 1 && !w.from_table) k_shade<true><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k);
+    else k_shade<false><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k);
     return cudaGetLastError();
 }
 
@@ -968,7 +985,7 @@ static void shadow_impl(const Wave& w, const PathState& ps, uint32_t k, uint32_t
 
 cudaError_t launch_shadow(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
                           cudaStream_t st) {
-    const bool one = w.njobs == 1;
+    const bool one = w.njobs == 1 && !w.from_table;
     if (work) one ? shadow_impl<true, true>(w, ps, k, status, work, st) : shadow_impl<true, false>(w, ps, k, status, work, st);
     else one ? shadow_impl<false, true>(w, ps, k, status, nullptr, st) : shadow_impl<false, false>(w, ps, k, status, nullptr, st);
     return cudaGetLastError();
@@ -977,7 +994,7 @@ cudaError_t launch_shadow(const Wave& w, const PathState& ps, uint32_t k, uint32
 cudaError_t launch_accumulate(const Wave& w, const PathState& ps, uint32_t max_pixels, unsigned long long* totals,
                               cudaStream_t st) {
     dim3 grid(grid_for(max_pixels, 256, 8), w.njobs);
-    if (w.njobs == 1) k_accumulate<true><<<grid, 256, 0, st>>>(w, ps);
+    if (w.njobs == 1 && !w.from_table) k_accumulate<true><<<grid, 256, 0, st>>>(w, ps);
     else k_accumulate<false><<<grid, 256, 0, st>>>(w, ps);
     if (totals) k_wave_stats<<<1, 32, 0, st>>>(w, ps, w.max_bounces, totals);
     return cudaGetLastError();

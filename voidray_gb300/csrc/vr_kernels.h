@@ -40,6 +40,7 @@ struct Wave {
     uint32_t total_paths;
     uint32_t max_bounces;   // over the jobs
     uint32_t any_nee;       // some job uses the NEE estimator
+    uint32_t from_table;    // read every job from `jobs` even when njobs == 1 (graph replays)
     Job first;              // copy of jobs[0]: single-job waves read it from kernel parameters
 };
 
@@ -64,6 +65,18 @@ struct PathState {
     uint32_t* cursors;  // 2 * MAX_DEPTH_SLOTS fetch cursors: [k] extend, [M + k] shadow
     float4* aov;        // 2*cap, when some job wants AOVs: first-hit albedo [0, cap), normal [cap, 2 cap)
 };
+
+// Launch shapes chosen at run time (the autotuner's knobs): block size and
+// resident blocks per SM of the shade / raygen stages.  `generation` changes
+// on every set so cached CUDA graphs can tell a new shape.
+struct Tuning {
+    uint32_t shade_block = 256;
+    uint32_t shade_blocks_per_sm = 8;
+    uint32_t raygen_block = 256;
+    uint32_t generation = 0;
+};
+Tuning get_tuning();
+bool set_tuning(const Tuning& t);  // false: out of range (unchanged)
 
 // Batch closest/any hit; `counter` is a device word the persistent kernel
 // uses as its ray-fetch cursor (reset by the launcher).

@@ -19,6 +19,22 @@ Here many progressive renders run at once:
   (a - b)^2 nA nB / (nA + nB)^2, and the estimate is its mean ratio to
   (m^2 + 1e-2) over pixels and channels (the relMSE definition).  A job
   finishes when the estimate reaches the target or its sample cap.
+* Denoised serving (requests with denoise=True, a backend with a denoiser):
+  the job also accumulates first-hit albedo / normal per half-buffer, and its
+  output may be a blend Y = alpha D(P) + (1 - alpha) P of the denoised full
+  mean D(P) and the plain mean P.  The error of Y is predicted from the
+  halves without a reference: the denoiser's error at n_A samples is
+  E|D(A) - B|^2 - Var(B) (B is independent of D(A)); its residual noise
+  scales as 1/n (from E|D(A) - D(B)|^2), its bias is taken as constant
+  between n_A and n (an over-estimate, the bias shrinks with n), and its
+  covariance with the plain noise comes from E[(D(A) - D(B))(A - B)].
+  Every term is normalised by (P^2 + 1e-2) like the plain estimate; since P
+  shares B's noise this over-states the denoiser's error somewhat (jobs stop
+  late rather than early), whereas normalising by the denoised image would
+  under-state it (the denoiser's bias would lower its own weights).
+  alpha minimises the predicted error; the job finishes when the smaller of
+  the plain and the blended prediction reaches the target, and returns that
+  output.  The plain progressive render stays the fallback (alpha = 0).
 * A job's result depends only on its own sample streams and pass schedule,
   so it is the same alone and in any mix.
 
@@ -47,6 +63,7 @@ class JobRequest:
     target_relmse: float = 1e-3
     seed: int = 0
     scene_bytes: int = 0       # device bytes of the scene (counted once while resident)
+    denoise: bool = False      # render AOVs and allow a denoised / blended output
 
 
 @dataclass
@@ -65,13 +82,17 @@ class JobState:
     bufs: Any = None
     result: Optional[np.ndarray] = None
     error: str = ""
+    alpha: float = 0.0         # weight of the denoised image in the output
+    plain_estimate: float = float("inf")
 
     @property
     def latency(self) -> Optional[float]:
         return None if self.finished is None else self.finished - self.arrival
 
     def footprint(self) -> int:
-        return 2 * self.req.width * self.req.height * 16
+        # two RGBA f32 half-buffers, plus albedo/normal per half and the
+        # denoiser's full-mean inputs and outputs when denoising
+        return (9 if self.req.denoise else 2) * self.req.width * self.req.height * 16
 
 
 @dataclass
@@ -131,22 +152,57 @@ def _estimate(a, b, na: int, nb: int, xp=np) -> float:
     return float(xp.mean(var / (m * m + EPS_REL)))
 
 
-class GpuBackend:
-    """Device accumulation buffers (torch) and one vr_batch for every pass."""
+def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
+    """Predicted relMSE of the plain mean P and of the best blend
+    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
+    the full mean p and the denoised half means da, db.  Returns
+    (plain, blend, alpha)."""
+    n = na + nb
+    den = p * p + EPS_REL
+    ab = a - b
+    s_ab = float(xp.mean(ab * ab / den))
+    v_p = s_ab * na * nb / (n * n)                      # Var(P)
+    var_a, var_b = s_ab * nb / n, s_ab * na / n          # Var(A), Var(B)
+    e_a = float(xp.mean((da - b) ** 2 / den)) - var_b   # error of D(A)
+    e_b = float(xp.mean((db - a) ** 2 / den)) - var_a   # error of D(B)
+    dd = da - db
+    tau2 = float(xp.mean(dd * dd / den)) * na * nb / n  # residual noise x samples
+    kap = float(xp.mean(dd * ab / den)) * na * nb / n   # covariance with the plain noise x samples
+    bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
+    v_eta, c = tau2 / n, kap / n
+    e_d = bias2 + v_eta
+    q = e_d + v_p - 2.0 * c
+    alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
+    blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
+    return v_p, max(blend, 0.0), alpha
 
-    def __init__(self, max_wave_paths: int = 0):
+
+class GpuBackend:
+    """Device accumulation buffers (torch) and one vr_batch for every pass;
+    with a denoiser, jobs that ask for it also get AOV buffers and blended
+    outputs (the module docstring describes the prediction)."""
+
+    def __init__(self, max_wave_paths: int = 0, denoiser=None, denoise_below: float = 16.0):
         import torch
 
         from .batch import Batch
 
         self.torch = torch
         self.batch = Batch(max_wave_paths)
+        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
         self.stream = torch.cuda.Stream()
+        self.dn = denoiser
+        # the denoiser prediction runs once the plain estimate is within this
+        # factor of the job's target (it cannot finish a job much earlier)
+        self.denoise_below = denoise_below
+        self.denoise_calls = 0
 
     def alloc(self, job: JobState):
         t = self.torch
         h, w = job.req.height, job.req.width
-        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda"), t.zeros((h, w, 4), dtype=t.float32, device="cuda")]
+        k = 6 if (job.req.denoise and self.dn is not None) else 2
+        # [A, B] radiance sums, then albedo A/B and normal A/B sums
+        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
 
     def free(self, job: JobState) -> None:
         job.bufs = None
@@ -160,20 +216,54 @@ class GpuBackend:
         for job, b, first, n in work:
             # buffers accumulate raw sums: total_samples = 1
             st = replace(job.req.settings, total_samples=1)
+            aov = len(job.bufs) == 6
             jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
-                                  job.req.seed, first))
+                                  job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
+                                  job.bufs[4 + b].data_ptr() if aov else 0))
         self.batch.render(jobs, self.stream.cuda_stream)
         self.batch.synchronize(self.stream.cuda_stream)
 
+    def _denoise(self, rad, alb, nrm, scale: float):
+        t = self.torch
+        h, w = rad.shape[0], rad.shape[1]
+        out = t.empty((h, w, 4), dtype=t.float32, device="cuda")
+        self.dn.denoise(rad, alb, nrm, scale, out, w, h, stream=self.stream.cuda_stream)
+        self.denoise_calls += 1
+        return out
+
     def estimate(self, job: JobState) -> float:
         t = self.torch
-        a = job.bufs[0][..., :3].double() / max(job.n_a, 1)
-        b = job.bufs[1][..., :3].double() / max(job.n_b, 1)
-        return _estimate(a, b, job.n_a, job.n_b, xp=t)
+        na, nb = job.n_a, job.n_b
+        a = job.bufs[0][..., :3].double() / max(na, 1)
+        b = job.bufs[1][..., :3].double() / max(nb, 1)
+        plain = _estimate(a, b, na, nb, xp=t)
+        job.plain_estimate, job.alpha = plain, 0.0
+        if len(job.bufs) != 6 or plain > self.denoise_below * job.req.target_relmse:
+            return plain
+        with t.cuda.stream(self.stream):
+            da = self._denoise(job.bufs[0], job.bufs[2], job.bufs[4], 1.0 / na)[..., :3].double()
+            db = self._denoise(job.bufs[1], job.bufs[3], job.bufs[5], 1.0 / nb)[..., :3].double()
+        self.stream.synchronize()
+        p = (a * na + b * nb) / (na + nb)
+        _, blend, alpha = blend_prediction(a, b, p, da, db, na, nb, xp=t)
+        if blend < plain:
+            job.alpha = alpha
+            return blend
+        return plain
 
     def result(self, job: JobState) -> np.ndarray:
-        a, b = job.bufs
-        return ((a[..., :3] + b[..., :3]) / (job.n_a + job.n_b)).cpu().numpy()
+        t = self.torch
+        n = job.n_a + job.n_b
+        p = (job.bufs[0] + job.bufs[1]) / n
+        if job.alpha <= 0.0:
+            return p[..., :3].cpu().numpy()
+        with t.cuda.stream(self.stream):
+            alb = (job.bufs[2] + job.bufs[3]) / n
+            nrm = (job.bufs[4] + job.bufs[5]) / n
+            d = self._denoise(p, alb, nrm, 1.0)
+            y = job.alpha * d[..., :3] + (1.0 - job.alpha) * p[..., :3]
+        self.stream.synchronize()
+        return y.cpu().numpy()
 
 
 class Server:
