@@ -391,6 +391,18 @@ __global__ void k_avgpool2(const bf16* __restrict__ in, bf16* __restrict__ out, 
     }
 }
 
+__global__ void k_upsample2(const uint4* __restrict__ in, uint4* __restrict__ out, int n, int h, int w, int c8) {
+    const size_t total = (size_t)n * h * w * c8;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c8);
+        const size_t p = i / c8;
+        const int x = (int)(p % w);
+        const int y = (int)((p / w) % h);
+        const int nn = (int)(p / ((size_t)w * h));
+        out[i] = in[(((size_t)nn * (h >> 1) + (y >> 1)) * (w >> 1) + (x >> 1)) * c8 + ch];
+    }
+}
+
 __global__ void k_skip_bwd(const bf16* __restrict__ dcat, int ccat, int coff, const bf16* __restrict__ dpool,
                            const bf16* __restrict__ act, bf16* __restrict__ dz, int n, int h, int w, int c) {
     const int c8 = c >> 3, hc = h >> 1, wc = w >> 1;
@@ -651,6 +663,14 @@ cudaError_t avgpool2(const bf16* in, bf16* out, int n, int h, int w, int c, cuda
     if ((h | w) & 1 || c % 8) return cudaErrorInvalidValue;
     const size_t total = (size_t)n * (h / 2) * (w / 2) * (c / 8);
     k_avgpool2<<<grid_for(total, 256), 256, 0, st>>>(in, out, n, h, w, c);
+    return cudaGetLastError();
+}
+
+cudaError_t upsample2(const bf16* in, bf16* out, int n, int h, int w, int c, cudaStream_t st) {
+    if ((h | w) & 1 || c % 8) return cudaErrorInvalidValue;
+    const size_t total = (size_t)n * h * w * (c / 8);
+    k_upsample2<<<grid_for(total, 256), 256, 0, st>>>(reinterpret_cast<const uint4*>(in), reinterpret_cast<uint4*>(out),
+                                                      n, h, w, c / 8);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,14 @@ struct WgradArgs {
 };
 
 cudaError_t conv3x3(const ConvArgs& a, cudaStream_t st);
+// The same convolution on the 5th-generation tensor cores (tcgen05.mma,
+// TMEM accumulator, TMA operand staging; dn_tc.cu).  Forward only: no mask,
+// no upsampled source (materialise it with upsample2 first), Cout 16..256.
+// `status` (optional device word) receives bit 1 / 2 when a bounded wait ran out.
+bool conv3x3_tc_supported(const ConvArgs& a);
+cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st);
+// out[n][y][x][c] = in[n][y/2][x/2][c] (nearest 2x upsample, (h, w) = output size)
+cudaError_t upsample2(const bf16* in, bf16* out, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t conv3x3_wgrad(const WgradArgs& a, cudaStream_t st);
 // db[c] += sum_p dz[p][c]
 cudaError_t bias_grad(const bf16* dz, int p, int c, float* db, cudaStream_t st);

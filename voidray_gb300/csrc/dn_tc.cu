@@ -1,0 +1,356 @@
+// dn_tc.cu — Blackwell-native 3x3 convolution of the denoiser: tcgen05.mma
+// with the accumulator in tensor memory (TMEM), operands staged in shared
+// memory by TMA (cp.async.bulk.tensor, no multicast), an mbarrier pipeline
+// between one producer thread, one MMA-issuing thread and a 4-warp epilogue.
+//
+// Implicit GEMM per CTA: M = 128 output pixels (an 8 x 16 block of one
+// image), N = Cout (16..256, one tile), K = 9 taps x Cin in chunks of BK
+// channels.  For tap (dy, dx) and channel chunk c0 the A tile is one 4-D TMA
+// box (BK channels x 16 columns x 8 rows x 1 image) of the NHWC activation at
+// (c0, x0 + dx, y0 + dy, n); out-of-image coordinates read zeros, which is
+// the convolution's zero padding.  The B tile is the (N x BK) slice of the
+// [Cout][9 * Cin] weight matrix.  Both land K-major and swizzled (BK = 64:
+// 128-byte, 32: 64-byte, 16: 32-byte rows), the layout tcgen05 reads through
+// its shared-memory descriptors.  The epilogue reads the fp32 accumulator
+// with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e. pixels), adds
+// the bias, applies ReLU and stores bf16 (or fp32) NHWC rows.
+//
+// Every mbarrier wait is bounded: a wait that runs out sets an error bit in
+// the caller's status word and the CTA still drains and frees its TMEM.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "dn_kernels.h"
+
+namespace dn {
+namespace {
+
+constexpr int TC_THREADS = 128;
+constexpr int TC_STAGES = 4;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;  // iterations of a bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// true when the phase with this parity has completed; gives up after WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major, swizzled operand whose rows
+// are `row_bytes` (= the swizzle span) long: start address, leading byte
+// offset 16 (unused for swizzled K-major), stride byte offset = 8 rows,
+// descriptor version 1, swizzle mode.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t row_bytes) {
+    const uint64_t swz = row_bytes == 128 ? 2ull : row_bytes == 64 ? 4ull : 6ull;
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)((8u * row_bytes) >> 4) << 32;
+    d |= 1ull << 46;
+    d |= swz << 61;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: fp32 accumulator, bf16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t m, uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+struct TcArgs {
+    const float* bias;
+    bf16* out;
+    float* out_f32;
+    uint32_t* status;
+    int n, h, w;
+    int c1, cin, cout;
+    int bk;           // channels per K chunk (16, 32, 64)
+    int relu;
+    int tiles_x, tiles_y;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_conv3x3_tc(const __grid_constant__ CUtensorMap map_a1, const __grid_constant__ CUtensorMap map_a2,
+                 const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t dsmem[];
+    __shared__ uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], done_bar;
+    __shared__ uint32_t tmem_base;
+    // 1024-byte aligned stage buffers (the 128-byte swizzle atom is 8 x 128 B)
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = a.cout;
+    const uint32_t a_bytes = 128u * a.bk * 2u, b_bytes = (uint32_t)N * a.bk * 2u;
+    const uint32_t stage_bytes = a_bytes + b_bytes;
+    const uint32_t tmem_cols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
+
+    int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x;
+    tile /= a.tiles_x;
+    const int ty = tile % a.tiles_y;
+    const int img = tile / a.tiles_y;
+    const int x0 = tx * 16, y0 = ty * 8;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&done_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&tmem_base)),
+                     "r"(tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
+
+    const int kc = a.cin / a.bk;
+    const int nk = 9 * kc;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // producer: TMA loads of the A (activation box) and B (weight slice) tiles
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % TC_STAGES;
+            if (kt >= TC_STAGES && !mbar_wait(&empty_bar[s], ((kt / TC_STAGES) & 1) ^ 1)) {
+                ok = false;
+                break;
+            }
+            const int tap = kt / kc, c0 = (kt % kc) * a.bk;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            uint8_t* sa = smem + (size_t)s * stage_bytes;
+            uint8_t* sb = sa + a_bytes;
+            mbar_expect_tx(&full_bar[s], stage_bytes);
+            if (c0 < a.c1) tma_load_4d(sa, &map_a1, &full_bar[s], c0, x0 + dx, y0 + dy, img);
+            else tma_load_4d(sa, &map_a2, &full_bar[s], c0 - a.c1, x0 + dx, y0 + dy, img);
+            tma_load_2d(sb, &map_b, &full_bar[s], tap * a.cin + c0, 0);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer: BK/16 tcgen05.mma per stage, accumulating in TMEM
+        const uint32_t idesc = instr_desc(128, (uint32_t)N);
+        const uint32_t row_bytes = (uint32_t)a.bk * 2u;
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % TC_STAGES;
+            if (!mbar_wait(&full_bar[s], (kt / TC_STAGES) & 1)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = smem_addr(smem + (size_t)s * stage_bytes);
+            const uint32_t sb = sa + a_bytes;
+            for (int kk = 0; kk < a.bk / 16; ++kk) {
+                const uint64_t da = smem_desc(sa + kk * 32, row_bytes);
+                const uint64_t db = smem_desc(sb + kk * 32, row_bytes);
+                const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            }
+            // frees the stage once these MMAs have read it
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_addr(&empty_bar[s]))
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         smem_addr(&done_bar))
+                     : "memory");
+    }
+    if (!ok && a.status) atomicOr(a.status, 1u);
+    __syncwarp();
+
+    // epilogue: all four warps wait for the accumulator
+    const bool acc_ready = mbar_wait(&done_bar, 0);
+    if (!acc_ready && lane == 0 && a.status) atomicOr(a.status, 2u);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int m = warp * 32 + lane;  // TMEM lane = pixel of the 8 x 16 block
+    const int y = y0 + (m >> 4), x = x0 + (m & 15);
+    const bool in_img = y < a.h && x < a.w;
+    const size_t pix = ((size_t)img * a.h + y) * a.w + x;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (!in_img || !acc_ready) continue;
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            v[j] = __uint_as_float(r[j]) + (a.bias ? a.bias[c0 + j] : 0.0f);
+            if (a.relu) v[j] = fmaxf(v[j], 0.0f);
+        }
+        if (a.out_f32) {
+            float4* o = reinterpret_cast<float4*>(a.out_f32 + pix * N + c0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        } else {
+            union {
+                uint4 u[2];
+                bf16 h[16];
+            } pk;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) pk.h[j] = __float2bfloat16_rn(v[j]);
+            uint4* o = reinterpret_cast<uint4*>(a.out + pix * N + c0);
+            o[0] = pk.u[0];
+            o[1] = pk.u[1];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tmem_cols));
+    }
+}
+
+// ------------------------------------------------------------- host side --
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+CUtensorMapSwizzle swizzle_for(int bk) {
+    return bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : bk == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+}
+
+// NHWC activation (c channels) as a 4-D map with boxes of bk x 16 x 8 x 1
+bool encode_act(CUtensorMap* m, const bf16* p, int n, int h, int w, int c, int bk) {
+    const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)c * w * 2, (cuuint64_t)c * w * h * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)bk, 16, 8, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(p), dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(bk), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// weights [cout][9 * cin] as a 2-D map with boxes of bk x cout
+bool encode_wgt(CUtensorMap* m, const bf16* p, int cout, int cin, int bk) {
+    const cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};
+    const cuuint64_t strides[1] = {(cuuint64_t)9 * cin * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)cout};
+    const cuuint32_t es[2] = {1, 1};
+    return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(p), dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(bk), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+bool conv3x3_tc_supported(const ConvArgs& a) {
+    const int cin = a.c1 + a.c2;
+    if (a.up1 || a.mask || !encode_fn()) return false;
+    if (a.cout < 16 || a.cout > 256 || a.cout % 16) return false;
+    if (cin % 16 || a.c1 % 16 || a.c2 % 16) return false;
+    if (!aligned16(a.src1) || (a.c2 && !aligned16(a.src2)) || !aligned16(a.weight)) return false;
+    return true;
+}
+
+cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
+    if (!conv3x3_tc_supported(a)) return cudaErrorInvalidValue;
+    const int cin = a.c1 + a.c2;
+    // largest chunk that divides both sources (a chunk never straddles them)
+    int bk = 64;
+    while (bk > 16 && ((a.c1 % bk) || (a.c2 % bk))) bk >>= 1;
+    CUtensorMap ma1, ma2, mb;
+    std::memset(&ma2, 0, sizeof ma2);
+    if (!encode_act(&ma1, a.src1, a.n, a.h, a.w, a.c1, bk)) return cudaErrorInvalidValue;
+    if (a.c2 && !encode_act(&ma2, a.src2, a.n, a.h, a.w, a.c2, bk)) return cudaErrorInvalidValue;
+    if (!a.c2) ma2 = ma1;
+    if (!encode_wgt(&mb, a.weight, a.cout, cin, bk)) return cudaErrorInvalidValue;
+    TcArgs t{};
+    t.bias = a.bias;
+    t.out = a.out;
+    t.out_f32 = a.out_f32;
+    t.status = status;
+    t.n = a.n;
+    t.h = a.h;
+    t.w = a.w;
+    t.c1 = a.c1;
+    t.cin = cin;
+    t.cout = a.cout;
+    t.bk = bk;
+    t.relu = a.relu;
+    t.tiles_x = (a.w + 15) / 16;
+    t.tiles_y = (a.h + 7) / 8;
+    const size_t stage = (size_t)128 * bk * 2 + (size_t)a.cout * bk * 2;
+    const size_t smem = TC_STAGES * stage + 1024;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const unsigned grid = (unsigned)(t.tiles_x * t.tiles_y * a.n);
+    k_conv3x3_tc<<<grid, TC_THREADS, smem, st>>>(ma1, ma2, mb, t);
+    return cudaGetLastError();
+}
+
+}  // namespace dn

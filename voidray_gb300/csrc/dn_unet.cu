@@ -116,6 +116,9 @@ struct vr_denoiser {
     bf16* dcat[NL] = {};  // input gradients of the concatenating layers (8, 10, 12)
     bool train_ws = false;
     int loss_kind = dn::LOSS_L1_LOG;
+    int backend = VR_DN_BACKEND_MMA_SYNC;  // forward convolutions
+    bf16* up_tmp = nullptr;                // materialised 2x upsample (tcgen05 forward)
+    uint32_t* status = nullptr;            // device: bounded-wait timeouts of the tcgen05 kernel
 };
 
 namespace {
@@ -130,6 +133,7 @@ void free_ws(vr_denoiser* d) {
     d->gout = nullptr;
     d->dz[0] = d->dz[1] = nullptr;
     d->dpool = nullptr;
+    d->up_tmp = nullptr;
     d->wn = d->wh = d->ww = 0;
     d->train_ws = false;
 }
@@ -154,6 +158,12 @@ vr_status ensure_ws(vr_denoiser* d, int n, int h, int w, bool train) {
     for (int a = 0; a < NACT; ++a)
         if ((r = ws_alloc(d, &d->act[a], (P >> (2 * ACTS[a].lvl)) * ACTS[a].c)) != VR_OK) return free_ws(d), r;
     if ((r = ws_alloc(d, &d->out, P * OUT_C)) != VR_OK) return free_ws(d), r;
+    {
+        size_t upmax = 0;  // full-resolution copy of the upsampled input of layers 8, 10, 12
+        for (int l = 0; l < NL; ++l)
+            if (LAYERS[l].up1) upmax = std::max(upmax, (P >> (2 * level_of(LAYERS[l]))) * ACTS[LAYERS[l].in1].c);
+        if ((r = ws_alloc(d, &d->up_tmp, upmax)) != VR_OK) return free_ws(d), r;
+    }
     if (train) {
         size_t dzmax = 0, dpmax = 0;
         for (int l = 0; l < NL; ++l) {
@@ -203,7 +213,20 @@ vr_status forward(vr_denoiser* d, cudaStream_t st) {
         a.cout = L.cout;
         a.up1 = L.up1;
         a.relu = L.relu;
-        DN_CK(dn::conv3x3(a, st));
+        if (d->backend == VR_DN_BACKEND_TCGEN05) {
+            if (a.up1) {  // the TMA boxes read plain NHWC tiles: materialise the upsample
+                DN_CK(dn::upsample2(a.src1, d->up_tmp, n, a.h, a.w, a.c1, st));
+                a.src1 = d->up_tmp;
+                a.up1 = 0;
+            }
+            if (dn::conv3x3_tc_supported(a)) {
+                DN_CK(dn::conv3x3_tc(a, d->status, st));
+            } else {
+                DN_CK(dn::conv3x3(a, st));
+            }
+        } else {
+            DN_CK(dn::conv3x3(a, st));
+        }
         if (l == 1 || l == 3 || l == 5) {
             const int s = L.out, p = s + 1;  // S0 -> P0, S1 -> P1, S2 -> P2
             DN_CK(dn::avgpool2(d->act[s], d->act[p], n, h >> lv, w >> lv, ACTS[s].c, st));
@@ -349,7 +372,10 @@ vr_status vr_denoiser_create(uint64_t seed, vr_denoiser** out) {
     DN_ALLOC(d->w16, np);
     DN_ALLOC(d->wt16, np);
     DN_ALLOC(d->loss, 1);
+    DN_ALLOC(d->status, 1);
 #undef DN_ALLOC
+    if (cudaMemset(d->status, 0, sizeof(uint32_t)) != cudaSuccess)
+        return fail_free(vr::set_error(VR_ERR_CUDA, "status init"));
     // He-normal init; the zero-padded input channels of layer 0 and output
     // channels >= 3 of the last layer stay zero
     std::vector<float> host(np, 0.0f);
@@ -376,7 +402,7 @@ vr_status vr_denoiser_destroy(vr_denoiser* d) {
     cudaDeviceSynchronize();
     free_ws(d);
     for (void* p : {(void*)d->w32, (void*)d->g32, (void*)d->m, (void*)d->v, (void*)d->w16, (void*)d->wt16,
-                    (void*)d->loss})
+                    (void*)d->loss, (void*)d->status})
         if (p) cudaFree(p);
     delete d;
     return VR_OK;
@@ -400,6 +426,23 @@ vr_status vr_denoiser_set_loss(vr_denoiser* d, int32_t kind) {
     if (!d) return vr::set_error(VR_ERR_INVALID, "null denoiser");
     if (kind != VR_DN_LOSS_L1_LOG && kind != VR_DN_LOSS_RELMSE) return vr::set_error(VR_ERR_INVALID, "bad loss kind");
     d->loss_kind = kind == VR_DN_LOSS_RELMSE ? dn::LOSS_RELMSE : dn::LOSS_L1_LOG;
+    return VR_OK;
+}
+
+vr_status vr_denoiser_set_backend(vr_denoiser* d, int32_t backend) {
+    if (!d) return vr::set_error(VR_ERR_INVALID, "null denoiser");
+    if (backend != VR_DN_BACKEND_MMA_SYNC && backend != VR_DN_BACKEND_TCGEN05)
+        return vr::set_error(VR_ERR_INVALID, "bad backend");
+    d->backend = backend;
+    return VR_OK;
+}
+
+vr_status vr_denoiser_status(vr_denoiser* d, uint32_t* flags) {
+    if (!d || !flags) return vr::set_error(VR_ERR_INVALID, "null argument");
+    DN_CK(cudaDeviceSynchronize());
+    DN_CK(cudaMemcpy(flags, d->status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    DN_CK(cudaMemset(d->status, 0, sizeof(uint32_t)));
+    if (*flags) return vr::set_error(VR_ERR_TIMEOUT, "a tcgen05 convolution gave up a bounded wait");
     return VR_OK;
 }
 
@@ -511,6 +554,32 @@ vr_status vr_dn_conv3x3_device(const uint16_t* src1, uint32_t c1, int32_t up1, c
     if (e == cudaErrorInvalidValue)
         return vr::set_error(VR_ERR_INVALID, "channel counts must be multiples of 16, h and w even when up1");
     DN_CK(e);
+    return VR_OK;
+}
+
+vr_status vr_dn_conv3x3_tc_device(const uint16_t* src1, uint32_t c1, const uint16_t* src2, uint32_t c2,
+                                  const uint16_t* weight, const float* bias, uint16_t* out_bf16, float* out_f32,
+                                  uint32_t cout, uint32_t n, uint32_t h, uint32_t w, int32_t relu,
+                                  uint32_t* status_device, void* stream) {
+    if (!src1 || !weight || (!out_bf16 == !out_f32) || (c2 && !src2))
+        return vr::set_error(VR_ERR_INVALID, "src1, weight and exactly one output are required");
+    dn::ConvArgs a{};
+    a.src1 = reinterpret_cast<const bf16*>(src1);
+    a.src2 = reinterpret_cast<const bf16*>(src2);
+    a.weight = reinterpret_cast<const bf16*>(weight);
+    a.bias = bias;
+    a.out = reinterpret_cast<bf16*>(out_bf16);
+    a.out_f32 = out_f32;
+    a.n = (int)n;
+    a.h = (int)h;
+    a.w = (int)w;
+    a.c1 = (int)c1;
+    a.c2 = (int)c2;
+    a.cout = (int)cout;
+    a.relu = relu ? 1 : 0;
+    if (!dn::conv3x3_tc_supported(a))
+        return vr::set_error(VR_ERR_UNSUPPORTED, "tcgen05 convolution: Cout 16..256 and channels multiples of 16");
+    DN_CK(dn::conv3x3_tc(a, status_device, static_cast<cudaStream_t>(stream)));
     return VR_OK;
 }
 

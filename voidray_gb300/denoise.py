@@ -82,6 +82,19 @@ class Denoiser:
     LOSS_L1_LOG = 0
     LOSS_RELMSE = 1
 
+    MMA_SYNC = 0
+    TCGEN05 = 1
+
+    def set_backend(self, backend: int) -> None:
+        """Forward convolutions on mma.sync (0) or tcgen05 + TMEM + TMA (1)."""
+        check(lib().vr_denoiser_set_backend(self.handle, int(backend)))
+
+    def status(self) -> int:
+        """Synchronises; raises VoidrayError if a tcgen05 kernel gave up a bounded wait."""
+        f = C.c_uint32()
+        check(lib().vr_denoiser_status(self.handle, C.byref(f)))
+        return f.value
+
     def set_loss(self, kind: int) -> None:
         check(lib().vr_denoiser_set_loss(self.handle, int(kind)))
 
@@ -141,6 +154,14 @@ def conv3x3(src1, c1: int, weight, cout: int, n: int, h: int, w: int, *, src2=No
     check(lib().vr_dn_conv3x3_device(_p(src1), int(c1), int(up1), _p(src2), int(c2), _p(weight), _p(bias), _p(mask),
                                      _p(out_bf16), _p(out_f32), int(cout), int(n), int(h), int(w), int(relu),
                                      C.c_void_p(stream or None)))
+
+
+def conv3x3_tc(src1, c1: int, weight, cout: int, n: int, h: int, w: int, *, src2=None, c2: int = 0, bias=None,
+               out_bf16=None, out_f32=None, relu: bool = False, status=None, stream: int = 0) -> None:
+    """Single forward convolution on tcgen05 (device pointers)."""
+    check(lib().vr_dn_conv3x3_tc_device(_p(src1), int(c1), _p(src2), int(c2), _p(weight), _p(bias), _p(out_bf16),
+                                        _p(out_f32), int(cout), int(n), int(h), int(w), int(relu), _p(status),
+                                        C.c_void_p(stream or None)))
 
 
 def conv3x3_wgrad(dz, src1, c1: int, dw, cout: int, n: int, h: int, w: int, *, src2=None, c2: int = 0,
