@@ -213,21 +213,26 @@ def serving_benchmark(args):
                              "prediction of the blend's error from the halves",
            "reference": "4096 spp per scene", "denoiser": "U-Net 32/64/128/256, bf16, shipped weights"}
     spp_pass = 32
-    # served: as many active jobs as fill a ~16M-path wavefront per pass, so
-    # that jobs complete in admission order instead of all at the end
-    fill = max(1, (1 << 24) // (size * size * spp_pass))
-    out["served_max_active"] = fill
-    modes = (("plain", 1, False), ("served", fill, False), ("served_denoised", fill, True))
-    for name, active, dn in modes:
-        backend = GpuBackend(denoiser=net if dn else None)
+    # plain: the progressive single-scene loop, one job at a time, 32 spp per
+    # pass, stopping on the same half-buffer estimate.  served: continuous
+    # batching with predictive per-job pass sizes (16M-path passes, jobs take
+    # them in admission order).  served_denoised: the same plus AOVs and the
+    # denoiser blend.
+    plain_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=1, spp_per_pass=spp_pass, min_samples=64)
+    served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pass_paths=1 << 24,
+                              first_pass_spp=64, min_samples=64)
+    out["served_config"] = {"adaptive": True, "pass_paths": 1 << 24, "first_pass_spp": 64, "max_active": 64}
+    modes = (("plain", plain_cfg, False), ("served", served_cfg, False), ("served_denoised", served_cfg, True))
+    for name, cfg, dn in modes:
+        active = cfg.max_active
+        backend = GpuBackend(denoiser=net if dn else None, denoise_below=1e9)
         requests = []
         for i, t in enumerate(arrivals):
             acc, st, nbytes, _ = pool[picks[i]]
             requests.append((float(t), JobRequest(acc, st, size, size, max_samples=2048,
                                                   target_relmse=args.serve_target, seed=1000 + i,
                                                   scene_bytes=nbytes, denoise=dn)))
-        srv = Server(backend, ServerConfig(memory_budget=150 * 10**9, max_active=active, spp_per_pass=spp_pass,
-                                           min_samples=64))
+        srv = Server(backend, cfg)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         srv.run(requests)
@@ -290,9 +295,10 @@ def denoiser_equal_time(pool, refs, net, size):
         net.denoise(bufs[0], bufs[1], bufs[2], 1.0, bufs[3], size, size, stream=h)
         render_device(acc, st, 1, bufs[0].data_ptr(), size, size, seed=6, stream=h)
         for spp in (4, 16, 64, 256):
-            for b in bufs:
-                b.zero_()
-            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):  # ordered after everything rendered on this stream
+                for b in bufs:
+                    b.zero_()
+            stream.synchronize()
             t_r = timed(lambda: render_device(acc, st, spp, bufs[0].data_ptr(), size, size, seed=7, stream=h,
                                               albedo_device=bufs[1].data_ptr(), normal_device=bufs[2].data_ptr()))
             t_d = timed(lambda: net.denoise(bufs[0], bufs[1], bufs[2], 1.0 / spp, bufs[3], size, size, stream=h))
@@ -300,8 +306,10 @@ def denoiser_equal_time(pool, refs, net, size):
             # plain frame in the same time: samples scale with the time budget
             t_plain_1 = timed(lambda: render_device(acc, st, spp, bufs[0].data_ptr(), size, size, seed=8, stream=h))
             spp_eq = max(spp, int(spp * (t_r + t_d) / max(t_plain_1, 1e-3)))
-            bufs[0].zero_()
+            with torch.cuda.stream(stream):
+                bufs[0].zero_()
             t_eq = timed(lambda: render_device(acc, st, spp_eq, bufs[0].data_ptr(), size, size, seed=8, stream=h))
+            stream.synchronize()
             plain = (bufs[0][..., :3].double() / spp_eq).cpu().numpy()
             r = refs[id(acc)]
             e_d = float(np.mean((den - r) ** 2 / (r * r + 1e-2)))
@@ -508,6 +516,15 @@ def main():
     serve = None
     if rank == 0 and world == 1 and not args.no_serve:
         serve = serving_benchmark(args)
+    dnb = None
+    if rank == 0 and world == 1 and not args.no_serve:
+        # the denoiser's kernels on a 1920x1080 frame (tensor-bound; see its roofline)
+        from voidray_gb300 import denoise_bench
+
+        dnb = denoise_bench.run(1920, 1080, iters=10)
+        dnb["roofline"] = {"bound": "tensor", "kernel": "U-Net forward (15 3x3 convolutions), tcgen05",
+                           "achieved": dnb["tcgen05"]["tflops"], "peak": dnb["peak_tflops"], "unit": "TFLOP/s",
+                           "frac": dnb["tcgen05"]["frac"], "peak_source": dnb["peak_source"]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, st, args, args.cpu_seconds)
@@ -526,7 +543,7 @@ def main():
             "mrays_per_s": (ext_rays + shd_rays) / (ms / 1e3) / 1e6,
             "rays": {"extend": int(ext_rays), "shadow": int(shd_rays)},
             "stages": stage, "gpu_launches": gpu_launches, "clocks": clk, "e2e": e2e, "roofline": roofline,
-            "cpu_baseline": cpu, "image_finite": finite, "serving": serve,
+            "cpu_baseline": cpu, "image_finite": finite, "serving": serve, "denoiser": dnb,
         }
         print(json.dumps(line), flush=True)
     acc.destroy()

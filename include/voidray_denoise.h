@@ -81,6 +81,14 @@ vr_status vr_denoiser_set_params(vr_denoiser* net, const float* host, uint64_t c
 vr_status vr_denoise_device(vr_denoiser* net, const float* rgba, const float* albedo, const float* normal,
                             float scale, float* out_rgba, uint32_t width, uint32_t height, void* stream);
 
+/* Denoises `batch` images of width x height at once ([batch][height][width][4]
+ * f32 device buffers); image i is scaled by scales[i] (host array of batch
+ * floats).  Same result per image as vr_denoise_device; one launch sequence
+ * for the whole batch. */
+vr_status vr_denoise_batch_device(vr_denoiser* net, const float* rgba, const float* albedo, const float* normal,
+                                  const float* scales, float* out_rgba, uint32_t batch, uint32_t width,
+                                  uint32_t height, void* stream);
+
 /* Loss and gradients of a batch of `batch` crops (width, height multiples of
  * 8): inputs as vr_denoise_device (scaled by scale_in), target radiance
  * scaled by scale_target, all [batch][height][width][4] f32 on the device.

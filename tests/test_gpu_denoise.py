@@ -229,3 +229,22 @@ def test_bad_arguments_are_errors(gpu):
             net.train_step(y, y, y, y, 1, 12, 12, lr=1e-3)
     finally:
         net.destroy()
+
+
+def test_denoise_batch_equals_single_images(gpu):
+    net = D.Denoiser(seed=4)
+    try:
+        h, w, n = 24, 40, 3
+        rad, alb, nrm, _ = batch_arrays(n, h, w, 21)
+        t = [torch.from_numpy(a).cuda() for a in (rad, alb, nrm)]
+        scales = [1.0, 0.5, 0.25]
+        out = torch.zeros((n, h, w, 4), dtype=torch.float32, device="cuda")
+        net.denoise_batch(*t, scales, out, w, h)
+        torch.cuda.synchronize()
+        for i in range(n):
+            one = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+            net.denoise(t[0][i], t[1][i], t[2][i], scales[i], one, w, h)
+            torch.cuda.synchronize()
+            assert torch.equal(one, out[i])
+    finally:
+        net.destroy()

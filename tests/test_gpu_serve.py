@@ -49,7 +49,8 @@ def test_served_same_alone_and_in_mix(gpu):
     assert r0[1] < 256  # stopped on the error estimate
 
 
-def test_denoised_serving_same_alone_and_in_mix(gpu):
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive):
     """With the denoiser in the loop (AOV buffers, blended output) a job's
     stopping point, blend weight and image still depend only on the job."""
     import voidray_gb300 as vr
@@ -58,7 +59,8 @@ def test_denoised_serving_same_alone_and_in_mix(gpu):
     from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig
 
     scenes = _scenes(vr, W)
-    cfg = ServerConfig(spp_per_pass=8, min_samples=16)
+    cfg = ServerConfig(spp_per_pass=8, min_samples=16, adaptive=adaptive, pass_paths=40 * 32 * 16,
+                       first_pass_spp=16)
     net = Denoiser.pretrained()
 
     def run(mix):

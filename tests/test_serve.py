@@ -190,3 +190,43 @@ def test_blend_prediction_limits():
     assert alpha == pytest.approx(1.0, abs=0.05) and blend < 0.1 * vp
     vp, blend, alpha = blend_prediction(a, b, p, a + 0.5, b + 0.5, 32, 32)
     assert alpha < 0.05 and blend == pytest.approx(vp, rel=0.1)
+
+
+ADAPTIVE = ServerConfig(adaptive=True, pass_paths=4 * 64 * 64, first_pass_spp=64, min_samples=64, max_active=64)
+
+
+def test_adaptive_same_alone_and_in_mix():
+    """Predictive allocation: a job's pass sizes follow its own estimates, so
+    its samples, stopping point and image are the same in any mix."""
+    def run(mix):
+        s = Server(FakeBackend(noise=0.3), ADAPTIVE, clock=Clock())
+        for k in range(mix):   # earlier arrivals take the pass budget first
+            s.submit(req(seed=100 + k, target=5e-4, max_samples=4096))
+        jid = s.submit(req(seed=7, target=1e-3, max_samples=4096))
+        while not s.idle():
+            s.step()
+        j = s.status(jid)
+        return j.result, j.samples, j.n_a, j.n_b
+
+    r0, r1 = run(0), run(6)
+    assert r0[1:] == r1[1:] and np.array_equal(r0[0], r1[0])
+
+
+def test_adaptive_meets_target_in_few_passes():
+    s = Server(FakeBackend(noise=0.3), ADAPTIVE, clock=Clock())
+    jid = s.submit(req(seed=3, target=1e-3, max_samples=100000))
+    while not s.idle():
+        s.step()
+    j = s.status(jid)
+    assert j.estimate <= 1e-3
+    assert j.passes <= 4                          # fixed 16-spp passes would need dozens
+    assert abs(j.n_a - j.n_b) <= j.samples // 4   # halves stay balanced
+
+
+def test_adaptive_finishes_jobs_in_admission_order():
+    s = Server(FakeBackend(noise=0.3), ADAPTIVE, clock=Clock())
+    ids = [s.submit(req(seed=20 + k, target=1e-3, max_samples=100000)) for k in range(6)]
+    while not s.idle():
+        s.step()
+    finished = [s.status(i).finished for i in ids]
+    assert finished == sorted(finished)

@@ -157,6 +157,7 @@ _SIGS = [
     ("vr_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
     ("vr_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
     ("vr_denoise_device", C.c_int, [P, P, P, P, C.c_float, P, C.c_uint32, C.c_uint32, P]),
+    ("vr_denoise_batch_device", C.c_int, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
     ("vr_denoiser_gradients_device", C.c_int,
      [P, P, P, P, P, C.c_float, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P]),
     ("vr_denoiser_train_step_device", C.c_int,

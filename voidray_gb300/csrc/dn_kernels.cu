@@ -460,8 +460,8 @@ __device__ __forceinline__ float finite_or_zero(float v) {
 }
 
 __global__ void k_preprocess(const float4* __restrict__ rad, const float4* __restrict__ alb,
-                             const float4* __restrict__ nrm, float scale, int n, int ih, int iw, int h, int w,
-                             bf16* __restrict__ x0) {
+                             const float4* __restrict__ nrm, float scale_all, const float* __restrict__ scales, int n,
+                             int ih, int iw, int h, int w, bf16* __restrict__ x0) {
     const size_t total = (size_t)n * h * w;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < total; p += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(p % w);
@@ -471,6 +471,7 @@ __global__ void k_preprocess(const float4* __restrict__ rad, const float4* __res
 #pragma unroll
         for (int k = 0; k < 8; ++k) lo.h[k] = hi.h[k] = __float2bfloat16_rn(0.0f);
         if (y < ih && x < iw) {
+            const float scale = scales ? scales[nn] : scale_all;
             const size_t s = ((size_t)nn * ih + y) * iw + x;
             const float4 r = rad[s], a = alb[s], q = nrm[s];
             const float ar = finite_or_zero(a.x * scale), ag = finite_or_zero(a.y * scale),
@@ -494,14 +495,16 @@ __global__ void k_preprocess(const float4* __restrict__ rad, const float4* __res
     }
 }
 
-__global__ void k_postprocess(const float* __restrict__ out, int cout, const float4* __restrict__ alb, float scale,
-                              int n, int ih, int iw, int h, int w, float4* __restrict__ rgba) {
+__global__ void k_postprocess(const float* __restrict__ out, int cout, const float4* __restrict__ alb,
+                              float scale_all, const float* __restrict__ scales, int n, int ih, int iw, int h, int w,
+                              float4* __restrict__ rgba) {
     const size_t total = (size_t)n * ih * iw;
     for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < total; s += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(s % iw);
         const int y = (int)((s / iw) % ih);
         const int nn = (int)(s / ((size_t)iw * ih));
         const float* o = out + (((size_t)nn * h + y) * w + x) * cout;
+        const float scale = scales ? scales[nn] : scale_all;
         const float4 a = alb[s];
         float4 r;
         r.x = expm1f(fminf(fmaxf(o[0], 0.0f), 80.0f)) * (finite_or_zero(a.x * scale) + DEMOD_EPS);
@@ -690,17 +693,17 @@ cudaError_t up_bwd(const bf16* dcat, int ccat, const bf16* act, bf16* dz, int n,
     return cudaGetLastError();
 }
 
-cudaError_t preprocess(const float4* rad, const float4* alb, const float4* nrm, float scale, int n, int img_h,
-                       int img_w, int h, int w, bf16* x0, cudaStream_t st) {
+cudaError_t preprocess(const float4* rad, const float4* alb, const float4* nrm, float scale, const float* scales,
+                       int n, int img_h, int img_w, int h, int w, bf16* x0, cudaStream_t st) {
     const size_t total = (size_t)n * h * w;
-    k_preprocess<<<grid_for(total, 256), 256, 0, st>>>(rad, alb, nrm, scale, n, img_h, img_w, h, w, x0);
+    k_preprocess<<<grid_for(total, 256), 256, 0, st>>>(rad, alb, nrm, scale, scales, n, img_h, img_w, h, w, x0);
     return cudaGetLastError();
 }
 
-cudaError_t postprocess(const float* out, int cout, const float4* alb, float scale, int n, int img_h, int img_w,
-                        int h, int w, float4* rgba, cudaStream_t st) {
+cudaError_t postprocess(const float* out, int cout, const float4* alb, float scale, const float* scales, int n,
+                        int img_h, int img_w, int h, int w, float4* rgba, cudaStream_t st) {
     const size_t total = (size_t)n * img_h * img_w;
-    k_postprocess<<<grid_for(total, 256), 256, 0, st>>>(out, cout, alb, scale, n, img_h, img_w, h, w, rgba);
+    k_postprocess<<<grid_for(total, 256), 256, 0, st>>>(out, cout, alb, scale, scales, n, img_h, img_w, h, w, rgba);
     return cudaGetLastError();
 }
 

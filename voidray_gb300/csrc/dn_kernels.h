@@ -65,15 +65,16 @@ cudaError_t skip_bwd(const bf16* dcat, int ccat, int coff, const bf16* dpool, co
 // dz[q][c] = (sum of the 2x2 fine pixels dcat[.][c], c < c1) * (act[q][c] > 0), coarse resolution (hc, wc)
 cudaError_t up_bwd(const bf16* dcat, int ccat, const bf16* act, bf16* dz, int n, int hc, int wc, int c1,
                    cudaStream_t st);
-// Network input from renderer buffers (RGBA f32, width x height, sums scaled
-// by `scale`): ch 0-2 log1p(radiance / (albedo + DEMOD_EPS)), 3-5 albedo,
-// 6-8 normal, 9-15 zero; pixels outside the image (padding to h x w) zero.
+// Network input from renderer buffers (RGBA f32, n images of width x height,
+// sums scaled by scales[image] (device) or, when scales is null, by `scale`):
+// ch 0-2 log1p(radiance / (albedo + DEMOD_EPS)), 3-5 albedo, 6-8 normal,
+// 9-15 zero; pixels outside the image (padding to h x w) zero.
 constexpr float DEMOD_EPS = 0.01f;
-cudaError_t preprocess(const float4* rad, const float4* alb, const float4* nrm, float scale, int n, int img_h,
-                       int img_w, int h, int w, bf16* x0, cudaStream_t st);
+cudaError_t preprocess(const float4* rad, const float4* alb, const float4* nrm, float scale, const float* scales,
+                       int n, int img_h, int img_w, int h, int w, bf16* x0, cudaStream_t st);
 // out[p][0..2] (log irradiance) -> rgba = expm1(clamp(o, 0, 80)) * (albedo + DEMOD_EPS), alpha 1
-cudaError_t postprocess(const float* out, int cout, const float4* alb, float scale, int n, int img_h, int img_w,
-                        int h, int w, float4* rgba, cudaStream_t st);
+cudaError_t postprocess(const float* out, int cout, const float4* alb, float scale, const float* scales, int n,
+                        int img_h, int img_w, int h, int w, float4* rgba, cudaStream_t st);
 // Loss against the target radiance; writes the gradient (bf16, [P][cout],
 // zero beyond channel 2, scaled by inv_count) and adds the loss sum to *loss_sum.
 constexpr int LOSS_L1_LOG = 0;  // L1 of the log-demodulated prediction

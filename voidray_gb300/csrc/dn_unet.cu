@@ -119,6 +119,8 @@ struct vr_denoiser {
     int backend = VR_DN_BACKEND_MMA_SYNC;  // forward convolutions
     bf16* up_tmp = nullptr;                // materialised 2x upsample (tcgen05 forward)
     uint32_t* status = nullptr;            // device: bounded-wait timeouts of the tcgen05 kernel
+    float* scales_dev = nullptr;           // per-image input scales of batched inference
+    uint32_t scales_cap = 0;
 };
 
 namespace {
@@ -310,7 +312,7 @@ vr_status loss_and_grads(vr_denoiser* d, const float* rgba, const float* albedo,
     if ((r = ensure_ws(d, (int)batch, (int)height, (int)width, true)) != VR_OK) return r;
     const int n = (int)batch, h = (int)height, w = (int)width;
     DN_CK(dn::preprocess(reinterpret_cast<const float4*>(rgba), reinterpret_cast<const float4*>(albedo),
-                         reinterpret_cast<const float4*>(normal), scale_in, n, h, w, h, w, d->act[X0], st));
+                         reinterpret_cast<const float4*>(normal), scale_in, nullptr, n, h, w, h, w, d->act[X0], st));
     if ((r = forward(d, st)) != VR_OK) return r;
     DN_CK(cudaMemsetAsync(d->loss, 0, sizeof(float), st));
     const float inv = 1.0f / (3.0f * (float)n * h * w);
@@ -402,7 +404,7 @@ vr_status vr_denoiser_destroy(vr_denoiser* d) {
     cudaDeviceSynchronize();
     free_ws(d);
     for (void* p : {(void*)d->w32, (void*)d->g32, (void*)d->m, (void*)d->v, (void*)d->w16, (void*)d->wt16,
-                    (void*)d->loss, (void*)d->status})
+                    (void*)d->loss, (void*)d->status, (void*)d->scales_dev})
         if (p) cudaFree(p);
     delete d;
     return VR_OK;
@@ -469,25 +471,54 @@ vr_status vr_denoiser_set_params(vr_denoiser* d, const float* host, uint64_t cou
     return VR_OK;
 }
 
-vr_status vr_denoise_device(vr_denoiser* d, const float* rgba, const float* albedo, const float* normal, float scale,
-                            float* out_rgba, uint32_t width, uint32_t height, void* stream) {
+namespace {
+vr_status denoise_impl(vr_denoiser* d, const float* rgba, const float* albedo, const float* normal, float scale,
+                       const float* scales_host, float* out_rgba, uint32_t batch, uint32_t width, uint32_t height,
+                       void* stream) {
     if (!d || !rgba || !albedo || !normal || !out_rgba) return vr::set_error(VR_ERR_INVALID, "null argument");
-    if (!width || !height || (uint64_t)width * height > (1ull << 28))
+    if (!batch || !width || !height || (uint64_t)batch * width * height > (1ull << 28))
         return vr::set_error(VR_ERR_INVALID, "bad image size");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int h = (int)((height + 7) & ~7u), w = (int)((width + 7) & ~7u);
+    const int h = (int)((height + 7) & ~7u), w = (int)((width + 7) & ~7u), n = (int)batch;
     vr_status r;
-    if (!(d->wn == 1 && d->wh == h && d->ww == w)) {
+    if (!(d->wn == n && d->wh == h && d->ww == w)) {
         DN_CK(cudaStreamSynchronize(st));
-        if ((r = ensure_ws(d, 1, h, w, false)) != VR_OK) return r;
+        if ((r = ensure_ws(d, n, h, w, false)) != VR_OK) return r;
+    }
+    const float* scales = nullptr;
+    if (scales_host) {
+        if (d->scales_cap < batch) {
+            DN_CK(cudaStreamSynchronize(st));
+            if (d->scales_dev) cudaFree(d->scales_dev);
+            d->scales_dev = nullptr;
+            d->scales_cap = 0;
+            DN_CK(cudaMalloc(&d->scales_dev, batch * sizeof(float)));
+            d->scales_cap = batch;
+        }
+        // pageable source: staged before the call returns, ordered on the stream
+        DN_CK(cudaMemcpyAsync(d->scales_dev, scales_host, batch * sizeof(float), cudaMemcpyHostToDevice, st));
+        scales = d->scales_dev;
     }
     DN_CK(dn::preprocess(reinterpret_cast<const float4*>(rgba), reinterpret_cast<const float4*>(albedo),
-                         reinterpret_cast<const float4*>(normal), scale, 1, (int)height, (int)width, h, w,
+                         reinterpret_cast<const float4*>(normal), scale, scales, n, (int)height, (int)width, h, w,
                          d->act[X0], st));
     if ((r = forward(d, st)) != VR_OK) return r;
-    DN_CK(dn::postprocess(d->out, OUT_C, reinterpret_cast<const float4*>(albedo), scale, 1, (int)height, (int)width,
-                          h, w, reinterpret_cast<float4*>(out_rgba), st));
+    DN_CK(dn::postprocess(d->out, OUT_C, reinterpret_cast<const float4*>(albedo), scale, scales, n, (int)height,
+                          (int)width, h, w, reinterpret_cast<float4*>(out_rgba), st));
     return VR_OK;
+}
+}  // namespace
+
+vr_status vr_denoise_device(vr_denoiser* d, const float* rgba, const float* albedo, const float* normal, float scale,
+                            float* out_rgba, uint32_t width, uint32_t height, void* stream) {
+    return denoise_impl(d, rgba, albedo, normal, scale, nullptr, out_rgba, 1, width, height, stream);
+}
+
+vr_status vr_denoise_batch_device(vr_denoiser* d, const float* rgba, const float* albedo, const float* normal,
+                                  const float* scales, float* out_rgba, uint32_t batch, uint32_t width,
+                                  uint32_t height, void* stream) {
+    if (!scales) return vr::set_error(VR_ERR_INVALID, "scales is NULL");
+    return denoise_impl(d, rgba, albedo, normal, 1.0f, scales, out_rgba, batch, width, height, stream);
 }
 
 vr_status vr_denoiser_gradients_device(vr_denoiser* d, const float* rgba, const float* albedo, const float* normal,

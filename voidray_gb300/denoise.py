@@ -116,6 +116,12 @@ class Denoiser:
         check(lib().vr_denoise_device(self.handle, _p(rgba), _p(albedo), _p(normal), float(scale), _p(out),
                                       int(width), int(height), C.c_void_p(stream or None)))
 
+    def denoise_batch(self, rgba, albedo, normal, scales, out, width: int, height: int, stream: int = 0) -> None:
+        """Images stacked as [batch][height][width][4] device buffers; scales: one float per image."""
+        sc = np.ascontiguousarray(scales, np.float32)
+        check(lib().vr_denoise_batch_device(self.handle, _p(rgba), _p(albedo), _p(normal), sc.ctypes.data, _p(out),
+                                            int(sc.size), int(width), int(height), C.c_void_p(stream or None)))
+
     def gradients(self, rgba, albedo, normal, target, batch: int, width: int, height: int, scale_in: float = 1.0,
                   scale_target: float = 1.0, stream: int = 0):
         """(loss, gradient vector) of one batch, no update."""

@@ -44,6 +44,7 @@ deterministic CPU stand-in used by the scheduler tests).
 from __future__ import annotations
 
 import itertools
+import math
 import time
 from dataclasses import dataclass, field
 from typing import Any, Callable, Optional
@@ -84,6 +85,7 @@ class JobState:
     error: str = ""
     alpha: float = 0.0         # weight of the denoised image in the output
     plain_estimate: float = float("inf")
+    next_spp: int = 0          # adaptive: samples of the job's next pass (0: first pass)
 
     @property
     def latency(self) -> Optional[float]:
@@ -101,6 +103,17 @@ class ServerConfig:
     max_active: int = 64
     spp_per_pass: int = 16
     min_samples: int = 32      # no error estimate before this many samples
+    # predictive allocation (adaptive=True): a job's next pass renders the
+    # samples its own estimate predicts it still needs (error ~ 1/n), split
+    # evenly over its halves; jobs take their passes in admission order while
+    # the pass has paths left (the first job of a pass always runs), so the
+    # GPU gets large passes and jobs finish in order.  A job's sequence of
+    # pass sizes depends only on its own estimates, never on the mix.
+    adaptive: bool = False
+    pass_paths: int = 1 << 24  # paths per pass the scheduler aims for
+    first_pass_spp: int = 64
+    min_pass_spp: int = 8
+    overshoot: float = 1.1     # planned samples x this, against estimate noise
 
 
 class FakeBackend:
@@ -232,24 +245,46 @@ class GpuBackend:
         return out
 
     def estimate(self, job: JobState) -> float:
+        return self.estimate_many([job])[0]
+
+    def estimate_many(self, jobs: list[JobState]) -> list[float]:
+        """Plain estimates of all jobs; for denoising jobs close enough to
+        their target, the blend prediction, with the denoiser run once over
+        the half-buffers of all of them (batched per image size)."""
         t = self.torch
-        na, nb = job.n_a, job.n_b
-        a = job.bufs[0][..., :3].double() / max(na, 1)
-        b = job.bufs[1][..., :3].double() / max(nb, 1)
-        plain = _estimate(a, b, na, nb, xp=t)
-        job.plain_estimate, job.alpha = plain, 0.0
-        if len(job.bufs) != 6 or plain > self.denoise_below * job.req.target_relmse:
-            return plain
-        with t.cuda.stream(self.stream):
-            da = self._denoise(job.bufs[0], job.bufs[2], job.bufs[4], 1.0 / na)[..., :3].double()
-            db = self._denoise(job.bufs[1], job.bufs[3], job.bufs[5], 1.0 / nb)[..., :3].double()
-        self.stream.synchronize()
-        p = (a * na + b * nb) / (na + nb)
-        _, blend, alpha = blend_prediction(a, b, p, da, db, na, nb, xp=t)
-        if blend < plain:
-            job.alpha = alpha
-            return blend
-        return plain
+        out, halves = [], []
+        for job in jobs:
+            na, nb = job.n_a, job.n_b
+            a = job.bufs[0][..., :3].double() / max(na, 1)
+            b = job.bufs[1][..., :3].double() / max(nb, 1)
+            plain = _estimate(a, b, na, nb, xp=t)
+            job.plain_estimate, job.alpha = plain, 0.0
+            out.append(plain)
+            if len(job.bufs) == 6 and plain <= self.denoise_below * job.req.target_relmse:
+                halves.append((len(out) - 1, job, a, b))
+        groups = {}
+        for item in halves:
+            groups.setdefault((item[1].req.height, item[1].req.width), []).append(item)
+        for (h, w), items in groups.items():
+            with t.cuda.stream(self.stream):
+                rad = t.stack([x for _, j, *_ in items for x in (j.bufs[0], j.bufs[1])])
+                alb = t.stack([x for _, j, *_ in items for x in (j.bufs[2], j.bufs[3])])
+                nrm = t.stack([x for _, j, *_ in items for x in (j.bufs[4], j.bufs[5])])
+                scales = [s for _, j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
+                den = t.empty_like(rad)
+                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=self.stream.cuda_stream)
+                self.denoise_calls += 1
+            self.stream.synchronize()
+            for k, (i, job, a, b) in enumerate(items):
+                na, nb = job.n_a, job.n_b
+                da = den[2 * k][..., :3].double()
+                db = den[2 * k + 1][..., :3].double()
+                p = (a * na + b * nb) / (na + nb)
+                _, blend, alpha = blend_prediction(a, b, p, da, db, na, nb, xp=t)
+                if blend < out[i]:
+                    job.alpha = alpha
+                    out[i] = blend
+        return out
 
     def result(self, job: JobState) -> np.ndarray:
         t = self.torch
@@ -336,44 +371,87 @@ class Server:
         self.backend.free(job)
 
     # -- passes ------------------------------------------------------------
+    def _plan(self) -> list:
+        """Work items (job, half, first sample, samples) of the next pass."""
+        work = []
+        if not self.cfg.adaptive:
+            for jid in self.active:
+                job = self.jobs[jid]
+                n = min(self.cfg.spp_per_pass, job.req.max_samples - job.samples)
+                work.append((job, job.passes % 2, job.samples, n))
+            return work
+        budget = self.cfg.pass_paths
+        for jid in self.active:
+            job = self.jobs[jid]
+            want = job.next_spp or self.cfg.first_pass_spp
+            want = max(1, min(want, job.req.max_samples - job.samples))
+            paths = want * job.req.width * job.req.height
+            if work and paths > budget:
+                continue  # runs in a later pass, with the same size
+            budget -= paths
+            half = (want + 1) // 2
+            work.append((job, 0, job.samples, half))
+            if want - half:
+                work.append((job, 1, job.samples + half, want - half))
+        return work
+
+    def _next_spp(self, job: JobState) -> int:
+        if not math.isfinite(job.estimate):
+            return self.cfg.first_pass_spp
+        need = job.samples * job.estimate / job.req.target_relmse
+        more = int(math.ceil(self.cfg.overshoot * max(0.0, need - job.samples)))
+        more = max(self.cfg.min_pass_spp, more + (more & 1))
+        return min(more, job.req.max_samples - job.samples)
+
     def step(self) -> int:
-        """Admits what fits, renders one pass of every active job, retires
+        """Admits what fits, renders one pass (every active job, or with
+        adaptive allocation the jobs the pass has room for), estimates, retires
         finished jobs.  Returns the number of jobs rendered."""
         self._admit()
         if not self.active:
             return 0
-        work = []
-        for jid in self.active:
-            job = self.jobs[jid]
-            n = min(self.cfg.spp_per_pass, job.req.max_samples - job.samples)
-            work.append((job, job.passes % 2, job.samples, n))
+        work = self._plan()
         try:
             self.backend.render(work)
         except Exception as e:
-            for job, *_ in work:
+            for job in {id(w[0]): w[0] for w in work}.values():
                 job.state, job.error, job.finished = "failed", str(e), self.clock()
                 self._release(job)
-            self.active = []
+                self.active.remove(job.job_id)
             return 0
         self.passes += 1
-        done = []
+        rendered = {}
         for job, b, first, n in work:
             job.samples += n
             if b == 0:
                 job.n_a += n
             else:
                 job.n_b += n
+            rendered[job.job_id] = job
+        check = []
+        for job in rendered.values():
             job.passes += 1
             if job.n_a and job.n_b and job.samples >= self.cfg.min_samples:
-                job.estimate = self.backend.estimate(job)
+                check.append(job)
+        if check:
+            if hasattr(self.backend, "estimate_many"):
+                ests = self.backend.estimate_many(check)
+            else:
+                ests = [self.backend.estimate(j) for j in check]
+            for job, e in zip(check, ests):
+                job.estimate = e
+        done = []
+        for job in rendered.values():
             if job.estimate <= job.req.target_relmse or job.samples >= job.req.max_samples:
                 job.result = self.backend.result(job)
                 job.state, job.finished = "done", self.clock()
                 done.append(job.job_id)
+            elif self.cfg.adaptive:
+                job.next_spp = self._next_spp(job)
         for jid in done:
             self._release(self.jobs[jid])
             self.active.remove(jid)
-        return len(work)
+        return len(rendered)
 
     def idle(self) -> bool:
         return not self.waiting and not self.active
