@@ -165,22 +165,26 @@ def _estimate(a, b, na: int, nb: int, xp=np) -> float:
     return float(xp.mean(var / (m * m + EPS_REL)))
 
 
-def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
-    """Predicted relMSE of the plain mean P and of the best blend
-    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
-    the full mean p and the denoised half means da, db.  Returns
-    (plain, blend, alpha)."""
-    n = na + nb
+def blend_moments(a, b, p, da, db, xp=np) -> list:
+    """The five pixel means the blend prediction needs (arrays or tensors,
+    not yet converted to floats, so a caller can read many at once)."""
     den = p * p + EPS_REL
     ab = a - b
-    s_ab = float(xp.mean(ab * ab / den))
-    v_p = s_ab * na * nb / (n * n)                      # Var(P)
-    var_a, var_b = s_ab * nb / n, s_ab * na / n          # Var(A), Var(B)
-    e_a = float(xp.mean((da - b) ** 2 / den)) - var_b   # error of D(A)
-    e_b = float(xp.mean((db - a) ** 2 / den)) - var_a   # error of D(B)
     dd = da - db
-    tau2 = float(xp.mean(dd * dd / den)) * na * nb / n  # residual noise x samples
-    kap = float(xp.mean(dd * ab / den)) * na * nb / n   # covariance with the plain noise x samples
+    return [xp.mean(ab * ab / den), xp.mean((da - b) ** 2 / den), xp.mean((db - a) ** 2 / den),
+            xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
+
+
+def blend_from_moments(m, na: int, nb: int):
+    """(plain, blend, alpha) from blend_moments() values."""
+    s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
+    n = na + nb
+    v_p = s_ab * na * nb / (n * n)                     # Var(P)
+    var_a, var_b = s_ab * nb / n, s_ab * na / n         # Var(A), Var(B)
+    e_a = s_dab - var_b                                 # error of D(A)
+    e_b = s_dba - var_a                                 # error of D(B)
+    tau2 = s_dd * na * nb / n                           # residual noise x samples
+    kap = s_ddab * na * nb / n                          # covariance with the plain noise x samples
     bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
     v_eta, c = tau2 / n, kap / n
     e_d = bias2 + v_eta
@@ -188,6 +192,168 @@ def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
     alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
     blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
     return v_p, max(blend, 0.0), alpha
+
+
+def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
+    """Predicted relMSE of the plain mean P and of the best blend
+    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
+    the full mean p and the denoised half means da, db.  Returns
+    (plain, blend, alpha)."""
+    return blend_from_moments(blend_moments(a, b, p, da, db, xp), na, nb)
+
+
+class GpuBackend:
+    """Device accumulation buffers (torch) and one vr_batch for every pass;
+    with a denoiser, jobs that ask for it also get AOV buffers and blended
+    outputs (the module docstring describes the prediction)."""
+
+    def __init__(self, max_wave_paths: int = 0, denoiser=None, denoise_below: float = 16.0):
+        import torch
+
+        from .batch import Batch
+
+        self.torch = torch
+        self.batch = Batch(max_wave_paths)
+        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
+        self.stream = torch.cuda.Stream()
+        self.dn = denoiser
+        # the denoiser prediction runs once the plain estimate is within this
+        # factor of the job's target (it cannot finish a job much earlier)
+        self.denoise_below = denoise_below
+        self.denoise_calls = 0
+        self.time = {"render": 0.0, "estimate": 0.0, "result": 0.0}  # host wall seconds per phase
+
+    def alloc(self, job: JobState):
+        t = self.torch
+        h, w = job.req.height, job.req.width
+        k = 6 if (job.req.denoise and self.dn is not None) else 2
+        # [A, B] radiance sums, then albedo A/B and normal A/B sums
+        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
+
+    def free(self, job: JobState) -> None:
+        job.bufs = None
+
+    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        from dataclasses import replace
+
+        from .batch import RenderJob
+
+        jobs = []
+        for job, b, first, n in work:
+            # buffers accumulate raw sums: total_samples = 1
+            st = replace(job.req.settings, total_samples=1)
+            aov = len(job.bufs) == 6
+            jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
+                                  job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
+                                  job.bufs[4 + b].data_ptr() if aov else 0))
+        t0 = time.perf_counter()
+        self.batch.render(jobs, self.stream.cuda_stream)
+        self.batch.synchronize(self.stream.cuda_stream)
+        self.time["render"] += time.perf_counter() - t0
+
+    def _denoise(self, rad, alb, nrm, scale: float):
+        t = self.torch
+        h, w = rad.shape[0], rad.shape[1]
+        out = t.empty((h, w, 4), dtype=t.float32, device="cuda")
+        self.dn.denoise(rad, alb, nrm, scale, out, w, h, stream=self.stream.cuda_stream)
+        self.denoise_calls += 1
+        return out
+
+    def estimate(self, job: JobState) -> float:
+        return self.estimate_many([job])[0]
+
+    def estimate_many(self, jobs: list[JobState]) -> list[float]:
+        """Plain estimates of all jobs; for denoising jobs close enough to
+        their target, the blend prediction, with the denoiser run once over
+        the half-buffers of all of them (batched per image size).  The pixel
+        means of all jobs are read back in one transfer."""
+        t = self.torch
+        t0 = time.perf_counter()
+        halves, plain_m = [], []
+        for job in jobs:
+            na, nb = job.n_a, job.n_b
+            a = job.bufs[0][..., :3].double() / max(na, 1)
+            b = job.bufs[1][..., :3].double() / max(nb, 1)
+            n = na + nb
+            m = (a * na + b * nb) / n
+            plain_m.append(t.mean((a - b) ** 2 * (na * nb / (n * n)) / (m * m + EPS_REL)))
+            halves.append((job, a, b, m))
+        out = [float(x) for x in t.stack(plain_m).cpu()]
+        for job, e in zip(jobs, out):
+            job.plain_estimate, job.alpha = e, 0.0
+        cand = [(i, *h) for i, h in enumerate(halves)
+                if len(h[0].bufs) == 6 and out[i] <= self.denoise_below * h[0].req.target_relmse]
+        groups = {}
+        for item in cand:
+            groups.setdefault((item[1].req.height, item[1].req.width), []).append(item)
+        for (h, w), items in groups.items():
+            with t.cuda.stream(self.stream):
+                rad = t.stack([x for _, j, *_ in items for x in (j.bufs[0], j.bufs[1])])
+                alb = t.stack([x for _, j, *_ in items for x in (j.bufs[2], j.bufs[3])])
+                nrm = t.stack([x for _, j, *_ in items for x in (j.bufs[4], j.bufs[5])])
+                scales = [s for _, j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
+                den = t.empty_like(rad)
+                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=self.stream.cuda_stream)
+                self.denoise_calls += 1
+                mom = []
+                for k, (i, job, a, b, m) in enumerate(items):
+                    mom += blend_moments(a, b, m, den[2 * k][..., :3].double(), den[2 * k + 1][..., :3].double(), t)
+                vals = [float(x) for x in t.stack(mom).cpu()]
+            for k, (i, job, a, b, m) in enumerate(items):
+                _, blend, alpha = blend_from_moments(vals[5 * k:5 * k + 5], job.n_a, job.n_b)
+                if blend < out[i]:
+                    job.alpha = alpha
+                    out[i] = blend
+        self.time["estimate"] += time.perf_counter() - t0
+        return out
+
+    def result(self, job: JobState) -> np.ndarray:
+        a, b = job.bufs
+        return (a + b) / (job.n_a + job.n_b)
+
+
+def _estimate(a, b, na: int, nb: int, xp=np) -> float:
+    n = na + nb
+    m = (a * na + b * nb) / n
+    var = (a - b) ** 2 * (na * nb) / (n * n)
+    return float(xp.mean(var / (m * m + EPS_REL)))
+
+
+def blend_moments(a, b, p, da, db, xp=np) -> list:
+    """The five pixel means the blend prediction needs (arrays or tensors,
+    not yet converted to floats, so a caller can read many at once)."""
+    den = p * p + EPS_REL
+    ab = a - b
+    dd = da - db
+    return [xp.mean(ab * ab / den), xp.mean((da - b) ** 2 / den), xp.mean((db - a) ** 2 / den),
+            xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
+
+
+def blend_from_moments(m, na: int, nb: int):
+    """(plain, blend, alpha) from blend_moments() values."""
+    s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
+    n = na + nb
+    v_p = s_ab * na * nb / (n * n)                     # Var(P)
+    var_a, var_b = s_ab * nb / n, s_ab * na / n         # Var(A), Var(B)
+    e_a = s_dab - var_b                                 # error of D(A)
+    e_b = s_dba - var_a                                 # error of D(B)
+    tau2 = s_dd * na * nb / n                           # residual noise x samples
+    kap = s_ddab * na * nb / n                          # covariance with the plain noise x samples
+    bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
+    v_eta, c = tau2 / n, kap / n
+    e_d = bias2 + v_eta
+    q = e_d + v_p - 2.0 * c
+    alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
+    blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
+    return v_p, max(blend, 0.0), alpha
+
+
+def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
+    """Predicted relMSE of the plain mean P and of the best blend
+    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
+    the full mean p and the denoised half means da, db.  Returns
+    (plain, blend, alpha)."""
+    return blend_from_moments(blend_moments(a, b, p, da, db, xp), na, nb)
 
 
 class GpuBackend:
@@ -288,17 +454,21 @@ class GpuBackend:
 
     def result(self, job: JobState) -> np.ndarray:
         t = self.torch
+        t0 = time.perf_counter()
         n = job.n_a + job.n_b
         p = (job.bufs[0] + job.bufs[1]) / n
         if job.alpha <= 0.0:
-            return p[..., :3].cpu().numpy()
-        with t.cuda.stream(self.stream):
-            alb = (job.bufs[2] + job.bufs[3]) / n
-            nrm = (job.bufs[4] + job.bufs[5]) / n
-            d = self._denoise(p, alb, nrm, 1.0)
-            y = job.alpha * d[..., :3] + (1.0 - job.alpha) * p[..., :3]
-        self.stream.synchronize()
-        return y.cpu().numpy()
+            out = p[..., :3].cpu().numpy()
+        else:
+            with t.cuda.stream(self.stream):
+                alb = (job.bufs[2] + job.bufs[3]) / n
+                nrm = (job.bufs[4] + job.bufs[5]) / n
+                d = self._denoise(p, alb, nrm, 1.0)
+                y = job.alpha * d[..., :3] + (1.0 - job.alpha) * p[..., :3]
+            self.stream.synchronize()
+            out = y.cpu().numpy()
+        self.time["result"] += time.perf_counter() - t0
+        return out
 
 
 class Server:
