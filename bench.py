@@ -33,6 +33,8 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
+# DRAM bytes per k_extend launch at the default workload (ncu capture summarised in profiles/)
+K_EXTEND_DRAM_BYTES_PER_LAUNCH = 2.374e9
 sys.path.insert(0, str(ROOT))
 
 CLOCK_FIELDS = ["uuid", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
@@ -220,9 +222,10 @@ def serving_benchmark(args):
     # them in admission order).  served_denoised: the same plus AOVs and the
     # denoiser blend.
     plain_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=1, spp_per_pass=spp_pass, min_samples=64)
-    served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pass_paths=1 << 24,
-                              first_pass_spp=64, min_samples=64)
-    out["served_config"] = {"adaptive": True, "pass_paths": 1 << 24, "first_pass_spp": 64, "max_active": 64}
+    served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
+                              pass_paths=1 << 24, first_pass_spp=64, min_samples=64)
+    out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "first_pass_spp": 64,
+                            "max_active": 64}
     modes = (("plain", plain_cfg, False), ("served", served_cfg, False), ("served_denoised", served_cfg, True))
     for name, cfg, dn in modes:
         active = cfg.max_active
@@ -469,6 +472,7 @@ def main():
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    default_workload = (args.width, args.height, args.spp, args.freq) == (1920, 1080, 256, 316)
     if not args.no_work_count:
         N.check(lib.vr_scene_instrument(acc.handle, N.INSTR_WORK))
         c0 = acc.stats()
@@ -485,7 +489,12 @@ def main():
         ext_launches_per_frame = ins.stage_launches[1] / args.steps
         achieved = alg_bytes / (ext_ms_per_frame / 1e3) / 1e9
         roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit BVH2 traversal)", "achieved": achieved,
-                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                    # ncu dram__bytes_read.sum + dram__bytes_write.sum per k_extend launch, mean over the 12
+                    # depths of one full-size wavefront of this workload (a constant from that capture:
+                    # profiles/k_extend_k_shadow_1920x1080_256spp_dram_traffic.md); only valid at the
+                    # default workload
+                    "traffic": K_EXTEND_DRAM_BYTES_PER_LAUNCH if default_workload else None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
                     "algorithmic_bytes_per_launch": alg_bytes / max(ext_launches_per_frame, 1),
                     "avg_launch_ms": ext_ms_per_frame / max(ext_launches_per_frame, 1),

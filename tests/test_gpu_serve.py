@@ -49,8 +49,8 @@ def test_served_same_alone_and_in_mix(gpu):
     assert r0[1] < 256  # stopped on the error estimate
 
 
-@pytest.mark.parametrize("adaptive", [False, True])
-def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive):
+@pytest.mark.parametrize("adaptive,pipelined", [(False, False), (True, False), (True, True)])
+def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
     """With the denoiser in the loop (AOV buffers, blended output) a job's
     stopping point, blend weight and image still depend only on the job."""
     import voidray_gb300 as vr
@@ -59,8 +59,8 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive):
     from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig
 
     scenes = _scenes(vr, W)
-    cfg = ServerConfig(spp_per_pass=8, min_samples=16, adaptive=adaptive, pass_paths=40 * 32 * 16,
-                       first_pass_spp=16)
+    cfg = ServerConfig(spp_per_pass=8, min_samples=16, adaptive=adaptive, pipelined=pipelined,
+                       pass_paths=40 * 32 * 16, first_pass_spp=16)
     net = Denoiser.pretrained()
 
     def run(mix):
@@ -74,6 +74,7 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive):
                                   denoise=bool(k % 2)))
         while not srv.idle():
             srv.step()
+        backend.finish()
         j = srv.status(jid)
         assert backend.denoise_calls > 0
         return j.result, j.samples, j.alpha, j.estimate

@@ -230,3 +230,57 @@ def test_adaptive_finishes_jobs_in_admission_order():
         s.step()
     finished = [s.status(i).finished for i in ids]
     assert finished == sorted(finished)
+
+
+PIPELINED = ServerConfig(adaptive=True, pipelined=True, pass_paths=4 * 64 * 64, first_pass_spp=64, min_samples=64,
+                         max_active=64)
+
+
+class LaggingBackend(FakeBackend):
+    """Estimates become visible only after `lag` polls, like device work still in flight."""
+
+    def __init__(self, lag=2, **kw):
+        super().__init__(**kw)
+        self.lag = lag
+
+    def estimate_async(self, jobs, after):
+        return {"left": self.lag, "ests": [self.estimate(j) for j in jobs]}
+
+    def poll(self, handle, block=False):
+        if block:
+            handle["left"] = 0
+        if handle["left"] > 0:
+            handle["left"] -= 1
+            return None
+        return handle["ests"]
+
+
+@pytest.mark.parametrize("backend", [FakeBackend, LaggingBackend])
+def test_pipelined_same_alone_and_in_mix(backend):
+    """Pipelined passes: estimates arrive late, other jobs render meanwhile;
+    each job's samples and image are still those of the job alone."""
+    def run(mix):
+        s = Server(backend(noise=0.3), PIPELINED, clock=Clock())
+        for k in range(mix):
+            s.submit(req(seed=100 + k, target=5e-4, max_samples=4096))
+        jid = s.submit(req(seed=7, target=1e-3, max_samples=4096))
+        while not s.idle():
+            s.step()
+        j = s.status(jid)
+        assert j.estimate <= 1e-3 and not s.pending
+        return j.result, j.samples, j.n_a, j.n_b
+
+    r0, r1 = run(0), run(6)
+    assert r0[1:] == r1[1:] and np.array_equal(r0[0], r1[0])
+
+
+def test_pipelined_renders_while_estimates_are_in_flight():
+    be = LaggingBackend(lag=3, noise=0.3)
+    s = Server(be, PIPELINED, clock=Clock())
+    ids = [s.submit(req(seed=40 + k, target=1e-3, max_samples=100000)) for k in range(8)]
+    while not s.idle():
+        s.step()
+    # some pass rendered jobs while another job's estimate was still pending
+    seen = [set(j for j, *_ in call) for call in be.calls]
+    assert len(seen) >= 3 and any(len(a - b) > 0 for a, b in zip(seen, seen[1:]))
+    assert all(s.status(i).state == "done" for i in ids)

@@ -86,6 +86,7 @@ class JobState:
     alpha: float = 0.0         # weight of the denoised image in the output
     plain_estimate: float = float("inf")
     next_spp: int = 0          # adaptive: samples of the job's next pass (0: first pass)
+    pending: bool = False      # pipelined: an estimate is in flight
 
     @property
     def latency(self) -> Optional[float]:
@@ -114,6 +115,10 @@ class ServerConfig:
     first_pass_spp: int = 64
     min_pass_spp: int = 8
     overshoot: float = 1.1     # planned samples x this, against estimate noise
+    # pipelined (adaptive only, backends with render_async / estimate_async /
+    # poll): a job's error estimate runs on the device while the next pass
+    # renders the jobs whose next pass size is already known
+    pipelined: bool = False
 
 
 class FakeBackend:
@@ -156,6 +161,17 @@ class FakeBackend:
     def result(self, job: JobState) -> np.ndarray:
         a, b = job.bufs
         return (a + b) / (job.n_a + job.n_b)
+
+    # asynchronous interface (runs synchronously here; the scheduler logic is the same)
+    def render_async(self, work):
+        self.render(work)
+        return None
+
+    def estimate_async(self, jobs, after):
+        return [self.estimate(j) for j in jobs]
+
+    def poll(self, handle, block: bool = False):
+        return handle
 
 
 def _estimate(a, b, na: int, nb: int, xp=np) -> float:
@@ -215,7 +231,8 @@ class GpuBackend:
         self.torch = torch
         self.batch = Batch(max_wave_paths)
         self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
-        self.stream = torch.cuda.Stream()
+        self.stream = torch.cuda.Stream()      # renders
+        self.est_stream = torch.cuda.Stream()  # estimates and results (pipelined mode)
         self.dn = denoiser
         # the denoiser prediction runs once the plain estimate is within this
         # factor of the job's target (it cannot finish a job much earlier)
@@ -227,13 +244,99 @@ class GpuBackend:
         t = self.torch
         h, w = job.req.height, job.req.width
         k = 6 if (job.req.denoise and self.dn is not None) else 2
-        # [A, B] radiance sums, then albedo A/B and normal A/B sums
-        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
+        # [A, B] radiance sums, then albedo A/B and normal A/B sums; zeroed on
+        # the render stream so the first pass is ordered after the fill
+        with t.cuda.stream(self.stream):
+            return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
 
     def free(self, job: JobState) -> None:
         job.bufs = None
 
     def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        t0 = time.perf_counter()
+        self._enqueue(work)
+        self.batch.synchronize(self.stream.cuda_stream)
+        self.time["render"] += time.perf_counter() - t0
+
+    def render_async(self, work):
+        """Enqueues the pass; returns an event recorded after it on the render stream."""
+        t0 = time.perf_counter()
+        self._enqueue(work)
+        ev = self.torch.cuda.Event()
+        ev.record(self.stream)
+        self.time["render"] += time.perf_counter() - t0
+        return ev
+
+    def estimate_async(self, jobs: list[JobState], after):
+        """Enqueues every job's plain moments and (denoising jobs) the batched
+        denoiser and blend moments on the estimate stream, after event `after`;
+        the values land in pinned host memory.  poll() turns them into estimates."""
+        t = self.torch
+        t0 = time.perf_counter()
+        es = self.est_stream
+        with t.cuda.stream(es):
+            if after is not None:
+                es.wait_event(after)
+            vals, halves = [], []
+            for job in jobs:
+                na, nb = job.n_a, job.n_b
+                a = job.bufs[0][..., :3].double() / na
+                b = job.bufs[1][..., :3].double() / nb
+                n = na + nb
+                m = (a * na + b * nb) / n
+                vals.append(t.mean((a - b) ** 2 * (na * nb / (n * n)) / (m * m + EPS_REL)))
+                halves.append((job, a, b, m))
+            dn = [h for h in halves if len(h[0].bufs) == 6]
+            groups = {}
+            for item in dn:
+                groups.setdefault((item[0].req.height, item[0].req.width), []).append(item)
+            order = []
+            for (h, w), items in groups.items():
+                rad = t.stack([x for j, *_ in items for x in (j.bufs[0], j.bufs[1])])
+                alb = t.stack([x for j, *_ in items for x in (j.bufs[2], j.bufs[3])])
+                nrm = t.stack([x for j, *_ in items for x in (j.bufs[4], j.bufs[5])])
+                scales = [s for j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
+                den = t.empty_like(rad)
+                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=es.cuda_stream)
+                self.denoise_calls += 1
+                for k, (job, a, b, m) in enumerate(items):
+                    vals += blend_moments(a, b, m, den[2 * k][..., :3].double(), den[2 * k + 1][..., :3].double(), t)
+                    order.append(job)
+            stacked = t.stack(vals)
+            host = t.empty(stacked.shape, dtype=stacked.dtype, pin_memory=True)
+            host.copy_(stacked, non_blocking=True)
+            done = t.cuda.Event()
+            done.record(es)
+        self.time["estimate"] += time.perf_counter() - t0
+        return (done, host, list(jobs), order)
+
+    def poll(self, handle, block: bool = False):
+        done, host, jobs, order = handle
+        if not block and not done.query():
+            return None
+        t0 = time.perf_counter()
+        done.synchronize()
+        v = host.tolist()
+        out = v[:len(jobs)]
+        for job, e in zip(jobs, out):
+            job.plain_estimate, job.alpha = e, 0.0
+        pos = {id(j): i for i, j in enumerate(jobs)}
+        for k, job in enumerate(order):
+            base = len(jobs) + 5 * k
+            _, blend, alpha = blend_from_moments(v[base:base + 5], job.n_a, job.n_b)
+            i = pos[id(job)]
+            if blend < out[i]:
+                job.alpha = alpha
+                out[i] = blend
+        self.time["estimate"] += time.perf_counter() - t0
+        return out
+
+    def finish(self) -> None:
+        """Waits for both streams and reports kernel-side errors of the passes."""
+        self.est_stream.synchronize()
+        self.batch.synchronize(self.stream.cuda_stream)
+
+    def _enqueue(self, work: list[tuple[JobState, int, int, int]]) -> None:
         from dataclasses import replace
 
         from .batch import RenderJob
@@ -246,10 +349,7 @@ class GpuBackend:
             jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
                                   job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
                                   job.bufs[4 + b].data_ptr() if aov else 0))
-        t0 = time.perf_counter()
         self.batch.render(jobs, self.stream.cuda_stream)
-        self.batch.synchronize(self.stream.cuda_stream)
-        self.time["render"] += time.perf_counter() - t0
 
     def _denoise(self, rad, alb, nrm, scale: float):
         t = self.torch
@@ -308,165 +408,23 @@ class GpuBackend:
         return out
 
     def result(self, job: JobState) -> np.ndarray:
-        a, b = job.bufs
-        return (a + b) / (job.n_a + job.n_b)
-
-
-def _estimate(a, b, na: int, nb: int, xp=np) -> float:
-    n = na + nb
-    m = (a * na + b * nb) / n
-    var = (a - b) ** 2 * (na * nb) / (n * n)
-    return float(xp.mean(var / (m * m + EPS_REL)))
-
-
-def blend_moments(a, b, p, da, db, xp=np) -> list:
-    """The five pixel means the blend prediction needs (arrays or tensors,
-    not yet converted to floats, so a caller can read many at once)."""
-    den = p * p + EPS_REL
-    ab = a - b
-    dd = da - db
-    return [xp.mean(ab * ab / den), xp.mean((da - b) ** 2 / den), xp.mean((db - a) ** 2 / den),
-            xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
-
-
-def blend_from_moments(m, na: int, nb: int):
-    """(plain, blend, alpha) from blend_moments() values."""
-    s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
-    n = na + nb
-    v_p = s_ab * na * nb / (n * n)                     # Var(P)
-    var_a, var_b = s_ab * nb / n, s_ab * na / n         # Var(A), Var(B)
-    e_a = s_dab - var_b                                 # error of D(A)
-    e_b = s_dba - var_a                                 # error of D(B)
-    tau2 = s_dd * na * nb / n                           # residual noise x samples
-    kap = s_ddab * na * nb / n                          # covariance with the plain noise x samples
-    bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
-    v_eta, c = tau2 / n, kap / n
-    e_d = bias2 + v_eta
-    q = e_d + v_p - 2.0 * c
-    alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
-    blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
-    return v_p, max(blend, 0.0), alpha
-
-
-def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
-    """Predicted relMSE of the plain mean P and of the best blend
-    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
-    the full mean p and the denoised half means da, db.  Returns
-    (plain, blend, alpha)."""
-    return blend_from_moments(blend_moments(a, b, p, da, db, xp), na, nb)
-
-
-class GpuBackend:
-    """Device accumulation buffers (torch) and one vr_batch for every pass;
-    with a denoiser, jobs that ask for it also get AOV buffers and blended
-    outputs (the module docstring describes the prediction)."""
-
-    def __init__(self, max_wave_paths: int = 0, denoiser=None, denoise_below: float = 16.0):
-        import torch
-
-        from .batch import Batch
-
-        self.torch = torch
-        self.batch = Batch(max_wave_paths)
-        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
-        self.stream = torch.cuda.Stream()
-        self.dn = denoiser
-        # the denoiser prediction runs once the plain estimate is within this
-        # factor of the job's target (it cannot finish a job much earlier)
-        self.denoise_below = denoise_below
-        self.denoise_calls = 0
-
-    def alloc(self, job: JobState):
-        t = self.torch
-        h, w = job.req.height, job.req.width
-        k = 6 if (job.req.denoise and self.dn is not None) else 2
-        # [A, B] radiance sums, then albedo A/B and normal A/B sums
-        return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
-
-    def free(self, job: JobState) -> None:
-        job.bufs = None
-
-    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
-        from dataclasses import replace
-
-        from .batch import RenderJob
-
-        jobs = []
-        for job, b, first, n in work:
-            # buffers accumulate raw sums: total_samples = 1
-            st = replace(job.req.settings, total_samples=1)
-            aov = len(job.bufs) == 6
-            jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
-                                  job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
-                                  job.bufs[4 + b].data_ptr() if aov else 0))
-        self.batch.render(jobs, self.stream.cuda_stream)
-        self.batch.synchronize(self.stream.cuda_stream)
-
-    def _denoise(self, rad, alb, nrm, scale: float):
-        t = self.torch
-        h, w = rad.shape[0], rad.shape[1]
-        out = t.empty((h, w, 4), dtype=t.float32, device="cuda")
-        self.dn.denoise(rad, alb, nrm, scale, out, w, h, stream=self.stream.cuda_stream)
-        self.denoise_calls += 1
-        return out
-
-    def estimate(self, job: JobState) -> float:
-        return self.estimate_many([job])[0]
-
-    def estimate_many(self, jobs: list[JobState]) -> list[float]:
-        """Plain estimates of all jobs; for denoising jobs close enough to
-        their target, the blend prediction, with the denoiser run once over
-        the half-buffers of all of them (batched per image size)."""
-        t = self.torch
-        out, halves = [], []
-        for job in jobs:
-            na, nb = job.n_a, job.n_b
-            a = job.bufs[0][..., :3].double() / max(na, 1)
-            b = job.bufs[1][..., :3].double() / max(nb, 1)
-            plain = _estimate(a, b, na, nb, xp=t)
-            job.plain_estimate, job.alpha = plain, 0.0
-            out.append(plain)
-            if len(job.bufs) == 6 and plain <= self.denoise_below * job.req.target_relmse:
-                halves.append((len(out) - 1, job, a, b))
-        groups = {}
-        for item in halves:
-            groups.setdefault((item[1].req.height, item[1].req.width), []).append(item)
-        for (h, w), items in groups.items():
-            with t.cuda.stream(self.stream):
-                rad = t.stack([x for _, j, *_ in items for x in (j.bufs[0], j.bufs[1])])
-                alb = t.stack([x for _, j, *_ in items for x in (j.bufs[2], j.bufs[3])])
-                nrm = t.stack([x for _, j, *_ in items for x in (j.bufs[4], j.bufs[5])])
-                scales = [s for _, j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
-                den = t.empty_like(rad)
-                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=self.stream.cuda_stream)
-                self.denoise_calls += 1
-            self.stream.synchronize()
-            for k, (i, job, a, b) in enumerate(items):
-                na, nb = job.n_a, job.n_b
-                da = den[2 * k][..., :3].double()
-                db = den[2 * k + 1][..., :3].double()
-                p = (a * na + b * nb) / (na + nb)
-                _, blend, alpha = blend_prediction(a, b, p, da, db, na, nb, xp=t)
-                if blend < out[i]:
-                    job.alpha = alpha
-                    out[i] = blend
-        return out
-
-    def result(self, job: JobState) -> np.ndarray:
         t = self.torch
         t0 = time.perf_counter()
         n = job.n_a + job.n_b
-        p = (job.bufs[0] + job.bufs[1]) / n
-        if job.alpha <= 0.0:
-            out = p[..., :3].cpu().numpy()
-        else:
-            with t.cuda.stream(self.stream):
+        es = self.est_stream
+        with t.cuda.stream(es):
+            p = (job.bufs[0] + job.bufs[1]) / n
+            if job.alpha <= 0.0:
+                y = p[..., :3]
+            else:
                 alb = (job.bufs[2] + job.bufs[3]) / n
                 nrm = (job.bufs[4] + job.bufs[5]) / n
-                d = self._denoise(p, alb, nrm, 1.0)
-                y = job.alpha * d[..., :3] + (1.0 - job.alpha) * p[..., :3]
-            self.stream.synchronize()
-            out = y.cpu().numpy()
+                out = t.empty((job.req.height, job.req.width, 4), dtype=t.float32, device="cuda")
+                self.dn.denoise(p, alb, nrm, 1.0, out, job.req.width, job.req.height, stream=es.cuda_stream)
+                self.denoise_calls += 1
+                y = job.alpha * out[..., :3] + (1.0 - job.alpha) * p[..., :3]
+        es.synchronize()
+        out = y.cpu().numpy()
         self.time["result"] += time.perf_counter() - t0
         return out
 
@@ -483,6 +441,7 @@ class Server:
         self.resident_scenes: dict[int, int] = {}  # id(scene) -> active users
         self.used = 0
         self.passes = 0
+        self.pending: list = []   # pipelined: (estimate handle, jobs) in issue order
 
     # -- requests --------------------------------------------------------
     def submit(self, req: JobRequest, arrival: Optional[float] = None) -> int:
@@ -553,6 +512,8 @@ class Server:
         budget = self.cfg.pass_paths
         for jid in self.active:
             job = self.jobs[jid]
+            if job.pending:
+                continue  # waits for its estimate
             want = job.next_spp or self.cfg.first_pass_spp
             want = max(1, min(want, job.req.max_samples - job.samples))
             paths = want * job.req.width * job.req.height
@@ -573,10 +534,77 @@ class Server:
         more = max(self.cfg.min_pass_spp, more + (more & 1))
         return min(more, job.req.max_samples - job.samples)
 
+    def _finish_or_plan(self, job: JobState) -> bool:
+        """After an estimate: retire the job (True) or plan its next pass."""
+        if job.estimate <= job.req.target_relmse or job.samples >= job.req.max_samples:
+            job.result = self.backend.result(job)
+            job.state, job.finished = "done", self.clock()
+            self._release(job)
+            self.active.remove(job.job_id)
+            return True
+        if self.cfg.adaptive:
+            job.next_spp = self._next_spp(job)
+        return False
+
+    def _harvest(self, block: bool) -> None:
+        """Collects finished estimates in order (waits for the oldest if block)."""
+        while self.pending:
+            handle, jobs = self.pending[0]
+            ests = self.backend.poll(handle, block=block)
+            if ests is None:
+                return
+            self.pending.pop(0)
+            block = False
+            for job, e in zip(jobs, ests):
+                job.estimate, job.pending = e, False
+                self._finish_or_plan(job)
+
+    def _step_pipelined(self) -> int:
+        self._admit()
+        self._harvest(block=False)
+        while True:
+            work = self._plan()
+            if work:
+                break
+            if not self.pending:
+                return 0
+            self._harvest(block=True)
+            self._admit()
+        try:
+            ev = self.backend.render_async(work)
+        except Exception as e:
+            for job in {id(w[0]): w[0] for w in work}.values():
+                job.state, job.error, job.finished = "failed", str(e), self.clock()
+                self._release(job)
+                self.active.remove(job.job_id)
+            return 0
+        self.passes += 1
+        rendered = {}
+        for job, b, first, n in work:
+            job.samples += n
+            if b == 0:
+                job.n_a += n
+            else:
+                job.n_b += n
+            rendered[job.job_id] = job
+        check = []
+        for job in rendered.values():
+            job.passes += 1
+            if job.n_a and job.n_b and job.samples >= self.cfg.min_samples:
+                job.pending = True
+                check.append(job)
+            else:
+                job.next_spp = self._next_spp(job)
+        if check:
+            self.pending.append((self.backend.estimate_async(check, ev), check))
+        return len(rendered)
+
     def step(self) -> int:
         """Admits what fits, renders one pass (every active job, or with
         adaptive allocation the jobs the pass has room for), estimates, retires
         finished jobs.  Returns the number of jobs rendered."""
+        if self.cfg.pipelined and self.cfg.adaptive and hasattr(self.backend, "render_async"):
+            return self._step_pipelined()
         self._admit()
         if not self.active:
             return 0
@@ -645,6 +673,8 @@ class Server:
             self.step()
             if not until_idle and i >= len(pending):
                 break
+        if hasattr(self.backend, "finish"):
+            self.backend.finish()
 
     def latencies(self, state: str = "done") -> np.ndarray:
         return np.array([j.latency for j in self.jobs.values() if j.state == state and j.latency is not None])
