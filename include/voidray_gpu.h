@@ -291,8 +291,10 @@ vr_status vr_tuning_set(const vr_tuning* tuning);
  * extend / shade / shadow, accumulate) is captured once as a CUDA graph and
  * replayed on later calls with the same job-set shape (job count, paths,
  * depth); the per-call data (sample offsets, seeds, scenes) is read from the
- * device job table, so results are identical to direct launches.  Needs a
- * non-NULL stream; off by default.  No counterpart in the reference. */
+ * device job table, so results are identical to direct launches.  A shape
+ * is captured the second time it shows up (shapes that never repeat run
+ * directly).  Needs a non-NULL stream; off by default.  No counterpart in the
+ * reference. */
 vr_status vr_batch_set_graphs(vr_batch* batch, int32_t enable);
 vr_status vr_batch_graph_stats(vr_batch* batch, uint64_t* captures, uint64_t* replays);
 

@@ -110,8 +110,8 @@ def test_graph_replays_equal_direct_launches(gpu, max_wave):
             batch.synchronize(stream.cuda_stream)
         results[graphs] = [o.cpu().numpy() for o in outs]
         caps, reps = batch.graph_stats()
-        if graphs:
-            assert caps >= 1 and reps >= caps * (passes - 1)
+        if graphs:  # pass 1 runs directly, pass 2 captures, passes 3.. replay
+            assert caps >= 1 and reps >= caps * (passes - 2)
         else:
             assert caps == 0 and reps == 0
         batch.destroy()

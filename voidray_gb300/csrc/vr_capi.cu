@@ -194,12 +194,23 @@ struct GraphCache {
         uint64_t used;
     };
     std::vector<Entry> entries;
+    std::vector<GraphKey> seen;  // shapes launched once without a graph (capture on the second sight)
     uint64_t tick = 0, captures = 0, replays = 0;
     bool broken = false;  // capture failed once: launch directly from then on
 
     void clear() {
         for (Entry& e : entries) cudaGraphExecDestroy(e.exec);
         entries.clear();
+        seen.clear();
+    }
+    // true the first time a shape shows up (it then runs without a graph:
+    // shapes that never repeat, like adaptive passes, cost no capture)
+    bool first_sight(const GraphKey& k) {
+        for (const GraphKey& s : seen)
+            if (std::memcmp(&s, &k, sizeof k) == 0) return false;
+        if (seen.size() >= 64) seen.erase(seen.begin());
+        seen.push_back(k);
+        return true;
     }
     cudaGraphExec_t find(const GraphKey& k) {
         for (Entry& e : entries)
@@ -425,7 +436,8 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
                 key.cap = ps.cap;
                 key.tuning_generation = vr::get_tuning().generation;
                 cudaGraphExec_t ex = graphs->find(key);
-                if (!ex) {
+                const bool capture = !ex && !graphs->first_sight(key);
+                if (capture) {
                     VR_CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
                     const vr_status sr = stages();
                     cudaGraph_t g = nullptr;
@@ -442,7 +454,7 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
                         graphs->insert(key, ex);
                         graphs->captures++;
                     }
-                } else {
+                } else if (ex) {
                     graphs->replays++;
                 }
                 if (ex) {

@@ -232,7 +232,8 @@ class GpuBackend:
         self.batch = Batch(max_wave_paths)
         self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
         self.stream = torch.cuda.Stream()      # renders
-        self.est_stream = torch.cuda.Stream()  # estimates and results (pipelined mode)
+        self.est_stream = torch.cuda.Stream()  # estimates (pipelined mode)
+        self.res_stream = torch.cuda.Stream()  # final images: never queued behind later estimates
         self.dn = denoiser
         # the denoiser prediction runs once the plain estimate is within this
         # factor of the job's target (it cannot finish a job much earlier)
@@ -334,6 +335,7 @@ class GpuBackend:
     def finish(self) -> None:
         """Waits for both streams and reports kernel-side errors of the passes."""
         self.est_stream.synchronize()
+        self.res_stream.synchronize()
         self.batch.synchronize(self.stream.cuda_stream)
 
     def _enqueue(self, work: list[tuple[JobState, int, int, int]]) -> None:
@@ -411,7 +413,7 @@ class GpuBackend:
         t = self.torch
         t0 = time.perf_counter()
         n = job.n_a + job.n_b
-        es = self.est_stream
+        es = self.res_stream
         with t.cuda.stream(es):
             p = (job.bufs[0] + job.bufs[1]) / n
             if job.alpha <= 0.0:
@@ -562,6 +564,11 @@ class Server:
     def _step_pipelined(self) -> int:
         self._admit()
         self._harvest(block=False)
+        # at most two passes in flight: a deeper queue would put later jobs'
+        # passes ahead of the next pass of the jobs waiting for their estimates
+        while len(self.pending) >= 2:
+            self._harvest(block=True)
+            self._admit()
         while True:
             work = self._plan()
             if work:
