@@ -77,7 +77,10 @@ vr_status vr_denoiser_set_params(vr_denoiser* net, const float* host, uint64_t c
  * width x height holding per-pixel sums, multiplied by `scale` (1/samples for
  * raw sums, 1 for means) before use.  Writes the denoised radiance (alpha 1)
  * to out_rgba (device, width x height x 4; may not alias the inputs).  Any
- * width and height: the network runs on the image padded to multiples of 8. */
+ * width and height: the network runs on the image padded to multiples of 8.
+ * A handle owns one activation workspace (kept and reused by every call that
+ * fits in it): calls on one handle from different streams must be ordered by
+ * the caller; use one handle per stream for concurrent work. */
 vr_status vr_denoise_device(vr_denoiser* net, const float* rgba, const float* albedo, const float* normal,
                             float scale, float* out_rgba, uint32_t width, uint32_t height, void* stream);
 

@@ -105,7 +105,8 @@ struct vr_denoiser {
     float* loss = nullptr; // device scalar
     uint64_t steps = 0;
     // workspace for (n, h, w)
-    int wn = 0, wh = 0, ww = 0;
+    int wn = 0, wh = 0, ww = 0;  // dimensions of the current call
+    size_t cap_px = 0;           // pixels the workspace holds (reused by any call that fits)
     std::vector<void*> ws;
     uint64_t ws_bytes = 0;
     bf16* act[NACT] = {};
@@ -137,6 +138,7 @@ void free_ws(vr_denoiser* d) {
     d->dpool = nullptr;
     d->up_tmp = nullptr;
     d->wn = d->wh = d->ww = 0;
+    d->cap_px = 0;
     d->train_ws = false;
 }
 
@@ -151,12 +153,25 @@ vr_status ws_alloc(vr_denoiser* d, T** out, size_t count) {
     return VR_OK;
 }
 
-// activations for an n x h x w batch (h, w multiples of 8); gradients too when train
+// activations for an n x h x w batch (h, w multiples of 8); gradients too
+// when train.  Every buffer scales with the pixel count, so a workspace
+// allocated for P pixels serves any later call of at most P pixels without
+// reallocating (a reallocation frees memory, which synchronises the device).
+// The workspace belongs to the handle: calls on one handle from different
+// streams must be ordered by the caller.
 vr_status ensure_ws(vr_denoiser* d, int n, int h, int w, bool train) {
-    if (d->wn == n && d->wh == h && d->ww == w && (d->train_ws || !train)) return VR_OK;
+    const size_t need = (size_t)n * h * w;
+    if (need <= d->cap_px && (d->train_ws || !train)) {
+        d->wn = n;
+        d->wh = h;
+        d->ww = w;
+        return VR_OK;
+    }
+    const bool was_train = d->train_ws;
+    const size_t P = std::max(need, d->cap_px);
     free_ws(d);
+    train = train || was_train;
     vr_status r;
-    const size_t P = (size_t)n * h * w;
     for (int a = 0; a < NACT; ++a)
         if ((r = ws_alloc(d, &d->act[a], (P >> (2 * ACTS[a].lvl)) * ACTS[a].c)) != VR_OK) return free_ws(d), r;
     if ((r = ws_alloc(d, &d->out, P * OUT_C)) != VR_OK) return free_ws(d), r;
@@ -184,6 +199,7 @@ vr_status ensure_ws(vr_denoiser* d, int n, int h, int w, bool train) {
     d->wn = n;
     d->wh = h;
     d->ww = w;
+    d->cap_px = P;
     d->train_ws = train;
     return VR_OK;
 }
@@ -481,10 +497,8 @@ vr_status denoise_impl(vr_denoiser* d, const float* rgba, const float* albedo, c
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int h = (int)((height + 7) & ~7u), w = (int)((width + 7) & ~7u), n = (int)batch;
     vr_status r;
-    if (!(d->wn == n && d->wh == h && d->ww == w)) {
-        DN_CK(cudaStreamSynchronize(st));
-        if ((r = ensure_ws(d, n, h, w, false)) != VR_OK) return r;
-    }
+    if ((size_t)n * h * w > d->cap_px) DN_CK(cudaStreamSynchronize(st));
+    if ((r = ensure_ws(d, n, h, w, false)) != VR_OK) return r;
     const float* scales = nullptr;
     if (scales_host) {
         if (d->scales_cap < batch) {
@@ -546,8 +560,7 @@ vr_status vr_denoiser_train_step_device(vr_denoiser* d, const float* rgba, const
     if (!d) return vr::set_error(VR_ERR_INVALID, "null denoiser");
     if (!(lr >= 0.0f) || !std::isfinite(lr)) return vr::set_error(VR_ERR_INVALID, "bad learning rate");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (!(d->wn == (int)batch && d->wh == (int)height && d->ww == (int)width && d->train_ws))
-        DN_CK(cudaStreamSynchronize(st));
+    if ((size_t)batch * width * height > d->cap_px || !d->train_ws) DN_CK(cudaStreamSynchronize(st));
     vr_status r = loss_and_grads(d, rgba, albedo, normal, target, scale_in, scale_target, batch, width, height, st);
     if (r != VR_OK) return r;
     if ((r = read_loss(d, batch, width, height, loss_host, st)) != VR_OK) return r;

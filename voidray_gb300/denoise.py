@@ -60,8 +60,16 @@ class Denoiser:
         h = C.c_void_p()
         check(lib().vr_denoiser_create(int(seed), C.byref(h)))
         self._h = h
+        self.backend = 0
         if params is not None:
             self.set_params(params)
+
+    def clone(self) -> "Denoiser":
+        """A second handle with the same weights and backend (its own
+        workspace, for use on another stream)."""
+        d = Denoiser(params=self.params())
+        d.set_backend(self.backend)
+        return d
 
     @classmethod
     def pretrained(cls, path: Path | str = WEIGHTS) -> "Denoiser":
@@ -88,6 +96,7 @@ class Denoiser:
     def set_backend(self, backend: int) -> None:
         """Forward convolutions on mma.sync (0) or tcgen05 + TMEM + TMA (1)."""
         check(lib().vr_denoiser_set_backend(self.handle, int(backend)))
+        self.backend = int(backend)
 
     def status(self) -> int:
         """Synchronises; raises VoidrayError if a tcgen05 kernel gave up a bounded wait."""

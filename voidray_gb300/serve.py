@@ -235,6 +235,211 @@ class GpuBackend:
         self.est_stream = torch.cuda.Stream()  # estimates (pipelined mode)
         self.res_stream = torch.cuda.Stream()  # final images: never queued behind later estimates
         self.dn = denoiser
+        # final images run on their own stream, so they get their own handle
+        # (a handle's workspace must not be shared by concurrent streams)
+        self.dn_result = denoiser.clone() if denoiser is not None else None
+        # the denoiser prediction runs once the plain estimate is within this
+        # factor of the job's target (it cannot finish a job much earlier)
+        self.denoise_below = denoise_below
+        self.denoise_calls = 0
+        self.time = {"render": 0.0, "estimate": 0.0, "result": 0.0}  # host wall seconds per phase
+
+    def alloc(self, job: JobState):
+        t = self.torch
+        h, w = job.req.height, job.req.width
+        k = 6 if (job.req.denoise and self.dn is not None) else 2
+        # [A, B] radiance sums, then albedo A/B and normal A/B sums; zeroed on
+        # the render stream so the first pass is ordered after the fill
+        with t.cuda.stream(self.stream):
+            return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
+
+    def free(self, job: JobState) -> None:
+        job.bufs = None
+
+    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        t0 = time.perf_counter()
+        self._enqueue(work)
+        self.batch.synchronize(self.stream.cuda_stream)
+        self.time["render"] += time.perf_counter() - t0
+
+    def render_async(self, work):
+        """Enqueues the pass; returns an event recorded after it on the render stream."""
+        t0 = time.perf_counter()
+        self._enqueue(work)
+        ev = self.torch.cuda.Event()
+        ev.record(self.stream)
+        self.time["render"] += time.perf_counter() - t0
+        return ev
+
+    def estimate_async(self, jobs: list[JobState], after):
+        """Enqueues every job's plain moments and (denoising jobs) the batched
+        denoiser and blend moments on the estimate stream, after event `after`;
+        the values land in pinned host memory.  poll() turns them into estimates."""
+        t = self.torch
+        t0 = time.perf_counter()
+        es = self.est_stream
+        with t.cuda.stream(es):
+            if after is not None:
+                es.wait_event(after)
+            vals, halves = [], []
+            for job in jobs:
+                na, nb = job.n_a, job.n_b
+                a = job.bufs[0][..., :3].double() / na
+                b = job.bufs[1][..., :3].double() / nb
+                n = na + nb
+                m = (a * na + b * nb) / n
+                vals.append(t.mean((a - b) ** 2 * (na * nb / (n * n)) / (m * m + EPS_REL)))
+                halves.append((job, a, b, m))
+            dn = [h for h in halves if len(h[0].bufs) == 6]
+            groups = {}
+            for item in dn:
+                groups.setdefault((item[0].req.height, item[0].req.width), []).append(item)
+            order = []
+            for (h, w), items in groups.items():
+                rad = t.stack([x for j, *_ in items for x in (j.bufs[0], j.bufs[1])])
+                alb = t.stack([x for j, *_ in items for x in (j.bufs[2], j.bufs[3])])
+                nrm = t.stack([x for j, *_ in items for x in (j.bufs[4], j.bufs[5])])
+                scales = [s for j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
+                den = t.empty_like(rad)
+                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=es.cuda_stream)
+                self.denoise_calls += 1
+                for k, (job, a, b, m) in enumerate(items):
+                    vals += blend_moments(a, b, m, den[2 * k][..., :3].double(), den[2 * k + 1][..., :3].double(), t)
+                    order.append(job)
+            stacked = t.stack(vals)
+            host = t.empty(stacked.shape, dtype=stacked.dtype, pin_memory=True)
+            host.copy_(stacked, non_blocking=True)
+            done = t.cuda.Event()
+            done.record(es)
+        self.time["estimate"] += time.perf_counter() - t0
+        return (done, host, list(jobs), order)
+
+    def poll(self, handle, block: bool = False):
+        done, host, jobs, order = handle
+        if not block and not done.query():
+            return None
+        t0 = time.perf_counter()
+        done.synchronize()
+        v = host.tolist()
+        out = v[:len(jobs)]
+        for job, e in zip(jobs, out):
+            job.plain_estimate, job.alpha = e, 0.0
+        pos = {id(j): i for i, j in enumerate(jobs)}
+        for k, job in enumerate(order):
+            base = len(jobs) + 5 * k
+            _, blend, alpha = blend_from_moments(v[base:base + 5], job.n_a, job.n_b)
+            i = pos[id(job)]
+            if blend < out[i]:
+                job.alpha = alpha
+                out[i] = blend
+        self.time["estimate"] += time.perf_counter() - t0
+        return out
+
+    def finish(self) -> None:
+        """Waits for both streams and reports kernel-side errors of the passes."""
+        self.est_stream.synchronize()
+        self.res_stream.synchronize()
+        self.batch.synchronize(self.stream.cuda_stream)
+
+    def _enqueue(self, work: list[tuple[JobState, int, int, int]]) -> None:
+        from dataclasses import replace
+
+        from .batch import RenderJob
+
+        jobs = []
+        for job, b, first, n in work:
+            # buffers accumulate raw sums: total_samples = 1
+            st = replace(job.req.settings, total_samples=1)
+            aov = len(job.bufs) == 6
+            jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
+                                  job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
+                                  job.bufs[4 + b].data_ptr() if aov else 0))
+        self.batch.render(jobs, self.stream.cuda_stream)
+
+    def estimate(self, job: JobState) -> float:
+        a, b = self.means(job)
+        return _estimate(a, b, job.n_a, job.n_b)
+
+    def result(self, job: JobState) -> np.ndarray:
+        a, b = job.bufs
+        return (a + b) / (job.n_a + job.n_b)
+
+    # asynchronous interface (runs synchronously here; the scheduler logic is the same)
+    def render_async(self, work):
+        self.render(work)
+        return None
+
+    def estimate_async(self, jobs, after):
+        return [self.estimate(j) for j in jobs]
+
+    def poll(self, handle, block: bool = False):
+        return handle
+
+
+def _estimate(a, b, na: int, nb: int, xp=np) -> float:
+    n = na + nb
+    m = (a * na + b * nb) / n
+    var = (a - b) ** 2 * (na * nb) / (n * n)
+    return float(xp.mean(var / (m * m + EPS_REL)))
+
+
+def blend_moments(a, b, p, da, db, xp=np) -> list:
+    """The five pixel means the blend prediction needs (arrays or tensors,
+    not yet converted to floats, so a caller can read many at once)."""
+    den = p * p + EPS_REL
+    ab = a - b
+    dd = da - db
+    return [xp.mean(ab * ab / den), xp.mean((da - b) ** 2 / den), xp.mean((db - a) ** 2 / den),
+            xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
+
+
+def blend_from_moments(m, na: int, nb: int):
+    """(plain, blend, alpha) from blend_moments() values."""
+    s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
+    n = na + nb
+    v_p = s_ab * na * nb / (n * n)                     # Var(P)
+    var_a, var_b = s_ab * nb / n, s_ab * na / n         # Var(A), Var(B)
+    e_a = s_dab - var_b                                 # error of D(A)
+    e_b = s_dba - var_a                                 # error of D(B)
+    tau2 = s_dd * na * nb / n                           # residual noise x samples
+    kap = s_ddab * na * nb / n                          # covariance with the plain noise x samples
+    bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
+    v_eta, c = tau2 / n, kap / n
+    e_d = bias2 + v_eta
+    q = e_d + v_p - 2.0 * c
+    alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
+    blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
+    return v_p, max(blend, 0.0), alpha
+
+
+def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
+    """Predicted relMSE of the plain mean P and of the best blend
+    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
+    the full mean p and the denoised half means da, db.  Returns
+    (plain, blend, alpha)."""
+    return blend_from_moments(blend_moments(a, b, p, da, db, xp), na, nb)
+
+
+class GpuBackend:
+    """Device accumulation buffers (torch) and one vr_batch for every pass;
+    with a denoiser, jobs that ask for it also get AOV buffers and blended
+    outputs (the module docstring describes the prediction)."""
+
+    def __init__(self, max_wave_paths: int = 0, denoiser=None, denoise_below: float = 16.0):
+        import torch
+
+        from .batch import Batch
+
+        self.torch = torch
+        self.batch = Batch(max_wave_paths)
+        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
+        self.stream = torch.cuda.Stream()      # renders
+        self.est_stream = torch.cuda.Stream()  # estimates (pipelined mode)
+        self.res_stream = torch.cuda.Stream()  # final images: never queued behind later estimates
+        self.dn = denoiser
+        # final images run on their own stream, so they get their own handle
+        # (a handle's workspace must not be shared by concurrent streams)
+        self.dn_result = denoiser.clone() if denoiser is not None else None
         # the denoiser prediction runs once the plain estimate is within this
         # factor of the job's target (it cannot finish a job much earlier)
         self.denoise_below = denoise_below
@@ -422,7 +627,8 @@ class GpuBackend:
                 alb = (job.bufs[2] + job.bufs[3]) / n
                 nrm = (job.bufs[4] + job.bufs[5]) / n
                 out = t.empty((job.req.height, job.req.width, 4), dtype=t.float32, device="cuda")
-                self.dn.denoise(p, alb, nrm, 1.0, out, job.req.width, job.req.height, stream=es.cuda_stream)
+                self.dn_result.denoise(p, alb, nrm, 1.0, out, job.req.width, job.req.height,
+                                       stream=es.cuda_stream)
                 self.denoise_calls += 1
                 y = job.alpha * out[..., :3] + (1.0 - job.alpha) * p[..., :3]
         es.synchronize()
