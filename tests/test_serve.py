@@ -284,3 +284,23 @@ def test_pipelined_renders_while_estimates_are_in_flight():
     seen = [set(j for j, *_ in call) for call in be.calls]
     assert len(seen) >= 3 and any(len(a - b) > 0 for a, b in zip(seen, seen[1:]))
     assert all(s.status(i).state == "done" for i in ids)
+
+
+def test_blend_samples_needed_is_consistent():
+    """The planned sample count brings the predicted error to the target:
+    scaling the noise moments by n / n' at the returned n' lands on it."""
+    from voidray_gb300.serve import blend_from_moments, blend_samples_needed
+
+    yy, xx = np.mgrid[0:64, 0:64] / 64.0
+    truth = np.stack([0.2 + 0.6 * (xx > 0.5), 0.5 + 0.3 * np.sin(6 * xx), 0.3 + 0.0 * yy], -1)
+    a, b, p = _halves(truth, 0.8 * (0.3 + truth), 32, 32, 0)
+    from voidray_gb300.serve import blend_moments
+
+    m = [float(x) for x in blend_moments(a, b, p, _box(a), _box(b))]
+    plain, blend, _ = blend_from_moments(m, 32, 32)
+    target = 0.5 * min(plain, blend)
+    n2 = blend_samples_needed(m, 32, 32, target)
+    assert n2 > 64
+    # plain alone would need 64 * plain / target samples; the blend needs fewer
+    assert n2 <= int(np.ceil(64 * plain / target)) + 1
+    assert blend_samples_needed(m, 32, 32, 10.0) == 64

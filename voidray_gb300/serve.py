@@ -87,6 +87,7 @@ class JobState:
     plain_estimate: float = float("inf")
     next_spp: int = 0          # adaptive: samples of the job's next pass (0: first pass)
     pending: bool = False      # pipelined: an estimate is in flight
+    need_spp: int = 0          # samples the last estimate predicts the job needs (0: assume error ~ 1/n)
 
     @property
     def latency(self) -> Optional[float]:
@@ -119,6 +120,7 @@ class ServerConfig:
     # poll): a job's error estimate runs on the device while the next pass
     # renders the jobs whose next pass size is already known
     pipelined: bool = False
+    max_inflight: int = 2      # pipelined: passes whose estimates may be outstanding
 
 
 class FakeBackend:
@@ -191,23 +193,62 @@ def blend_moments(a, b, p, da, db, xp=np) -> list:
             xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
 
 
-def blend_from_moments(m, na: int, nb: int):
-    """(plain, blend, alpha) from blend_moments() values."""
+def _blend_terms(m, na: int, nb: int):
+    """(v_p, bias2, v_eta, c) at n = na + nb samples from blend_moments() values."""
     s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
     n = na + nb
-    v_p = s_ab * na * nb / (n * n)                     # Var(P)
-    var_a, var_b = s_ab * nb / n, s_ab * na / n         # Var(A), Var(B)
-    e_a = s_dab - var_b                                 # error of D(A)
-    e_b = s_dba - var_a                                 # error of D(B)
-    tau2 = s_dd * na * nb / n                           # residual noise x samples
-    kap = s_ddab * na * nb / n                          # covariance with the plain noise x samples
+    v_p = s_ab * na * nb / (n * n)
+    var_a, var_b = s_ab * nb / n, s_ab * na / n
+    e_a = s_dab - var_b
+    e_b = s_dba - var_a
+    tau2 = s_dd * na * nb / n
+    kap = s_ddab * na * nb / n
     bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
-    v_eta, c = tau2 / n, kap / n
+    return v_p, bias2, tau2 / n, kap / n
+
+
+def _best_blend(v_p, bias2, v_eta, c):
     e_d = bias2 + v_eta
     q = e_d + v_p - 2.0 * c
     alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
     blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
-    return v_p, max(blend, 0.0), alpha
+    return max(blend, 0.0), alpha
+
+
+def blend_samples_needed(m, na: int, nb: int, target: float) -> int:
+    """Fewest samples n' >= n at which the predicted error of the best of the
+    plain mean and the blend reaches `target`: the noise terms (plain
+    variance, residual denoiser noise, covariance) scale as n / n', the bias
+    stays."""
+    v_p, bias2, v_eta, c = _blend_terms(m, na, nb)
+    n = na + nb
+
+    def err(k):  # k = n' / n
+        b, _ = _best_blend(v_p / k, bias2, v_eta / k, c / k)
+        return min(b, v_p / k)
+
+    if err(1.0) <= target:
+        return n
+    lo, hi = 1.0, 2.0
+    while err(hi) > target and hi < 1e6:
+        lo, hi = hi, hi * 2.0
+    for _ in range(30):
+        mid = 0.5 * (lo + hi)
+        if err(mid) > target:
+            lo = mid
+        else:
+            hi = mid
+    return int(math.ceil(n * hi))
+
+
+def blend_from_moments(m, na: int, nb: int):
+    """(plain, blend, alpha) from blend_moments() values."""
+    # Var(P) from the halves; D(A)'s error is E|D(A)-B|^2 - Var(B); the
+    # residual denoiser noise x samples (tau2) from E|D(A)-D(B)|^2; its
+    # covariance with the plain noise x samples from E[(D(A)-D(B))(A-B)]
+    v_p, bias2, v_eta, c = _blend_terms(m, na, nb)
+    blend, alpha = _best_blend(v_p, bias2, v_eta, c)
+    return v_p, blend, alpha
 
 
 def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
@@ -323,11 +364,13 @@ class GpuBackend:
         v = host.tolist()
         out = v[:len(jobs)]
         for job, e in zip(jobs, out):
-            job.plain_estimate, job.alpha = e, 0.0
+            job.plain_estimate, job.alpha, job.need_spp = e, 0.0, 0
         pos = {id(j): i for i, j in enumerate(jobs)}
         for k, job in enumerate(order):
             base = len(jobs) + 5 * k
-            _, blend, alpha = blend_from_moments(v[base:base + 5], job.n_a, job.n_b)
+            mom = v[base:base + 5]
+            _, blend, alpha = blend_from_moments(mom, job.n_a, job.n_b)
+            job.need_spp = blend_samples_needed(mom, job.n_a, job.n_b, job.req.target_relmse)
             i = pos[id(job)]
             if blend < out[i]:
                 job.alpha = alpha
@@ -587,7 +630,7 @@ class GpuBackend:
             halves.append((job, a, b, m))
         out = [float(x) for x in t.stack(plain_m).cpu()]
         for job, e in zip(jobs, out):
-            job.plain_estimate, job.alpha = e, 0.0
+            job.plain_estimate, job.alpha, job.need_spp = e, 0.0, 0
         cand = [(i, *h) for i, h in enumerate(halves)
                 if len(h[0].bufs) == 6 and out[i] <= self.denoise_below * h[0].req.target_relmse]
         groups = {}
@@ -608,6 +651,7 @@ class GpuBackend:
                 vals = [float(x) for x in t.stack(mom).cpu()]
             for k, (i, job, a, b, m) in enumerate(items):
                 _, blend, alpha = blend_from_moments(vals[5 * k:5 * k + 5], job.n_a, job.n_b)
+                job.need_spp = blend_samples_needed(vals[5 * k:5 * k + 5], job.n_a, job.n_b, job.req.target_relmse)
                 if blend < out[i]:
                     job.alpha = alpha
                     out[i] = blend
@@ -737,7 +781,7 @@ class Server:
     def _next_spp(self, job: JobState) -> int:
         if not math.isfinite(job.estimate):
             return self.cfg.first_pass_spp
-        need = job.samples * job.estimate / job.req.target_relmse
+        need = job.need_spp or job.samples * job.estimate / job.req.target_relmse
         more = int(math.ceil(self.cfg.overshoot * max(0.0, need - job.samples)))
         more = max(self.cfg.min_pass_spp, more + (more & 1))
         return min(more, job.req.max_samples - job.samples)
@@ -770,9 +814,9 @@ class Server:
     def _step_pipelined(self) -> int:
         self._admit()
         self._harvest(block=False)
-        # at most two passes in flight: a deeper queue would put later jobs'
-        # passes ahead of the next pass of the jobs waiting for their estimates
-        while len(self.pending) >= 2:
+        # a bounded number of passes in flight: a deeper queue would put later
+        # jobs' passes ahead of the next pass of the jobs waiting for estimates
+        while len(self.pending) >= self.cfg.max_inflight:
             self._harvest(block=True)
             self._admit()
         while True:
