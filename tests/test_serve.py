@@ -304,3 +304,32 @@ def test_blend_samples_needed_is_consistent():
     # plain alone would need 64 * plain / target samples; the blend needs fewer
     assert n2 <= int(np.ceil(64 * plain / target)) + 1
     assert blend_samples_needed(m, 32, 32, 10.0) == 64
+
+
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_srpt_order_keeps_results_mix_independent(pipelined):
+    cfg = ServerConfig(adaptive=True, pipelined=pipelined, order="srpt", pass_paths=4 * 64 * 64, first_pass_spp=64,
+                       min_samples=64, max_active=64)
+
+    def run(mix):
+        s = Server(LaggingBackend(noise=0.3), cfg, clock=Clock())
+        for k in range(mix):
+            s.submit(req(seed=100 + k, target=5e-4 if k % 2 else 2e-3, max_samples=4096))
+        jid = s.submit(req(seed=7, target=1e-3, max_samples=4096))
+        while not s.idle():
+            s.step()
+        j = s.status(jid)
+        return j.result, j.samples
+
+    r0, r1 = run(0), run(7)
+    assert r0[1] == r1[1] and np.array_equal(r0[0], r1[0])
+
+
+def test_srpt_finishes_short_jobs_first():
+    cfg = ServerConfig(adaptive=True, order="srpt", pass_paths=64 * 64, first_pass_spp=64, min_samples=64)
+    s = Server(FakeBackend(noise=0.3), cfg, clock=Clock())
+    long_ = s.submit(req(seed=1, target=2e-4, max_samples=100000))
+    short = s.submit(req(seed=2, target=2e-3, max_samples=100000))
+    while not s.idle():
+        s.step()
+    assert s.status(short).finished < s.status(long_).finished

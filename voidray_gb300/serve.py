@@ -121,6 +121,11 @@ class ServerConfig:
     # renders the jobs whose next pass size is already known
     pipelined: bool = False
     max_inflight: int = 2      # pipelined: passes whose estimates may be outstanding
+    # adaptive: order in which jobs take a pass: "fifo" (admission order) or
+    # "srpt" (shortest predicted remaining work first: paths the job still
+    # needs by its last estimate; jobs before their first estimate count
+    # their first pass).  Either way a job's pass sizes are its own.
+    order: str = "fifo"
 
 
 class FakeBackend:
@@ -762,7 +767,13 @@ class Server:
                 work.append((job, job.passes % 2, job.samples, n))
             return work
         budget = self.cfg.pass_paths
-        for jid in self.active:
+        ids = self.active
+        if self.cfg.order == "srpt":
+            def remaining(jid):
+                j = self.jobs[jid]
+                return (j.next_spp or self.cfg.first_pass_spp) * j.req.width * j.req.height
+            ids = sorted(self.active, key=lambda jid: (remaining(jid), jid))
+        for jid in ids:
             job = self.jobs[jid]
             if job.pending:
                 continue  # waits for its estimate
