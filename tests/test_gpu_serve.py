@@ -64,7 +64,7 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
     net = Denoiser.pretrained()
 
     def run(mix):
-        backend = GpuBackend(denoiser=net, denoise_below=1e9)
+        backend = GpuBackend(denoiser=net)
         srv = Server(backend, cfg)
         acc, st = scenes[1]
         jid = srv.submit(JobRequest(acc, st, 40, 32, max_samples=128, target_relmse=2e-2, seed=5, denoise=True))
@@ -77,7 +77,7 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
         backend.finish()
         j = srv.status(jid)
         assert backend.denoise_calls > 0
-        return j.result, j.samples, j.alpha, j.estimate
+        return j.result, j.samples, np.asarray(j.alpha).tolist(), j.estimate
 
     try:
         r0 = run(0)
