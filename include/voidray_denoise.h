@@ -15,8 +15,9 @@
  * divided by (albedo + 0.01), the albedo, the normal.  The network predicts
  * the log1p of the demodulated radiance; the output is multiplied back by
  * (albedo + 0.01).  Loss (vr_denoiser_set_loss): the mean absolute error of
- * that prediction, or the relative MSE (y - t)^2 / (t^2 + 0.01) of the
- * remodulated radiance y against the target t.
+ * that prediction, or the relative MSE (y - t)^2 / (y^2 + 0.01) of the
+ * remodulated radiance y against the target t, the denominator held constant
+ * (the form suited to noisy rendered targets).
  *
  * Shares vr_status and vr_last_error() with voidray_gpu.h.
  */

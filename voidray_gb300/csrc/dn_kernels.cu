@@ -516,9 +516,11 @@ __global__ void k_postprocess(const float* __restrict__ out, int cout, const flo
 }
 
 // kind LOSS_L1_LOG: |o - log1p(t / (albedo + eps))|, gradient sign(d) / count.
-// kind LOSS_RELMSE: (y - t)^2 / (t^2 + 0.01) with y = expm1(min(o, 20)) *
-// (albedo + eps), the metric the renders are judged by; gradient
-// 2 (y - t) / (t^2 + 0.01) * (albedo + eps) * exp(o) / count.
+// kind LOSS_RELMSE: (y - t)^2 / (max(y, 0)^2 + 0.01) with y = expm1(min(o, 20))
+// * (albedo + eps), the relative error the renders are judged by, normalised
+// by the prediction held constant (the target is itself a noisy render, and a
+// noisy denominator would bias the fit); gradient
+// 2 (y - t) / (max(y, 0)^2 + 0.01) * (albedo + eps) * exp(o) / count.
 __global__ void k_loss(const float* __restrict__ out, int cout, const float4* __restrict__ tgt,
                        const float4* __restrict__ alb, float st, float sa, size_t total, float inv_count, int kind,
                        bf16* __restrict__ grad, float* __restrict__ loss) {
@@ -539,7 +541,8 @@ __global__ void k_loss(const float* __restrict__ out, int cout, const float4* __
                     // produces; the cap keeps the square and gradient finite
                     const float e = expf(fminf(o[c], 20.0f));
                     const float y = (e - 1.0f) * ae;
-                    const float den = 1.0f / (tc * tc + 0.01f);
+                    const float yp = fmaxf(y, 0.0f);
+                    const float den = 1.0f / (yp * yp + 0.01f);
                     const float r = y - tc;
                     s += r * r * den;
                     gv = o[c] < 20.0f ? 2.0f * r * den * ae * e * inv_count : 0.0f;
