@@ -61,8 +61,9 @@ vr_status vr_denoiser_layer_get(uint32_t index, vr_denoiser_layer* layer);
 #define VR_DN_LOSS_L1_LOG 0
 #define VR_DN_LOSS_RELMSE 1
 vr_status vr_denoiser_set_loss(vr_denoiser* net, int32_t kind);
-/* Forward convolutions on mma.sync (default) or on tcgen05 + TMEM with TMA
- * operand staging.  The backward pass always runs on mma.sync. */
+/* Convolutions on mma.sync (default) or on tcgen05 + TMEM with TMA operand
+ * staging (forward and backward-data; the weight gradient stays on
+ * mma.sync). */
 #define VR_DN_BACKEND_MMA_SYNC 0
 #define VR_DN_BACKEND_TCGEN05 1
 vr_status vr_denoiser_set_backend(vr_denoiser* net, int32_t backend);
@@ -119,13 +120,13 @@ vr_status vr_dn_conv3x3_device(const uint16_t* src1, uint32_t c1, int32_t up1, c
                                const uint16_t* weight, const float* bias, const uint16_t* mask, uint16_t* out_bf16,
                                float* out_f32, uint32_t cout, uint32_t n, uint32_t h, uint32_t w, int32_t relu,
                                void* stream);
-/* The forward convolution on the tcgen05 tensor cores (no upsample, no
- * mask; Cout 16..256).  status_device (optional) gets bit 1 / 2 when a
- * bounded wait inside the kernel ran out. */
+/* The same convolution on the tcgen05 tensor cores (no upsample; Cout a
+ * multiple of 16, split into tiles of at most 256).  status_device
+ * (optional) gets bit 1 / 2 when a bounded wait inside the kernel ran out. */
 vr_status vr_dn_conv3x3_tc_device(const uint16_t* src1, uint32_t c1, const uint16_t* src2, uint32_t c2,
-                                  const uint16_t* weight, const float* bias, uint16_t* out_bf16, float* out_f32,
-                                  uint32_t cout, uint32_t n, uint32_t h, uint32_t w, int32_t relu,
-                                  uint32_t* status_device, void* stream);
+                                  const uint16_t* weight, const float* bias, const uint16_t* mask,
+                                  uint16_t* out_bf16, float* out_f32, uint32_t cout, uint32_t n, uint32_t h,
+                                  uint32_t w, int32_t relu, uint32_t* status_device, void* stream);
 /* dw[co][tap][ci] += sum over pixels of dz[p][co] * input(p + tap)[ci]. */
 vr_status vr_dn_conv3x3_wgrad_device(const uint16_t* dz, const uint16_t* src1, uint32_t c1, int32_t up1,
                                      const uint16_t* src2, uint32_t c2, float* dw, uint32_t cout, uint32_t n,

@@ -13,7 +13,7 @@ from test_gpu_denoise import batch_arrays, conv_ref, rand_bf16, ulp_bf16
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
-TC_CASES = [  # c1, c2, cout, n, h, w, relu, bias, f32
+TC_CASES = [  # c1, c2, cout, n, h, w, relu, bias, f32 (mask when relu == 2)
     (16, 0, 32, 1, 8, 16, 1, 1, 0),      # one tile, first-layer shape (16-channel chunks)
     (16, 0, 32, 2, 16, 16, 1, 1, 0),
     (32, 0, 64, 1, 24, 40, 1, 1, 0),     # partial tiles at the right edge
@@ -23,6 +23,9 @@ TC_CASES = [  # c1, c2, cout, n, h, w, relu, bias, f32
     (64, 32, 32, 2, 16, 8, 1, 1, 0),     # 64 + 32: 32-channel chunks
     (32, 0, 16, 1, 16, 16, 0, 1, 1),     # output layer, fp32
     (64, 0, 192, 1, 8, 24, 0, 0, 0),
+    (16, 0, 32, 1, 16, 16, 2, 0, 0),     # backward-data shapes: ReLU mask epilogue
+    (128, 0, 384, 1, 8, 8, 2, 0, 0),     # 384 output channels: two 192-channel tiles
+    (32, 0, 96, 2, 8, 16, 2, 0, 0),
 ]
 
 
@@ -35,13 +38,16 @@ def test_conv3x3_tc_matches_fp64(gpu, case):
     wgt = rand_bf16((cout, 9, c1 + c2), rng, scale=np.sqrt(2.0 / (9 * (c1 + c2))))
     b = torch.from_numpy(rng.standard_normal(cout).astype(np.float32) * 0.1) if bias else None
     y, s = conv_ref(x1, x2, 0, wgt, b)
-    if relu:
+    m = rand_bf16((n, h, w, cout), rng) if relu == 2 else None
+    if relu == 1:
         y = np.maximum(y, 0.0)
+    if m is not None:
+        y = np.where(m.float().numpy() > 0, y, 0.0)
     dev = lambda t: None if t is None else t.cuda()
     out = torch.full((n, h, w, cout), 7.0, dtype=torch.float32 if f32 else torch.bfloat16, device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
-    D.conv3x3_tc(dev(x1), c1, dev(wgt), cout, n, h, w, src2=dev(x2), c2=c2, bias=dev(b),
-                 out_bf16=None if f32 else out, out_f32=out if f32 else None, relu=bool(relu), status=status)
+    D.conv3x3_tc(dev(x1), c1, dev(wgt), cout, n, h, w, src2=dev(x2), c2=c2, bias=dev(b), mask=dev(m),
+                 out_bf16=None if f32 else out, out_f32=out if f32 else None, relu=relu == 1, status=status)
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     g = out.double().cpu().numpy()
@@ -52,8 +58,8 @@ def test_conv3x3_tc_matches_fp64(gpu, case):
 
 def test_tc_rejects_what_it_does_not_cover(gpu):
     x = torch.zeros(64 * 128, dtype=torch.bfloat16, device="cuda")
-    with pytest.raises(D.N.VoidrayError) as e:   # Cout 384 > 256
-        D.conv3x3_tc(x, 16, x, 384, 1, 8, 8, out_bf16=x)
+    with pytest.raises(D.N.VoidrayError) as e:   # Cout 24: not a multiple of 16
+        D.conv3x3_tc(x, 16, x, 24, 1, 8, 8, out_bf16=x)
     assert e.value.status == 2
 
 
@@ -79,5 +85,33 @@ def test_network_forward_tc_equals_mma_sync(gpu):
             assert rel < 1e-4, rel
         rel = np.mean((outs[0][..., :3] - outs[1][..., :3]) ** 2 / (outs[0][..., :3] ** 2 + 1e-2))
         assert rel < 1e-4, rel
+    finally:
+        net.destroy()
+
+
+def test_network_gradients_tc_backend_match_fp64(gpu):
+    """Training on the tcgen05 backend (forward and backward-data on tcgen05,
+    weight gradients on mma.sync): same bound as the mma.sync network test."""
+    net = D.Denoiser(seed=11)
+    try:
+        net.set_backend(D.Denoiser.TCGEN05)
+        p = net.params()
+        offs, _ = R.offsets()
+        n, h, w = 1, 16, 16
+        rad, alb, nrm, _ = batch_arrays(n, h, w, 3)
+        tgt = (1e4 * (rad + 0.5)).astype(np.float32)
+        t = [torch.from_numpy(a).cuda() for a in (rad, alb, nrm, tgt)]
+        loss, g = net.gradients(*t, n, w, h)
+        assert net.status() == 0
+        loss_r, g_r, _ = R.loss_and_grads(p, rad, alb, nrm, tgt)
+        assert loss == pytest.approx(loss_r, rel=2e-3)
+        for l, L in enumerate(R.LAYERS):
+            for a, b in [(offs[l][0], offs[l][1]), (offs[l][1], offs[l][1] + L[4])]:
+                ref = g_r[a:b]
+                nr = np.linalg.norm(ref)
+                if nr == 0:
+                    assert np.all(g[a:b] == 0)
+                    continue
+                assert np.linalg.norm(g[a:b] - ref) <= 1e-2 * nr, (l, np.linalg.norm(g[a:b] - ref) / nr)
     finally:
         net.destroy()

@@ -153,7 +153,7 @@ _SIGS = [
     ("vr_denoiser_set_backend", C.c_int, [P, C.c_int32]),
     ("vr_denoiser_status", C.c_int, [P, P]),
     ("vr_dn_conv3x3_tc_device", C.c_int,
-     [P, C.c_uint32, P, C.c_uint32, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, P, P]),
+     [P, C.c_uint32, P, C.c_uint32, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, P, P]),
     ("vr_denoiser_get_params", C.c_int, [P, P, C.c_uint64]),
     ("vr_denoiser_set_params", C.c_int, [P, P, C.c_uint64]),
     ("vr_denoise_device", C.c_int, [P, P, P, P, C.c_float, P, C.c_uint32, C.c_uint32, P]),

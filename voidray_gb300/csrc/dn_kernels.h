@@ -47,8 +47,9 @@ struct WgradArgs {
 
 cudaError_t conv3x3(const ConvArgs& a, cudaStream_t st);
 // The same convolution on the 5th-generation tensor cores (tcgen05.mma,
-// TMEM accumulator, TMA operand staging; dn_tc.cu).  Forward only: no mask,
-// no upsampled source (materialise it with upsample2 first), Cout 16..256.
+// TMEM accumulator, TMA operand staging; dn_tc.cu): forward and
+// backward-data (mask epilogue); no upsampled source (materialise it with
+// upsample2 first); Cout a multiple of 16 split into tiles of at most 256.
 // `status` (optional device word) receives bit 1 / 2 when a bounded wait ran out.
 bool conv3x3_tc_supported(const ConvArgs& a);
 cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st);

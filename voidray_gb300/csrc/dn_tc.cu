@@ -4,7 +4,8 @@
 // between one producer thread, one MMA-issuing thread and a 4-warp epilogue.
 //
 // Implicit GEMM per CTA: M = 128 output pixels (an 8 x 16 block of one
-// image), N = Cout (16..256, one tile), K = 9 taps x Cin in chunks of BK
+// image), N = up to 256 output channels (Cout split into equal tiles of a
+// multiple of 16 over blockIdx.y), K = 9 taps x Cin in chunks of BK
 // channels.  For tap (dy, dx) and channel chunk c0 the A tile is one 4-D TMA
 // box (BK channels x 16 columns x 8 rows x 1 image) of the NHWC activation at
 // (c0, x0 + dx, y0 + dy, n); out-of-image coordinates read zeros, which is
@@ -13,7 +14,9 @@
 // 128-byte, 32: 64-byte, 16: 32-byte rows), the layout tcgen05 reads through
 // its shared-memory descriptors.  The epilogue reads the fp32 accumulator
 // with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e. pixels), adds
-// the bias, applies ReLU and stores bf16 (or fp32) NHWC rows.
+// the bias, applies ReLU and/or a ReLU-backward mask and stores bf16 (or
+// fp32) NHWC rows.  With flipped weights the same kernel is the backward-data
+// convolution.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets an error bit in
 // the caller's status word and the CTA still drains and frees its TMEM.
@@ -100,11 +103,13 @@ __host__ __device__ constexpr uint32_t instr_desc(uint32_t m, uint32_t n) {
 
 struct TcArgs {
     const float* bias;
+    const bf16* mask;  // zero the output where mask <= 0 (ReLU backward), [P][cout], or null
     bf16* out;
     float* out_f32;
     uint32_t* status;
     int n, h, w;
     int c1, cin, cout;
+    int ntile;        // output channels per CTA (16..256; cout is a multiple)
     int bk;           // channels per K chunk (16, 32, 64)
     int relu;
     int tiles_x, tiles_y;
@@ -119,7 +124,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // 1024-byte aligned stage buffers (the 128-byte swizzle atom is 8 x 128 B)
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int N = a.cout;
+    const int N = a.ntile;              // MMA N: this CTA's output channels
+    const int n0 = blockIdx.y * N;      // first output channel of this CTA
     const uint32_t a_bytes = 128u * a.bk * 2u, b_bytes = (uint32_t)N * a.bk * 2u;
     const uint32_t stage_bytes = a_bytes + b_bytes;
     const uint32_t tmem_cols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
@@ -168,7 +174,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_expect_tx(&full_bar[s], stage_bytes);
             if (c0 < a.c1) tma_load_4d(sa, &map_a1, &full_bar[s], c0, x0 + dx, y0 + dy, img);
             else tma_load_4d(sa, &map_a2, &full_bar[s], c0 - a.c1, x0 + dx, y0 + dy, img);
-            tma_load_2d(sb, &map_b, &full_bar[s], tap * a.cin + c0, 0);
+            tma_load_2d(sb, &map_b, &full_bar[s], tap * a.cin + c0, n0);
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer: BK/16 tcgen05.mma per stage, accumulating in TMEM
@@ -226,11 +232,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float v[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            v[j] = __uint_as_float(r[j]) + (a.bias ? a.bias[c0 + j] : 0.0f);
+            v[j] = __uint_as_float(r[j]) + (a.bias ? a.bias[n0 + c0 + j] : 0.0f);
             if (a.relu) v[j] = fmaxf(v[j], 0.0f);
         }
+        const size_t o0 = pix * (size_t)a.cout + n0 + c0;
+        if (a.mask) {
+            union {
+                uint4 u[2];
+                bf16 h[16];
+            } mk;
+            const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o0);
+            mk.u[0] = mp[0];
+            mk.u[1] = mp[1];
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (!(__bfloat162float(mk.h[j]) > 0.0f)) v[j] = 0.0f;
+        }
         if (a.out_f32) {
-            float4* o = reinterpret_cast<float4*>(a.out_f32 + pix * N + c0);
+            float4* o = reinterpret_cast<float4*>(a.out_f32 + o0);
 #pragma unroll
             for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         } else {
@@ -240,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             } pk;
 #pragma unroll
             for (int j = 0; j < 16; ++j) pk.h[j] = __float2bfloat16_rn(v[j]);
-            uint4* o = reinterpret_cast<uint4*>(a.out + pix * N + c0);
+            uint4* o = reinterpret_cast<uint4*>(a.out + o0);
             o[0] = pk.u[0];
             o[1] = pk.u[1];
         }
@@ -289,11 +308,11 @@ bool encode_act(CUtensorMap* m, const bf16* p, int n, int h, int w, int c, int b
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// weights [cout][9 * cin] as a 2-D map with boxes of bk x cout
-bool encode_wgt(CUtensorMap* m, const bf16* p, int cout, int cin, int bk) {
+// weights [cout][9 * cin] as a 2-D map with boxes of bk x ntile
+bool encode_wgt(CUtensorMap* m, const bf16* p, int cout, int cin, int bk, int ntile) {
     const cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};
     const cuuint64_t strides[1] = {(cuuint64_t)9 * cin * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)cout};
+    const cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)ntile};
     const cuuint32_t es[2] = {1, 1};
     return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(p), dims, strides, box, es,
                        CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(bk), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -304,10 +323,20 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 }  // namespace
 
+// output channels per CTA: all of them up to 256, else the largest multiple
+// of 16 up to 256 that divides cout
+int ntile_for(int cout) {
+    if (cout <= 256) return cout;
+    for (int t = 256; t >= 16; t -= 16)
+        if (cout % t == 0) return t;
+    return 0;
+}
+
 bool conv3x3_tc_supported(const ConvArgs& a) {
     const int cin = a.c1 + a.c2;
-    if (a.up1 || a.mask || !encode_fn()) return false;
-    if (a.cout < 16 || a.cout > 256 || a.cout % 16) return false;
+    if (a.up1 || !encode_fn()) return false;
+    if (a.cout < 16 || a.cout % 16 || !ntile_for(a.cout)) return false;
+    if (a.mask && !aligned16(a.mask)) return false;
     if (cin % 16 || a.c1 % 16 || a.c2 % 16) return false;
     if (!aligned16(a.src1) || (a.c2 && !aligned16(a.src2)) || !aligned16(a.weight)) return false;
     return true;
@@ -324,9 +353,12 @@ cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (!encode_act(&ma1, a.src1, a.n, a.h, a.w, a.c1, bk)) return cudaErrorInvalidValue;
     if (a.c2 && !encode_act(&ma2, a.src2, a.n, a.h, a.w, a.c2, bk)) return cudaErrorInvalidValue;
     if (!a.c2) ma2 = ma1;
-    if (!encode_wgt(&mb, a.weight, a.cout, cin, bk)) return cudaErrorInvalidValue;
+    const int ntile = ntile_for(a.cout);
+    if (!encode_wgt(&mb, a.weight, a.cout, cin, bk, ntile)) return cudaErrorInvalidValue;
     TcArgs t{};
     t.bias = a.bias;
+    t.mask = a.mask;
+    t.ntile = ntile;
     t.out = a.out;
     t.out_f32 = a.out_f32;
     t.status = status;
@@ -340,7 +372,7 @@ cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     t.relu = a.relu;
     t.tiles_x = (a.w + 15) / 16;
     t.tiles_y = (a.h + 7) / 8;
-    const size_t stage = (size_t)128 * bk * 2 + (size_t)a.cout * bk * 2;
+    const size_t stage = (size_t)128 * bk * 2 + (size_t)ntile * bk * 2;
     const size_t smem = TC_STAGES * stage + 1024;
     static size_t configured = 0;
     if (smem > configured) {
@@ -348,7 +380,7 @@ cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    const unsigned grid = (unsigned)(t.tiles_x * t.tiles_y * a.n);
+    const dim3 grid((unsigned)(t.tiles_x * t.tiles_y * a.n), (unsigned)(a.cout / ntile));
     k_conv3x3_tc<<<grid, TC_THREADS, smem, st>>>(ma1, ma2, mb, t);
     return cudaGetLastError();
 }

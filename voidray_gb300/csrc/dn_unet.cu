@@ -287,14 +287,20 @@ vr_status backward(vr_denoiser* d, cudaStream_t st) {
         a.c1 = L.cout;
         a.cout = cin;
         bf16* next = d->dz[flip];
+        // backward-data on tcgen05 when the forward runs there
+        auto conv = [&](const dn::ConvArgs& c) -> cudaError_t {
+            if (d->backend == VR_DN_BACKEND_TCGEN05 && dn::conv3x3_tc_supported(c))
+                return dn::conv3x3_tc(c, d->status, st);
+            return dn::conv3x3(c, st);
+        };
         if (L.in2 >= 0) {
             a.out = d->dcat[l];
-            DN_CK(dn::conv3x3(a, st));
+            DN_CK(conv(a));
             const int lc = ACTS[L.in1].lvl;
             DN_CK(dn::up_bwd(d->dcat[l], cin, d->act[L.in1], next, n, h >> lc, w >> lc, c1, st));
         } else if (L.in1 == P0 || L.in1 == P1 || L.in1 == P2) {
             a.out = d->dpool;
-            DN_CK(dn::conv3x3(a, st));
+            DN_CK(conv(a));
             const int s = L.in1 - 1;  // the pooled skip tensor
             const int k = skip_consumer(s);
             const int ls = ACTS[s].lvl;
@@ -303,7 +309,7 @@ vr_status backward(vr_denoiser* d, cudaStream_t st) {
         } else {
             a.mask = d->act[L.in1];
             a.out = next;
-            DN_CK(dn::conv3x3(a, st));
+            DN_CK(conv(a));
         }
         cur = next;
         flip ^= 1;
@@ -602,9 +608,9 @@ vr_status vr_dn_conv3x3_device(const uint16_t* src1, uint32_t c1, int32_t up1, c
 }
 
 vr_status vr_dn_conv3x3_tc_device(const uint16_t* src1, uint32_t c1, const uint16_t* src2, uint32_t c2,
-                                  const uint16_t* weight, const float* bias, uint16_t* out_bf16, float* out_f32,
-                                  uint32_t cout, uint32_t n, uint32_t h, uint32_t w, int32_t relu,
-                                  uint32_t* status_device, void* stream) {
+                                  const uint16_t* weight, const float* bias, const uint16_t* mask,
+                                  uint16_t* out_bf16, float* out_f32, uint32_t cout, uint32_t n, uint32_t h,
+                                  uint32_t w, int32_t relu, uint32_t* status_device, void* stream) {
     if (!src1 || !weight || (!out_bf16 == !out_f32) || (c2 && !src2))
         return vr::set_error(VR_ERR_INVALID, "src1, weight and exactly one output are required");
     dn::ConvArgs a{};
@@ -612,6 +618,7 @@ vr_status vr_dn_conv3x3_tc_device(const uint16_t* src1, uint32_t c1, const uint1
     a.src2 = reinterpret_cast<const bf16*>(src2);
     a.weight = reinterpret_cast<const bf16*>(weight);
     a.bias = bias;
+    a.mask = reinterpret_cast<const bf16*>(mask);
     a.out = reinterpret_cast<bf16*>(out_bf16);
     a.out_f32 = out_f32;
     a.n = (int)n;
@@ -622,7 +629,7 @@ vr_status vr_dn_conv3x3_tc_device(const uint16_t* src1, uint32_t c1, const uint1
     a.cout = (int)cout;
     a.relu = relu ? 1 : 0;
     if (!dn::conv3x3_tc_supported(a))
-        return vr::set_error(VR_ERR_UNSUPPORTED, "tcgen05 convolution: Cout 16..256 and channels multiples of 16");
+        return vr::set_error(VR_ERR_UNSUPPORTED, "tcgen05 convolution: channels multiples of 16, 16-byte aligned");
     DN_CK(dn::conv3x3_tc(a, status_device, static_cast<cudaStream_t>(stream)));
     return VR_OK;
 }

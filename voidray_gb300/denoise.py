@@ -172,11 +172,11 @@ def conv3x3(src1, c1: int, weight, cout: int, n: int, h: int, w: int, *, src2=No
 
 
 def conv3x3_tc(src1, c1: int, weight, cout: int, n: int, h: int, w: int, *, src2=None, c2: int = 0, bias=None,
-               out_bf16=None, out_f32=None, relu: bool = False, status=None, stream: int = 0) -> None:
-    """Single forward convolution on tcgen05 (device pointers)."""
-    check(lib().vr_dn_conv3x3_tc_device(_p(src1), int(c1), _p(src2), int(c2), _p(weight), _p(bias), _p(out_bf16),
-                                        _p(out_f32), int(cout), int(n), int(h), int(w), int(relu), _p(status),
-                                        C.c_void_p(stream or None)))
+               mask=None, out_bf16=None, out_f32=None, relu: bool = False, status=None, stream: int = 0) -> None:
+    """Single convolution on tcgen05 (device pointers)."""
+    check(lib().vr_dn_conv3x3_tc_device(_p(src1), int(c1), _p(src2), int(c2), _p(weight), _p(bias), _p(mask),
+                                        _p(out_bf16), _p(out_f32), int(cout), int(n), int(h), int(w), int(relu),
+                                        _p(status), C.c_void_p(stream or None)))
 
 
 def conv3x3_wgrad(dz, src1, c1: int, dw, cout: int, n: int, h: int, w: int, *, src2=None, c2: int = 0,
