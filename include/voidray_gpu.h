@@ -328,6 +328,8 @@ typedef struct vr_instrument {
     uint64_t extend_tri_tests;
     uint64_t shadow_node_visits;
     uint64_t shadow_tri_tests;
+    uint64_t retired_paths;  /* VR_INSTR_WORK: paths that ended (queue conservation:
+                                equals the camera paths traced) */
 } vr_instrument;
 vr_status vr_scene_instrument(vr_scene* scene, uint32_t flags);
 vr_status vr_scene_instrument_get(vr_scene* scene, vr_instrument* out);

@@ -410,7 +410,7 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
                 for (uint32_t k = 0; k < wv.max_bounces; ++k) {
                     VR_CK(vr::launch_extend(wv, ps, k, status, wk, cs));
                     if (instr && (r = instr->mark(VR_STAGE_EXTEND, cs)) != VR_OK) return r;
-                    VR_CK(vr::launch_shade(wv, ps, k, cs));
+                    VR_CK(vr::launch_shade(wv, ps, k, wk ? wk + 4 : nullptr, cs));
                     if (instr && (r = instr->mark(VR_STAGE_SHADE, cs)) != VR_OK) return r;
                     if (wv.any_nee) {
                         VR_CK(vr::launch_shadow(wv, ps, k, status, wk ? wk + 2 : nullptr, cs));
@@ -582,8 +582,8 @@ vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
 vr_status vr_scene_instrument(vr_scene* s, uint32_t flags) {
     if (!s) return fail(VR_ERR_INVALID, "null scene");
     VR_CK(cudaStreamSynchronize(s->stream));
-    if (!s->instr.work) VR_CK(cudaMalloc(&s->instr.work, 4 * sizeof(unsigned long long)));
-    VR_CK(cudaMemset(s->instr.work, 0, 4 * sizeof(unsigned long long)));
+    if (!s->instr.work) VR_CK(cudaMalloc(&s->instr.work, 5 * sizeof(unsigned long long)));
+    VR_CK(cudaMemset(s->instr.work, 0, 5 * sizeof(unsigned long long)));
     s->instr.flags = flags;
     s->instr.used = 0;
     for (int i = 0; i < 8; ++i) {
@@ -604,12 +604,13 @@ vr_status vr_scene_instrument_get(vr_scene* s, vr_instrument* out) {
         out->stage_launches[i] = s->instr.stage_launches[i];
     }
     if (s->instr.work) {
-        unsigned long long w[4];
+        unsigned long long w[5];
         VR_CK(cudaMemcpy(w, s->instr.work, sizeof w, cudaMemcpyDeviceToHost));
         out->extend_node_visits = w[0];
         out->extend_tri_tests = w[1];
         out->shadow_node_visits = w[2];
         out->shadow_tri_tests = w[3];
+        out->retired_paths = w[4];
     }
     return VR_OK;
 }

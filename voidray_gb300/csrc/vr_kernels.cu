@@ -518,7 +518,7 @@ __device__ __forceinline__ uint32_t queue_append(bool want, uint32_t r, uint32_t
 }
 
 template <bool ONE>
-__global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k) {
+__global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;
     if (ONE) {
@@ -666,6 +666,12 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k)
                 }
             }
             ps.rng[p] = rng.state;
+        }
+        // queue conservation (instrumented runs): every path that does not
+        // continue is retired here, exactly once
+        if (retired) {
+            const uint32_t gone = __ballot_sync(0xffffffffu, i < n && !cont);
+            if (lane == 0 && gone) atomicAdd(retired, (unsigned long long)__popc(gone));
         }
         // warp-aggregated compaction into the job's next queue segment and shadow segment
         const uint32_t base_r = (ONE || i >= n) ? 0u : w.jobs[r].base;
@@ -968,10 +974,13 @@ cudaError_t launch_extend(const Wave& w, const PathState& ps, uint32_t k, uint32
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, cudaStream_t st) {
+cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, unsigned long long* retired,
+                         cudaStream_t st) {
     const int sb = (int)g_tuning.shade_block, per_sm = (int)g_tuning.shade_blocks_per_sm;
-    if (w.njobs == 1 && !w.from_table) k_shade<true><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k);
-    else k_shade<false><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k);
+    if (w.njobs == 1 && !w.from_table)
+        k_shade<true><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k, retired);
+    else
+        k_shade<false><<<grid_for(w.total_paths, sb, per_sm), sb, 0, st>>>(w, ps, k, retired);
     return cudaGetLastError();
 }
 
