@@ -73,7 +73,7 @@ def workload(args):
     if args.wavefront:
         st.wavefront_paths = args.wavefront
     cfg = {
-        "workload": "plain GPU render: displaced icosphere + ground, HDRI importance-sampled (configs[2])",
+        "workload": "plain GPU render: displaced icosphere + ground, HDRI importance-sampled, 1920x1080 x 256 spp",
         "triangles": scene.num_triangles(),
         "resolution": f"{args.width}x{args.height}",
         "spp": args.spp,

@@ -1,4 +1,4 @@
-"""The denoiser's FP64 CPU restatement is pinned before it judges the GPU:
+"""The denoiser's FP64 CPU restatement is pinned before it checks the GPU:
 its hand-written backward equals torch autograd on the unrounded graph, and
 its layer table / parameter packing equal the library's.  No GPU needed."""
 import numpy as np

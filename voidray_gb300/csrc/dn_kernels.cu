@@ -517,7 +517,7 @@ __global__ void k_postprocess(const float* __restrict__ out, int cout, const flo
 
 // kind LOSS_L1_LOG: |o - log1p(t / (albedo + eps))|, gradient sign(d) / count.
 // kind LOSS_RELMSE: (y - t)^2 / (max(y, 0)^2 + 0.01) with y = expm1(min(o, 20))
-// * (albedo + eps), the relative error the renders are judged by, normalised
+// * (albedo + eps), the relative error the renders are measured in, normalised
 // by the prediction held constant (the target is itself a noisy render, and a
 // noisy denominator would bias the fit); gradient
 // 2 (y - t) / (max(y, 0)^2 + 0.01) * (albedo + eps) * exp(o) / count.
