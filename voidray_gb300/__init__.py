@@ -5,6 +5,7 @@ The compute path is the native library ``_lib/libvoidray_gb300.so`` (C ABI in
 camera, material and settings API on top of it.
 """
 from ._native import EXPORTED, VR_MISS, VoidrayError, lib
+from .renderer import Renderer, RenderAction, RendererStats
 from .scene import (Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
                     Materials, Mesh, MicrofacetBSDF, RenderMode, RenderSettings, Scene, SceneAcceleration, Settings,
                     Surfaces, Tonemap, Vertex, degrees_to_radians, hex_color, iterative_render, render_device, tonemap)
@@ -13,5 +14,6 @@ __all__ = [
     "EXPORTED", "VR_MISS", "VoidrayError", "lib", "Camera", "ColorManagementSettings", "CpuRenderTarget",
     "Environment", "Environments", "Estimator", "Material", "Materials", "Mesh", "MicrofacetBSDF", "RenderMode",
     "RenderSettings", "Scene", "SceneAcceleration", "Settings", "Surfaces", "Tonemap", "Vertex",
-    "degrees_to_radians", "hex_color", "iterative_render", "render_device", "tonemap",
+    "degrees_to_radians", "hex_color", "iterative_render", "render_device", "tonemap", "Renderer", "RenderAction",
+    "RendererStats",
 ]
