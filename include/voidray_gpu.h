@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define VR_ABI_VERSION 1
+#define VR_ABI_VERSION 2
 
 typedef enum vr_status {
     VR_OK = 0,
@@ -120,6 +120,24 @@ typedef struct vr_camera_desc {
     float focal_point[3];
 } vr_camera_desc;
 
+/* Analytic surfaces (voidray_common/src/surfaces.rs:31-114): Surfaces::sphere
+ * (quadratic, normal (p - c) / r, uv 0) and Surfaces::ground_plane (y =
+ * height, normal +y, uv (x, z)).  Tested against every ray beside the
+ * triangle BVH; their prim id in hits is num_triangles + index. */
+typedef enum vr_analytic_kind {
+    VR_ANALYTIC_SPHERE = 1,
+    VR_ANALYTIC_GROUND_PLANE = 2
+} vr_analytic_kind;
+
+typedef struct vr_analytic_desc {
+    int32_t kind;             /* vr_analytic_kind                               */
+    float center[3];          /* sphere                                         */
+    float radius;             /* sphere                                         */
+    float height;             /* ground plane                                   */
+    uint32_t material;        /* index into vr_scene_desc.materials             */
+    uint32_t pad_;
+} vr_analytic_desc;
+
 typedef struct vr_scene_desc {
     const vr_mesh_desc* meshes;
     uint32_t num_meshes;
@@ -129,7 +147,11 @@ typedef struct vr_scene_desc {
     vr_camera_desc camera;
     uint32_t bvh_max_leaf;  /* 0 = default (4)                                  */
     uint32_t bvh_bins;      /* 0 = default (16)                                 */
+    const vr_analytic_desc* analytics;  /* may be NULL when num_analytics == 0  */
+    uint32_t num_analytics;             /* at most VR_MAX_ANALYTICS             */
+    uint32_t pad_;
 } vr_scene_desc;
+#define VR_MAX_ANALYTICS 64
 
 typedef struct vr_scene vr_scene;
 

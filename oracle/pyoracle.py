@@ -26,7 +26,13 @@ def build(force: bool = False) -> Path:
 
 class orc_mesh(C.Structure):
     _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p), ("indices", C.c_void_p),
-                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32)]
+                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32), ("surface", C.c_uint32),
+                ("pad_", C.c_uint32)]
+
+
+class orc_analytic(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("center", C.c_float * 3), ("radius", C.c_float), ("height", C.c_float),
+                ("surface", C.c_uint32), ("pad_", C.c_uint32)]
 
 
 class orc_object(C.Structure):
@@ -52,7 +58,8 @@ class orc_camera(C.Structure):
 class orc_scene_desc(C.Structure):
     _fields_ = [("meshes", C.c_void_p), ("num_meshes", C.c_uint32), ("num_materials", C.c_uint32),
                 ("materials", C.c_void_p), ("objects", C.c_void_p), ("num_objects", C.c_uint32),
-                ("pad_", C.c_uint32), ("env", orc_env), ("camera", orc_camera)]
+                ("pad_", C.c_uint32), ("env", orc_env), ("camera", orc_camera), ("analytics", C.c_void_p),
+                ("num_analytics", C.c_uint32), ("pad2_", C.c_uint32)]
 
 
 class orc_settings(C.Structure):
@@ -108,13 +115,20 @@ class OracleScene:
 
     def __init__(self, scene):
         keep = []
-        n = len(scene.surfaces)
+        mesh_surfs = [(s, x) for s, x in enumerate(scene.surfaces) if isinstance(x, int)]
+        ana_surfs = [(s, x) for s, x in enumerate(scene.surfaces) if not isinstance(x, int)]
+        n = len(mesh_surfs)
         meshes = (orc_mesh * max(1, n))()
-        for s, mi in enumerate(scene.surfaces):
+        for k, (s, mi) in enumerate(mesh_surfs):
             m = scene.meshes[mi]
             keep.append(m)
-            meshes[s] = orc_mesh(_p(m.positions), _p(m.normals), _p(m.uvs), _p(m.indices), len(m.positions),
-                                 len(m.indices))
+            meshes[k] = orc_mesh(_p(m.positions), _p(m.normals), _p(m.uvs), _p(m.indices), len(m.positions),
+                                 len(m.indices), s, 0)
+        anas = (orc_analytic * max(1, len(ana_surfs)))()
+        for k, (s, a) in enumerate(ana_surfs):
+            anas[k].kind, anas[k].radius, anas[k].height, anas[k].surface = a.kind, a.radius, a.height, s
+            for j in range(3):
+                anas[k].center[j] = float(a.center[j])
         mats = (orc_material * max(1, len(scene.materials)))()
         for i, m in enumerate(scene.materials):
             c = mats[i]
@@ -123,9 +137,11 @@ class OracleScene:
                 c.color[k] = float(m.color[k])
             c.fuzz, c.ir, c.roughness, c.metallic = m.fuzz, m.ir, m.roughness, m.metallic
             c.emittance, c.transparent = m.emittance, int(m.transparent)
+        keep.append(anas)
         objs = (orc_object * max(1, len(scene.objects)))(*[orc_object(o.surface, o.material) for o in scene.objects])
         d = orc_scene_desc()
         d.meshes, d.num_meshes = C.addressof(meshes), n
+        d.analytics, d.num_analytics = C.addressof(anas), len(ana_surfs)
         d.materials, d.num_materials = C.addressof(mats), len(scene.materials)
         d.objects, d.num_objects = C.addressof(objs), len(scene.objects)
         env = scene.environment

@@ -272,8 +272,19 @@ struct EnvTables {
     std::vector<float> marginal, conditional, cell;
 };
 
+struct Analytic {
+    int kind;  // 1 sphere, 2 ground plane
+    V3 center;
+    float radius, height;
+    int surface;
+};
+
 struct Scene {
     std::vector<Mesh> meshes;
+    std::vector<Analytic> analytics;
+    std::vector<int> mesh_surface;      // surface index of each mesh
+    std::vector<int> surf_mesh;         // per surface: mesh index or -1
+    std::vector<int> surf_analytic;     // per surface: analytic index or -1
     std::vector<orc_material> materials;
     std::vector<int> surface_material;  // material of surface s (QUIRK, scene.rs:377)
     Bvh top;
@@ -388,10 +399,48 @@ HitPair mesh_hit(const Mesh& m, const Ray& r, float tmin, float tmax) {
     }
     return hp;
 }
+// Sphere::hit (surfaces.rs:45-80) and GroundPlane::hit (surfaces.rs:86-105).
+// The hit's prim id is num_prims + analytic index.
+HitPair analytic_hit(const Scene& s, int ai, const Ray& r, float tmin, float tmax) {
+    const Analytic& a = s.analytics[ai];
+    HitPair hp;
+    Hit h;
+    h.prim = (uint32_t)(s.num_prims + ai);
+    h.bu = h.bv = 0.0f;
+    if (a.kind == 1) {
+        V3 oc = r.o - a.center;
+        float aa = mag2(r.d);
+        float half_b = dot(oc, r.d);
+        float c = mag2(oc) - a.radius * a.radius;
+        float disc = half_b * half_b - aa * c;
+        if (disc < 0.0f) return hp;
+        float sq = std::sqrt(disc);
+        float root = (-half_b - sq) / aa;
+        if (root < tmin || tmax < root) {
+            root = (-half_b + sq) / aa;
+            if (root < tmin || tmax < root) return hp;
+        }
+        V3 point = r.o + r.d * root;
+        V3 normal = (point - a.center) / a.radius;
+        make_hit(h, point, normal, root, 0.0f, 0.0f, r);
+    } else {
+        float t = (a.height - r.o.y) / r.d.y;
+        if (t <= tmin || t >= tmax) return hp;
+        V3 point = r.o + r.d * t;
+        make_hit(h, point, v3(0.0f, 1.0f, 0.0f), t, point.x, point.z, r);
+    }
+    hp.ok = true;
+    hp.best = h;
+    return hp;
+}
+HitPair surface_hit(const Scene& s, int si, const Ray& r, float tmin, float tmax) {
+    if (s.surf_mesh[si] >= 0) return mesh_hit(s.meshes[s.surf_mesh[si]], r, tmin, tmax);
+    return analytic_hit(s, s.surf_analytic[si], r, tmin, tmax);
+}
 HitPair top_hit(const Scene& s, int ni, const Ray& r, float tmin, float tmax) {
     const Node& n = s.top.nodes[ni];
     HitPair hp;
-    if (n.kind == 1) return mesh_hit(s.meshes[n.handle], r, tmin, tmax);
+    if (n.kind == 1) return surface_hit(s, (int)n.handle, r, tmin, tmax);
     if (n.kind == 2 && aabb_hit(n.bounds, r, tmin, tmax))
         return merge(top_hit(s, n.left, r, tmin, tmax), top_hit(s, n.right, r, tmin, tmax));
     return hp;
@@ -402,13 +451,21 @@ inline HitPair scene_hit(const Scene& s, const Ray& r, float tmin = SCENE_TMIN, 
     if (s.top.root < 0) return HitPair{};
     return top_hit(s, s.top.root, r, tmin, tmax);
 }
-int surface_of_prim(const Scene& s, uint32_t prim) {
+int mesh_of_prim(const Scene& s, uint32_t prim) {
     // meshes are few; linear search is fine for the oracle
     for (size_t i = 0; i < s.meshes.size(); ++i) {
         const Mesh& m = s.meshes[i];
         if (prim >= m.first_prim && prim < m.first_prim + m.face_n.size()) return (int)i;
     }
     return -1;
+}
+int surface_of_prim(const Scene& s, uint32_t prim) {
+    if (prim >= s.num_prims) {
+        const uint64_t a = prim - s.num_prims;
+        return a < s.analytics.size() ? s.analytics[a].surface : -1;
+    }
+    const int m = mesh_of_prim(s, prim);
+    return m < 0 ? -1 : s.mesh_surface[m];
 }
 
 // ----------------------------------------------------------- environment --
@@ -991,20 +1048,48 @@ orc_scene* orc_scene_create(const orc_scene_desc* d) {
             m.has_bvh = true;
         }
     }
+    // the surface list: meshes and analytic surfaces at their surface indices
+    const size_t nsurf = d->num_meshes + (size_t)d->num_analytics;
+    s.surf_mesh.assign(nsurf, -1);
+    s.surf_analytic.assign(nsurf, -1);
+    for (uint32_t mi = 0; mi < d->num_meshes; ++mi) {
+        const uint32_t si = d->meshes[mi].surface;
+        if (si >= nsurf || s.surf_mesh[si] >= 0) { g_err = "bad mesh surface index"; return nullptr; }
+        s.surf_mesh[si] = (int)mi;
+        s.mesh_surface.push_back((int)si);
+    }
+    for (uint32_t ai = 0; ai < d->num_analytics; ++ai) {
+        const orc_analytic& ad = d->analytics[ai];
+        if (ad.surface >= nsurf || s.surf_mesh[ad.surface] >= 0 || s.surf_analytic[ad.surface] >= 0) {
+            g_err = "bad analytic surface index";
+            return nullptr;
+        }
+        s.surf_analytic[ad.surface] = (int)ai;
+        s.analytics.push_back(Analytic{ad.kind, load3(ad.center), ad.radius, ad.height, (int)ad.surface});
+    }
     // QUIRK (scene.rs:283-285, 377-378): the top-level BVH is over surface
     // indices and the hit surface index is used as the object index.
-    s.surface_material.assign(s.meshes.size(), -1);
-    for (size_t si = 0; si < s.meshes.size(); ++si) {
+    s.surface_material.assign(nsurf, -1);
+    for (size_t si = 0; si < nsurf; ++si) {
         if (si >= d->num_objects) { g_err = "surface without an object at the same index"; return nullptr; }
         uint32_t mat = d->objects[si].material;
         if (mat >= d->num_materials) { g_err = "material index out of range"; return nullptr; }
         s.surface_material[si] = (int)mat;
     }
     {
-        std::vector<uint32_t> objs(s.meshes.size());
+        std::vector<uint32_t> objs(nsurf);
         for (uint32_t i = 0; i < objs.size(); ++i) objs[i] = i;
         const Scene* sp = &s;
-        auto bounds_ref = [sp](uint32_t i) { return sp->meshes[i].bounds; };
+        // Bounded::bounds: mesh box, sphere center +- r, ground plane infinite in x, z (surfaces.rs:37-43, 107-114)
+        auto bounds_ref = [sp](uint32_t i) {
+            if (sp->surf_mesh[i] >= 0) return sp->meshes[sp->surf_mesh[i]].bounds;
+            const Analytic& a = sp->analytics[sp->surf_analytic[i]];
+            if (a.kind == 1) {
+                V3 rr = v3(a.radius, a.radius, a.radius);
+                return Aabb{a.center - rr, a.center + rr};
+            }
+            return Aabb{v3(-INF_F, a.height - 0.0001f, -INF_F), v3(INF_F, a.height + 0.0001f, INF_F)};
+        };
         s.top.root = objs.empty() ? -1 : bvh_build(s.top, objs, bounds_ref);
     }
     s.env = d->env;
@@ -1052,6 +1137,10 @@ static void set_threads(int32_t t) {
 
 static HitPair brute(const Scene& s, const Ray& r, float tmin) {
     HitPair hp;
+    for (size_t a = 0; a < s.analytics.size(); ++a) {
+        HitPair ha = analytic_hit(s, (int)a, r, tmin, INF_F);
+        if (ha.ok && (!hp.ok || ha.best.t < hp.best.t)) hp = ha;
+    }
     for (const Mesh& m : s.meshes) {
         uint32_t nt = (uint32_t)m.face_n.size();
         for (uint32_t i = 0; i < nt; ++i) {
@@ -1100,7 +1189,7 @@ void orc_intersect(const orc_scene* sh, const orc_ray* rays, uint64_t n, orc_hit
 
 int32_t orc_triangle_hit(const orc_scene* sh, uint32_t prim, const orc_ray* q, float* t, float* u, float* v) {
     const Scene& s = sh->s;
-    int si = surface_of_prim(s, prim);
+    int si = mesh_of_prim(s, prim);
     if (si < 0) return 0;
     const Mesh& m = s.meshes[si];
     Hit h;
@@ -1114,7 +1203,7 @@ int32_t orc_triangle_hit(const orc_scene* sh, uint32_t prim, const orc_ray* q, f
 
 int32_t orc_reintersect_f64(const orc_scene* sh, uint32_t prim, const orc_ray* q, double* t, double* u, double* v) {
     const Scene& s = sh->s;
-    int si = surface_of_prim(s, prim);
+    int si = mesh_of_prim(s, prim);
     if (si < 0) return 0;
     const Mesh& m = s.meshes[si];
     const uint32_t* ix = &m.idx[3 * (prim - m.first_prim)];

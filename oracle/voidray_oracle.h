@@ -43,7 +43,19 @@ typedef struct orc_mesh {
     const uint32_t* indices; /* 3*nt */
     uint32_t num_vertices;
     uint32_t num_triangles;
+    uint32_t surface;        /* index in the scene's surface list */
+    uint32_t pad_;
 } orc_mesh;
+
+/* Surfaces::sphere / Surfaces::ground_plane (voidray_common/src/surfaces.rs) */
+typedef struct orc_analytic {
+    int32_t kind;            /* 1 sphere, 2 ground plane */
+    float center[3];
+    float radius;
+    float height;
+    uint32_t surface;        /* index in the scene's surface list */
+    uint32_t pad_;
+} orc_analytic;
 
 typedef struct orc_object { uint32_t surface; uint32_t material; } orc_object;
 
@@ -68,6 +80,7 @@ typedef struct orc_scene_desc {
     const orc_object* objects; uint32_t num_objects; uint32_t pad_;
     orc_env env;
     orc_camera camera;
+    const orc_analytic* analytics; uint32_t num_analytics; uint32_t pad2_;
 } orc_scene_desc;
 
 typedef struct orc_settings {

@@ -51,10 +51,16 @@ class vr_camera_desc(C.Structure):
                 ("has_dof", C.c_int32), ("aperture", C.c_float), ("focal_point", C.c_float * 3)]
 
 
+class vr_analytic_desc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("center", C.c_float * 3), ("radius", C.c_float), ("height", C.c_float),
+                ("material", C.c_uint32), ("pad_", C.c_uint32)]
+
+
 class vr_scene_desc(C.Structure):
     _fields_ = [("meshes", C.c_void_p), ("num_meshes", C.c_uint32), ("num_materials", C.c_uint32),
                 ("materials", C.c_void_p), ("environment", vr_environment_desc), ("camera", vr_camera_desc),
-                ("bvh_max_leaf", C.c_uint32), ("bvh_bins", C.c_uint32)]
+                ("bvh_max_leaf", C.c_uint32), ("bvh_bins", C.c_uint32), ("analytics", C.c_void_p),
+                ("num_analytics", C.c_uint32), ("pad_", C.c_uint32)]
 
 
 class vr_scene_info(C.Structure):

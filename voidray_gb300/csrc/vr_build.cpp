@@ -448,6 +448,31 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     }
     v.env_is = hs.has_tables ? 1 : 0;
     v.num_materials = (int32_t)d->num_materials;
+    // analytic surfaces (surfaces.rs:31-114)
+    if (d->num_analytics && !d->analytics) { err = "analytics is NULL"; return VR_ERR_INVALID; }
+    if (d->num_analytics > VR_MAX_ANALYTICS) { err = "too many analytic surfaces"; return VR_ERR_UNSUPPORTED; }
+    hs.analytic.clear();
+    for (uint32_t i = 0; i < d->num_analytics; ++i) {
+        const vr_analytic_desc& a = d->analytics[i];
+        if (a.material >= d->num_materials) {
+            err = "analytic surface " + std::to_string(i) + ": material index out of range";
+            return VR_ERR_INVALID;
+        }
+        float kb, mb;
+        std::memcpy(&kb, &a.kind, 4);
+        std::memcpy(&mb, &a.material, 4);
+        if (a.kind == VR_ANALYTIC_SPHERE)
+            hs.analytic.push_back(make_float4(a.center[0], a.center[1], a.center[2], a.radius));
+        else if (a.kind == VR_ANALYTIC_GROUND_PLANE)
+            hs.analytic.push_back(make_float4(0.0f, a.height, 0.0f, 0.0f));
+        else {
+            err = "analytic surface " + std::to_string(i) + ": unsupported kind";
+            return VR_ERR_UNSUPPORTED;
+        }
+        hs.analytic.push_back(make_float4(kb, mb, 0.0f, 0.0f));
+    }
+    v.num_analytic = d->num_analytics;
+    v.num_tris = (uint32_t)np;
     set_camera(v, d->camera);
     hs.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return VR_OK;

@@ -528,6 +528,7 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if ((st = upload(s, hs.shade, &s->view.shade)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.uvs, &s->view.uvs)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.materials, &s->view.materials)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.analytic, &s->view.analytic)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.env_img, &s->view.env_img)) != VR_OK) return cleanup(st);
     if (hs.has_tables) {
         if ((st = upload(s, hs.tables.marginal, &s->view.env_marg)) != VR_OK) return cleanup(st);
@@ -916,7 +917,7 @@ vr_status vr_intersect_device(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hi
     if (n && (!rays || !hits)) return fail(VR_ERR_INVALID, "null rays/hits");
     if (n == 0) return VR_OK;
     cudaStream_t cs = pick(s, stream);
-    if (s->info.num_triangles == 0) {
+    if (s->info.num_triangles == 0 && s->view.num_analytic == 0) {
         // empty scene: every ray misses
         VR_CK(cudaMemsetAsync(hits, 0xFF, n * sizeof(vr_hit), cs));
         return VR_OK;

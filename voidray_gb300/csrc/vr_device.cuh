@@ -50,6 +50,11 @@ struct SceneView {
     const float2* uvs;  // 3 per prim
     const Material* materials;
     int32_t num_materials;
+    // analytic surfaces: 2 float4 each, (center | radius) or (0, height, 0, 0),
+    // then (kind bits, material bits, 0, 0); prim id = num_tris + index
+    const float4* analytic;
+    uint32_t num_analytic;
+    uint32_t num_tris;
     // environment
     int32_t env_kind;
     float env_color[3];
@@ -162,6 +167,57 @@ __device__ __forceinline__ void unit_circle(Rng& r, float* x, float* y) {
         *x = diff / sum; *y = 2.0f * x1 * x2 / sum; return;
     }
     *x = 1.0f; *y = 0.0f;
+}
+
+// ------------------------------------------------------ analytic surfaces --
+constexpr uint32_t A_SPHERE = 1, A_PLANE = 2;
+
+// Sphere::hit (surfaces.rs:45-80) and GroundPlane::hit (surfaces.rs:86-105),
+// in the reference's operation order: true and t when the surface is hit in
+// the reference's (tmin, tmax) window.
+__device__ __forceinline__ bool analytic_hit(float4 a0, uint32_t kind, V3 o, V3 d, float tmin, float tmax, float& t) {
+    if (kind == A_SPHERE) {
+        const V3 oc = o - v3(a0.x, a0.y, a0.z);
+        const float a = mag2(d);
+        const float half_b = dot(oc, d);
+        const float c = mag2(oc) - a0.w * a0.w;
+        const float disc = half_b * half_b - a * c;
+        if (disc < 0.0f) return false;
+        const float sq = sqrtf(disc);
+        float root = (-half_b - sq) / a;
+        if (root < tmin || tmax < root) {
+            root = (-half_b + sq) / a;
+            if (root < tmin || tmax < root) return false;
+        }
+        t = root;
+        return true;
+    }
+    const float tt = (a0.y - o.y) / d.y;
+    if (tt <= tmin || tt >= tmax) return false;
+    t = tt;
+    return true;
+}
+
+// Nearest analytic hit in front of t_best (prim = num_tris + index).
+__device__ __forceinline__ void analytic_closest(const float4* ana, uint32_t nana, uint32_t ntris, V3 o, V3 d,
+                                                 float tmin, float tmax, float& t_best, uint32_t& prim) {
+    for (uint32_t i = 0; i < nana; ++i) {
+        const float4 a0 = __ldg(ana + 2 * i), a1 = __ldg(ana + 2 * i + 1);
+        float t;
+        if (analytic_hit(a0, __float_as_uint(a1.x), o, d, tmin, tmax, t) && t < t_best) {
+            t_best = t;
+            prim = ntris + i;
+        }
+    }
+}
+
+__device__ __forceinline__ bool analytic_any(const float4* ana, uint32_t nana, V3 o, V3 d, float tmin, float tmax) {
+    for (uint32_t i = 0; i < nana; ++i) {
+        const float4 a0 = __ldg(ana + 2 * i), a1 = __ldg(ana + 2 * i + 1);
+        float t;
+        if (analytic_hit(a0, __float_as_uint(a1.x), o, d, tmin, tmax, t)) return true;
+    }
+    return false;
 }
 
 }  // namespace vr

@@ -29,6 +29,7 @@ struct HostScene {
     std::vector<float4> shade;  // 4 per prim, global id order
     std::vector<float2> uvs;    // 3 per prim, empty if no mesh has uvs
     std::vector<Material> materials;
+    std::vector<float4> analytic;  // 2 per analytic surface
     std::vector<float> env_img;
     EnvTables tables;
     bool has_tables = false;

@@ -35,6 +35,9 @@ struct BatchIo {
     float4* hits;
     const float4* nodes;
     const float4* tris;
+    const float4* ana;  // analytic surfaces, tested after the BVH
+    uint32_t nana, ntris;
+    bool any;
     __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd, const float4*& n, const float4*& t) const {
         ro = __ldg(rays + 2 * (size_t)i);
         rd = __ldg(rays + 2 * (size_t)i + 1);
@@ -44,6 +47,17 @@ struct BatchIo {
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
         HitOut o = h;
         if (overflow) o.prim = MISS;
+        if (nana && !overflow && !(any && o.prim != MISS)) {
+            const float4 ro = __ldg(rays + 2 * (size_t)i), rd = __ldg(rays + 2 * (size_t)i + 1);
+            float tb = o.prim == MISS ? INF_F : o.t;
+            uint32_t pb = o.prim;
+            analytic_closest(ana, nana, ntris, xyz(ro), xyz(rd), ro.w, rd.w, tb, pb);
+            if (pb != o.prim) {
+                o.prim = pb;
+                o.t = tb;
+                o.u = o.v = 0.0f;
+            }
+        }
         hits[i] = pack_hit(o);
     }
 };
@@ -461,7 +475,7 @@ struct ExtendIo {
         const uint32_t q = slot(i, r);
         HitOut o = h;
         if (overflow) o.prim = MISS;
-        hits[q] = pack_hit(o);
+        hits[q] = pack_hit(o);  // analytic surfaces are tested by k_shade
     }
 };
 
@@ -550,8 +564,17 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
             p = ps.q_path[q];
             const float4 ro4 = ps.q_org[q], rd4 = ps.q_dir[q];
             const V3 ro = xyz(ro4), rd = xyz(rd4);
-            const float4 hh = ps.hits[q - in_half];
-            const uint32_t prim = __float_as_uint(hh.x);
+            float4 hh = ps.hits[q - in_half];
+            uint32_t prim = __float_as_uint(hh.x);
+            if (s.num_analytic) {  // SceneAcceleration::hit keeps the nearest surface, analytic ones included
+                float tb = prim == MISS ? INF_F : hh.y;
+                uint32_t pb = prim;
+                analytic_closest(s.analytic, s.num_analytic, s.num_tris, ro, rd, ro4.w, rd4.w, tb, pb);
+                if (pb != prim) {
+                    prim = pb;
+                    hh = make_float4(__uint_as_float(pb), tb, 0.0f, 0.0f);
+                }
+            }
             uint32_t pixel, sample;
             path_coords(j, p, pixel, sample);
             Rng rng;
@@ -578,18 +601,31 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                     unwind(ps, p, k, le, fc);
                 }
             } else {
-                // shading record and normal (mesh.rs:176-188, ray.rs:34-49)
-                const float4* sh = s.shade + 4 * (size_t)prim;
-                const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3);
-                const Material m = s.materials[__float_as_uint(s0.w)];
-                const float u = hh.z, v = hh.w, t = hh.y;
-                const float wb = 1.0f - u - v;
-                V3 normal = u * xyz(s1) + v * xyz(s2) + wb * xyz(s0);
-                const V3 fnm = xyz(s3);
-                const float ang = acosf(dot(normal, fnm) / (sqrtf(mag2(normal)) * sqrtf(mag2(fnm))));
-                if (ang > 30.0f * PI_F / 180.0f) normal = fnm;
+                const float t = hh.y;
+                const V3 point = ro + rd * t;
+                Material m;
+                V3 normal;
+                if (prim < s.num_tris) {
+                    // shading record and normal (mesh.rs:176-188, ray.rs:34-49)
+                    const float4* sh = s.shade + 4 * (size_t)prim;
+                    const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3);
+                    m = s.materials[__float_as_uint(s0.w)];
+                    const float u = hh.z, v = hh.w;
+                    const float wb = 1.0f - u - v;
+                    normal = u * xyz(s1) + v * xyz(s2) + wb * xyz(s0);
+                    const V3 fnm = xyz(s3);
+                    const float ang = acosf(dot(normal, fnm) / (sqrtf(mag2(normal)) * sqrtf(mag2(fnm))));
+                    if (ang > 30.0f * PI_F / 180.0f) normal = fnm;
+                } else {
+                    // analytic surface: sphere normal (p - c) / r, ground plane +y (surfaces.rs:74-75, 98-102)
+                    const float4 a0 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris));
+                    const float4 a1 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris) + 1);
+                    m = s.materials[__float_as_uint(a1.y)];
+                    normal = __float_as_uint(a1.x) == A_SPHERE ? (point - v3(a0.x, a0.y, a0.z)) / a0.w
+                                                                : v3(0.0f, 1.0f, 0.0f);
+                }
                 SurfHit hit;
-                hit.point = ro + rd * t;
+                hit.point = point;
                 hit.t = t;
                 hit.front = dot(rd, normal) < 0.0f;
                 hit.normal = hit.front ? normal : -normal;
@@ -701,9 +737,11 @@ struct ShadowIo {
     const Job* jobs;
     const uint32_t* pre;
     uint32_t njobs;
-    const float4* nodes1;  // ONE: the single job's BVH and clamp
+    const float4* nodes1;  // ONE: the single job's BVH, clamp and analytic surfaces
     const float4* tris1;
     float fc1;
+    const float4* ana1;
+    uint32_t nana1;
     __device__ __forceinline__ uint32_t slot(uint32_t i, uint32_t& r) const {
         if (ONE) {
             r = 0;
@@ -723,8 +761,13 @@ struct ShadowIo {
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
         uint32_t r;
         const uint32_t q = slot(i, r);
-        if (!overflow && h.prim == MISS)
-            rad_add(ps, ps.s_path[q], clampc(xyz(ps.s_contrib[q]), ONE ? fc1 : jobs[r].rp.firefly_clamp));
+        if (overflow || h.prim != MISS) return;
+        const uint32_t nana = ONE ? nana1 : jobs[r].view.num_analytic;
+        if (nana) {  // an analytic surface in the way also occludes
+            const float4 ro = ps.s_org[q], rd = ps.s_dir[q];
+            if (analytic_any(ONE ? ana1 : jobs[r].view.analytic, nana, xyz(ro), xyz(rd), ro.w, rd.w)) return;
+        }
+        rad_add(ps, ps.s_path[q], clampc(xyz(ps.s_contrib[q]), ONE ? fc1 : jobs[r].rp.firefly_clamp));
     }
 };
 
@@ -739,7 +782,15 @@ __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(Wave w, PathState
         job_prefix(ps.counts, MAX_DEPTH_SLOTS + k, w.njobs, pre);
         n = pre[w.njobs];
     }
-    ShadowIo<ONE> io{ps, w.jobs, pre, w.njobs, w.first.view.nodes, w.first.view.tris, w.first.rp.firefly_clamp};
+    ShadowIo<ONE> io{ps,
+                     w.jobs,
+                     pre,
+                     w.njobs,
+                     w.first.view.nodes,
+                     w.first.view.tris,
+                     w.first.rp.firefly_clamp,
+                     w.first.view.analytic,
+                     w.first.view.num_analytic};
     persistent_trace<true, COUNT>(n, &ps.cursors[MAX_DEPTH_SLOTS + k], io, status, work);
 }
 
@@ -931,7 +982,9 @@ static cudaError_t intersect_impl(const SceneView& s, const float4* rays, uint64
     if (!grid) grid = persistent_grid(k_intersect<ANY, COUNT>, 128);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(BatchIo{rays, hits, s.nodes, s.tris}, (uint32_t)n, counter, status,
+    k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(BatchIo{rays, hits, s.nodes, s.tris, s.analytic, s.num_analytic,
+                                                           s.num_tris, ANY},
+                                                   (uint32_t)n, counter, status,
                                                    work);
     return cudaGetLastError();
 }

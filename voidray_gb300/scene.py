@@ -259,10 +259,24 @@ class Surfaces:
         return Mesh(np.stack([_v(q1), _v(q2), _v(q3), _v(q4)]), [0, 1, 2, 2, 0, 3])
 
     @staticmethod
-    def sphere(center, radius):
-        raise VoidrayError(2, "analytic surfaces are not supported by the GPU path")
+    def sphere(center, radius) -> "AnalyticSurface":
+        """Sphere (surfaces.rs:31-80)."""
+        return AnalyticSurface(1, _v(center), float(f32(radius)), 0.0)
 
-    ground_plane = sphere
+    @staticmethod
+    def ground_plane(height) -> "AnalyticSurface":
+        """GroundPlane y = height (surfaces.rs:82-114)."""
+        return AnalyticSurface(2, np.zeros(3, np.float32), 0.0, float(f32(height)))
+
+
+@dataclass
+class AnalyticSurface:
+    """An analytic surface of the closed set the GPU path covers: kind 1
+    sphere (center, radius), kind 2 ground plane (height)."""
+    kind: int
+    center: np.ndarray
+    radius: float
+    height: float
 
 
 # ------------------------------------------------------------- environment --
@@ -352,8 +366,12 @@ class Scene:
         self.surfaces.append(len(self.meshes) - 1)
         return len(self.surfaces) - 1
 
-    def add_analytic_surface(self, surface) -> int:
-        raise VoidrayError(2, "analytic surfaces are not supported by the GPU path")
+    def add_analytic_surface(self, surface: "AnalyticSurface") -> int:
+        """scene.rs:110-116: analytic surfaces share the surface list with meshes."""
+        if not isinstance(surface, AnalyticSurface):
+            raise VoidrayError(2, "only Surfaces.sphere / Surfaces.ground_plane are supported by the GPU path")
+        self.surfaces.append(surface)
+        return len(self.surfaces) - 1
 
     def add_mesh_from_file(self, path: str) -> int:
         raise VoidrayError(2, "OBJ loading is not part of the GPU path; pass Mesh arrays")
@@ -385,11 +403,18 @@ class Scene:
         """Returns (vr_scene_desc, keepalive) for the native library."""
         mats = self.surface_materials()
         keep = []
-        meshes = (N.vr_mesh_desc * max(1, len(self.surfaces)))()
-        for s, mi in enumerate(self.surfaces):
+        mesh_surfs = [(s, x) for s, x in enumerate(self.surfaces) if isinstance(x, int)]
+        ana_surfs = [(s, x) for s, x in enumerate(self.surfaces) if not isinstance(x, int)]
+        meshes = (N.vr_mesh_desc * max(1, len(mesh_surfs)))()
+        anas = (N.vr_analytic_desc * max(1, len(ana_surfs)))()
+        for k, (s, a) in enumerate(ana_surfs):
+            anas[k].kind, anas[k].radius, anas[k].height, anas[k].material = a.kind, a.radius, a.height, mats[s]
+            for j in range(3):
+                anas[k].center[j] = float(a.center[j])
+        for k, (s, mi) in enumerate(mesh_surfs):
             m = self.meshes[mi]
             keep.append(m)
-            d = meshes[s]
+            d = meshes[k]
             d.positions = ptr(m.positions)
             d.normals = ptr(m.normals)
             d.uvs = ptr(m.uvs)
@@ -400,7 +425,9 @@ class Scene:
         cm = (N.vr_material * max(1, len(self.materials)))(*[m.to_c() for m in self.materials])
         desc = N.vr_scene_desc()
         desc.meshes = C.addressof(meshes)
-        desc.num_meshes = len(self.surfaces)
+        desc.num_meshes = len(mesh_surfs)
+        desc.analytics = C.addressof(anas)
+        desc.num_analytics = len(ana_surfs)
         desc.materials = C.addressof(cm)
         desc.num_materials = len(self.materials)
         env = self.environment
@@ -416,7 +443,7 @@ class Scene:
         desc.camera = self.camera.to_c()
         desc.bvh_max_leaf = bvh_max_leaf
         desc.bvh_bins = bvh_bins
-        keep += [meshes, cm]
+        keep += [meshes, cm, anas]
         return desc, keep
 
     def validate(self, **kw) -> N.vr_scene_info:

@@ -22,7 +22,8 @@ import math
 
 import numpy as np
 
-from .scene import (Camera, Environments, Estimator, Materials, Mesh, RenderSettings, Scene, degrees_to_radians)
+from .scene import (Camera, Environments, Estimator, Materials, Mesh, RenderSettings, Scene, Surfaces,
+                    degrees_to_radians)
 
 f32 = np.float32
 
@@ -281,5 +282,32 @@ def displaced_icosphere_scene(freq: int = 316, seed: int = 2, patch: int = 64, h
         s.environment = Environments.hdri_image(sky_hdri(*hdri_size), importance_sample=True)
     s.camera = Camera.look_at((0.0, 0.35, 3.4), (0.0, -0.15, 0.0), (0.0, 1.0, 0.0), degrees_to_radians(50.0))
     st = RenderSettings(total_samples=256, max_bounces=12, rr_depth=3, estimator=Estimator.NEE,
+                        firefly_clamp=float("inf"))
+    return s, st
+
+
+def spheres_scene(ground: bool = True, hdri: bool = False, seed: int = 3):
+    """A few analytic spheres (Lambertian, metal, dielectric, emitter) over a
+    ground plane and a small triangle box, the kind of scene the reference's
+    Surfaces::sphere / ground_plane build (voidray_common/src/surfaces.rs)."""
+    rng = np.random.default_rng(seed)
+    s = Scene()
+    grey = s.add_material(Materials.lambertian((0.6, 0.6, 0.6)))
+    mats = [s.add_material(Materials.lambertian((0.8, 0.3, 0.2))),
+            s.add_material(Materials.metal((0.9, 0.85, 0.7), 0.1)),
+            s.add_material(Materials.dielectric(1.5)),
+            s.add_material(Materials.colored_emissive((4.0, 3.0, 2.0), 1.0))]
+    if ground:
+        s.add_object(grey, s.add_analytic_surface(Surfaces.ground_plane(-1.0)))
+    for k in range(6):
+        c = (float(rng.uniform(-2, 2)), float(rng.uniform(-0.7, 0.5)), float(rng.uniform(-2.5, 0.5)))
+        s.add_object(mats[k % 4], s.add_analytic_surface(Surfaces.sphere(c, float(rng.uniform(0.2, 0.5)))))
+    s.add_object(grey, s.add_mesh(_box_mesh((0.9, -0.6, -1.0), (0.6, 0.8, 0.6), 20.0)))
+    if hdri:
+        s.environment = Environments.hdri_image(sky_hdri(128, 64, peak=200.0, sigma_deg=4.0))
+    else:
+        s.environment = Environments.uniform((0.5, 0.6, 0.8))
+    s.camera = Camera.look_at((0.0, 0.6, 4.0), (0.0, -0.3, -0.8), (0.0, 1.0, 0.0), degrees_to_radians(55.0))
+    st = RenderSettings(total_samples=16, max_bounces=8, rr_depth=0, estimator=Estimator.REFERENCE,
                         firefly_clamp=float("inf"))
     return s, st
