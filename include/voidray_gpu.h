@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define VR_ABI_VERSION 2
+#define VR_ABI_VERSION 3
 
 typedef enum vr_status {
     VR_OK = 0,
@@ -76,6 +76,11 @@ typedef struct vr_material {
     float emittance;    /* microfacet (stored, unused by its scatter, as in the
                            reference)                                           */
     int32_t transparent;/* microfacet                                           */
+    int32_t albedo_texture;  /* Lambertian: ColorType::Texture (simple.rs:83-133),
+                                index into vr_scene_desc.textures, -1 = color */
+    int32_t normal_texture;  /* Lambertian: normal map (its raw RGB replaces the
+                                shading normal of the scatter, simple.rs:109-113),
+                                -1 = none                                        */
 } vr_material;
 
 /* One triangle mesh: Mesh::from_buffers (voidray_renderer/src/core/mesh.rs:76-116).
@@ -120,6 +125,23 @@ typedef struct vr_camera_desc {
     float focal_point[3];
 } vr_camera_desc;
 
+/* ImageTexture (voidray_renderer/src/core/texture.rs:28-98): RGB f32, row 0
+ * first; sample(u, v) wraps u, v into [0, 1) as the reference does and reads
+ * the texel nearest to (u W, (1 - v) H) or blends the four around it, with
+ * the reference's linear-index modulo at the edges. */
+typedef enum vr_texture_sampling {
+    VR_TEX_NEAREST = 0,
+    VR_TEX_BILINEAR = 1
+} vr_texture_sampling;
+
+typedef struct vr_texture_desc {
+    const float* image;       /* width * height * 3 f32                           */
+    uint32_t width;
+    uint32_t height;
+    int32_t sampling;         /* vr_texture_sampling                              */
+    int32_t pad_;
+} vr_texture_desc;
+
 /* Analytic surfaces (voidray_common/src/surfaces.rs:31-114): Surfaces::sphere
  * (quadratic, normal (p - c) / r, uv 0) and Surfaces::ground_plane (y =
  * height, normal +y, uv (x, z)).  Tested against every ray beside the
@@ -149,7 +171,8 @@ typedef struct vr_scene_desc {
     uint32_t bvh_bins;      /* 0 = default (16)                                 */
     const vr_analytic_desc* analytics;  /* may be NULL when num_analytics == 0  */
     uint32_t num_analytics;             /* at most VR_MAX_ANALYTICS             */
-    uint32_t pad_;
+    uint32_t num_textures;
+    const vr_texture_desc* textures;    /* may be NULL when num_textures == 0   */
 } vr_scene_desc;
 #define VR_MAX_ANALYTICS 64
 

@@ -42,7 +42,12 @@ class orc_object(C.Structure):
 class orc_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("fuzz", C.c_float), ("ir", C.c_float),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("emittance", C.c_float),
-                ("transparent", C.c_int32)]
+                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32)]
+
+
+class orc_texture(C.Structure):
+    _fields_ = [("image", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("sampling", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 class orc_env(C.Structure):
@@ -59,7 +64,7 @@ class orc_scene_desc(C.Structure):
     _fields_ = [("meshes", C.c_void_p), ("num_meshes", C.c_uint32), ("num_materials", C.c_uint32),
                 ("materials", C.c_void_p), ("objects", C.c_void_p), ("num_objects", C.c_uint32),
                 ("pad_", C.c_uint32), ("env", orc_env), ("camera", orc_camera), ("analytics", C.c_void_p),
-                ("num_analytics", C.c_uint32), ("pad2_", C.c_uint32)]
+                ("num_analytics", C.c_uint32), ("num_textures", C.c_uint32), ("textures", C.c_void_p)]
 
 
 class orc_settings(C.Structure):
@@ -137,11 +142,17 @@ class OracleScene:
                 c.color[k] = float(m.color[k])
             c.fuzz, c.ir, c.roughness, c.metallic = m.fuzz, m.ir, m.roughness, m.metallic
             c.emittance, c.transparent = m.emittance, int(m.transparent)
-        keep.append(anas)
+            c.albedo_texture, c.normal_texture = m.albedo_texture, m.normal_texture
+        texs = (orc_texture * max(1, len(scene.textures)))()
+        for i, t in enumerate(scene.textures):
+            keep.append(t.image)
+            texs[i] = orc_texture(_p(t.image), t.image.shape[1], t.image.shape[0], int(t.sample_type), 0)
+        keep += [anas, texs]
         objs = (orc_object * max(1, len(scene.objects)))(*[orc_object(o.surface, o.material) for o in scene.objects])
         d = orc_scene_desc()
         d.meshes, d.num_meshes = C.addressof(meshes), n
         d.analytics, d.num_analytics = C.addressof(anas), len(ana_surfs)
+        d.textures, d.num_textures = C.addressof(texs), len(scene.textures)
         d.materials, d.num_materials = C.addressof(mats), len(scene.materials)
         d.objects, d.num_objects = C.addressof(objs), len(scene.objects)
         env = scene.environment

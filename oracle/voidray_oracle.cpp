@@ -240,6 +240,7 @@ int bvh_build(Bvh& bvh, std::vector<uint32_t>& objects, const BoundsFn& bounds_r
 // ----------------------------------------------------------------- scene --
 struct Hit {
     V3 point, normal;
+    V3 snormal;     // normal of the Lambertian scatter: the normal map's RGB when there is one
     float t;
     float uvx, uvy;
     bool front_face;
@@ -250,6 +251,7 @@ struct Hit {
 inline void make_hit(Hit& h, V3 point, V3 outward, float t, float ux, float uy, const Ray& r) {
     h.front_face = dot(r.d, outward) < 0.0f;
     h.normal = h.front_face ? outward : -outward;
+    h.snormal = h.normal;
     h.point = point;
     h.t = t;
     h.uvx = ux;
@@ -279,9 +281,16 @@ struct Analytic {
     int surface;
 };
 
+struct Texture {
+    uint32_t w = 0, h = 0;
+    int sampling = 0;  // 0 nearest, 1 bilinear
+    std::vector<float> img;
+};
+
 struct Scene {
     std::vector<Mesh> meshes;
     std::vector<Analytic> analytics;
+    std::vector<Texture> textures;
     std::vector<int> mesh_surface;      // surface index of each mesh
     std::vector<int> surf_mesh;         // per surface: mesh index or -1
     std::vector<int> surf_analytic;     // per surface: analytic index or -1
@@ -727,10 +736,36 @@ bool micro_sample(const orc_material& m, V3 n, V3 wo, Pcg32& rng, V3* wi_out, fl
 
 // Material::scatter for the closed set (simple.rs, traits.rs:19-41).
 // Returns true if a continuation ray was produced.
+// ImageTexture::sample (texture.rs:82-98) with nearest_sample / bilinear_sample (:52-78)
+V3 tex_sample(const Scene& s, int tix, float u, float v) {
+    const Texture& t = s.textures[tix];
+    const size_t W = t.w, H = t.h, len = W * H;
+    auto px = [&](size_t i) { return v3(t.img[3 * i], t.img[3 * i + 1], t.img[3 * i + 2]); };
+    if (u < 0.0f) u -= std::trunc(u) - 1.0f;
+    if (v < 0.0f) v -= std::trunc(v) - 1.0f;
+    const float x = std::fmod(u, 1.0f) * (float)W;
+    const float y = (1.0f - std::fmod(v, 1.0f)) * (float)H;
+    const size_t x0 = std::min(sat_usize(x), W - 1), y0 = std::min(sat_usize(y), H - 1);
+    if (t.sampling == 0) return px((y0 * W + x0) % len);
+    const float ax = x - (float)x0, ay = y - (float)y0;
+    return lerp3(lerp3(px((y0 * W + x0) % len), px((y0 * W + x0 + 1) % len), ax),
+                 lerp3(px(((y0 + 1) * W + x0) % len), px(((y0 + 1) * W + x0 + 1) % len), ax), ay);
+}
+// Lambertian textures (simple.rs:102-133): the albedo and the scatter normal from the hit's uv
+void apply_textures(const Scene& s, orc_material& m, Hit& hit) {
+    if (m.albedo_texture >= 0) {
+        V3 c = tex_sample(s, m.albedo_texture, hit.uvx, hit.uvy);
+        m.color[0] = c.x;
+        m.color[1] = c.y;
+        m.color[2] = c.z;
+    }
+    if (m.normal_texture >= 0) hit.snormal = tex_sample(s, m.normal_texture, hit.uvx, hit.uvy);
+}
+
 bool scatter(const orc_material& m, const Ray& ray, const Hit& hit, Pcg32& rng, V3* att, Ray* out) {
     switch (m.kind) {
     case M_LAMB: {  // simple.rs:102-133
-        V3 normal = hit.normal;
+        V3 normal = hit.snormal;
         V3 dir = normal + unit_sphere(rng);
         if (near_zero(dir)) dir = normal;
         *out = Ray{hit.point, normalize(dir)};
@@ -840,8 +875,9 @@ V3 trace_ref(const Scene& s, const orc_settings& st, const Ray& ray, uint32_t de
         c.extend++;
         HitPair hp = scene_hit(s, ray);
         if (!hp.ok) return env_eval(s, ray.d);
-        const Hit& hit = hp.best;
-        const orc_material& m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        Hit hit = hp.best;
+        orc_material m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        apply_textures(s, m, hit);
         V3 att;
         Ray sc;
         bool has;
@@ -887,14 +923,16 @@ V3 trace_nee(const Scene& s, const orc_settings& st, Ray ray, Pcg32& rng, Counte
             L = L + clampc(mul(T, le) * w, st.firefly_clamp);
             break;
         }
-        const Hit& hit = hp.best;
-        const orc_material& m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        Hit hit = hp.best;
+        orc_material m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        apply_textures(s, m, hit);
         if (st.render_mode != 1) {
             V3 nn = normalize(hit.normal);
             L = L + clampc(mul(T, (0.5f * nn) + v3(1, 1, 1) * 0.5f), st.firefly_clamp);
             break;
         }
-        const bool lamb = (m.kind == M_LAMB) && !(hit.normal.x == 0.0f && hit.normal.y == 0.0f && hit.normal.z == 0.0f);
+        const bool lamb = (m.kind == M_LAMB) && m.normal_texture < 0 &&
+                          !(hit.normal.x == 0.0f && hit.normal.y == 0.0f && hit.normal.z == 0.0f);
         if (lamb && env_is) {
             float u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform(), u4 = rng.uniform();
             V3 dl;
@@ -1003,6 +1041,21 @@ orc_scene* orc_scene_create(const orc_scene_desc* d) {
     std::unique_ptr<orc_scene> h(new orc_scene());
     Scene& s = h->s;
     s.materials.assign(d->materials, d->materials + d->num_materials);
+    for (uint32_t i = 0; i < d->num_textures; ++i) {
+        const orc_texture& td = d->textures[i];
+        if (!td.image || !td.width || !td.height) { g_err = "empty texture"; return nullptr; }
+        Texture t;
+        t.w = td.width;
+        t.h = td.height;
+        t.sampling = td.sampling;
+        t.img.assign(td.image, td.image + 3 * (size_t)td.width * td.height);
+        s.textures.push_back(std::move(t));
+    }
+    for (const orc_material& m : s.materials)
+        if (m.albedo_texture >= (int)d->num_textures || m.normal_texture >= (int)d->num_textures) {
+            g_err = "texture index out of range";
+            return nullptr;
+        }
     uint64_t prim = 0;
     for (uint32_t mi = 0; mi < d->num_meshes; ++mi) {
         const orc_mesh& md = d->meshes[mi];

@@ -62,7 +62,13 @@ typedef struct orc_object { uint32_t surface; uint32_t material; } orc_object;
 typedef struct orc_material {
     int32_t kind; float color[3]; float fuzz; float ir; float roughness;
     float metallic; float emittance; int32_t transparent;
+    int32_t albedo_texture; int32_t normal_texture;  /* -1: none */
 } orc_material;
+
+/* ImageTexture (voidray_renderer/src/core/texture.rs) */
+typedef struct orc_texture {
+    const float* image; uint32_t width; uint32_t height; int32_t sampling; int32_t pad_;
+} orc_texture;
 
 typedef struct orc_env {
     int32_t kind; float color[3]; const float* image; uint32_t width; uint32_t height;
@@ -80,7 +86,8 @@ typedef struct orc_scene_desc {
     const orc_object* objects; uint32_t num_objects; uint32_t pad_;
     orc_env env;
     orc_camera camera;
-    const orc_analytic* analytics; uint32_t num_analytics; uint32_t pad2_;
+    const orc_analytic* analytics; uint32_t num_analytics; uint32_t num_textures;
+    const orc_texture* textures;
 } orc_scene_desc;
 
 typedef struct orc_settings {

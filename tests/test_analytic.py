@@ -60,3 +60,18 @@ def test_surface_index_quirk_covers_analytic_surfaces(oracle):
     s.add_object(b, s1)   # object 0 (for surface 1) ...
     s.add_object(a, s0)   # ... but surface 0 renders with objects[0].material = b
     assert s.surface_materials() == [b, a]
+
+
+def test_textured_scene_lowers_and_checks_indices(native, oracle):
+    s, st = W.textured_scene()
+    assert s.validate().num_triangles == 4
+    o, _ = oracle.OracleScene(s).render(st, 2, 24, 16)
+    assert np.all(np.isfinite(o))
+    bad, _ = W.textured_scene()
+    bad.materials[0].albedo_texture = 7
+    with pytest.raises(vr.VoidrayError):
+        bad.validate()
+    metal, _ = W.textured_scene()
+    metal.materials[0].kind = 1   # only Lambertian takes textures
+    with pytest.raises(vr.VoidrayError):
+        metal.validate()

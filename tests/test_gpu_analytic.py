@@ -60,3 +60,25 @@ def test_spheres_nee_hdri(gpu, oracle):
     o, _ = oracle.OracleScene(s).render(st, 8, 64, 48)
     assert close_fraction(g, o) >= 0.95
     assert relmse(g, o) < 1e-3
+
+
+@pytest.mark.parametrize("rr", [0, 3])
+def test_textured_render_bit_parity(gpu, oracle, rr):
+    """Image textures (nearest and bilinear, uvs outside [0, 1]), a normal map
+    and a textured ground plane, against the oracle's texture.rs restatement."""
+    s, st = W.textured_scene()
+    st = RenderSettings(**{**st.__dict__, "rr_depth": rr})
+    g = gpu_render(s, st, 8, 64, 48)
+    o, _ = oracle.OracleScene(s).render(st, 8, 64, 48)
+    assert exact_fraction(g, o) >= 0.99
+    assert relmse(g, o) < 1e-4
+
+
+def test_textured_nee_matches_reference_estimator_in_expectation(gpu):
+    """NEE skips the normal-mapped vertices (their scatter is not cosine
+    distributed); both estimators converge to the same image."""
+    s, st = W.textured_scene()
+    ref = gpu_render(s, st, 512, 32, 24, seed=1)
+    nee = gpu_render(s, RenderSettings(**{**st.__dict__, "estimator": Estimator.NEE, "rr_depth": 3}), 512, 32, 24,
+                     seed=2)
+    assert relmse(nee, ref) < 5e-3

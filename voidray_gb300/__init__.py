@@ -6,12 +6,12 @@ camera, material and settings API on top of it.
 """
 from ._native import EXPORTED, VR_MISS, VoidrayError, lib
 from .renderer import Renderer, RenderAction, RendererStats
-from .scene import (AnalyticSurface, Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
+from .scene import (AnalyticSurface, ImageTexture, SampleType, Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
                     Materials, Mesh, MicrofacetBSDF, RenderMode, RenderSettings, Scene, SceneAcceleration, Settings,
                     Surfaces, Tonemap, Vertex, degrees_to_radians, hex_color, iterative_render, render_device, tonemap)
 
 __all__ = [
-    "EXPORTED", "VR_MISS", "VoidrayError", "lib", "AnalyticSurface", "Camera", "ColorManagementSettings", "CpuRenderTarget",
+    "EXPORTED", "VR_MISS", "VoidrayError", "lib", "AnalyticSurface", "ImageTexture", "SampleType", "Camera", "ColorManagementSettings", "CpuRenderTarget",
     "Environment", "Environments", "Estimator", "Material", "Materials", "Mesh", "MicrofacetBSDF", "RenderMode",
     "RenderSettings", "Scene", "SceneAcceleration", "Settings", "Surfaces", "Tonemap", "Vertex",
     "degrees_to_radians", "hex_color", "iterative_render", "render_device", "tonemap", "Renderer", "RenderAction",

@@ -32,7 +32,12 @@ class VoidrayError(RuntimeError):
 class vr_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("fuzz", C.c_float), ("ir", C.c_float),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("emittance", C.c_float),
-                ("transparent", C.c_int32)]
+                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32)]
+
+
+class vr_texture_desc(C.Structure):
+    _fields_ = [("image", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("sampling", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 class vr_mesh_desc(C.Structure):
@@ -60,7 +65,7 @@ class vr_scene_desc(C.Structure):
     _fields_ = [("meshes", C.c_void_p), ("num_meshes", C.c_uint32), ("num_materials", C.c_uint32),
                 ("materials", C.c_void_p), ("environment", vr_environment_desc), ("camera", vr_camera_desc),
                 ("bvh_max_leaf", C.c_uint32), ("bvh_bins", C.c_uint32), ("analytics", C.c_void_p),
-                ("num_analytics", C.c_uint32), ("pad_", C.c_uint32)]
+                ("num_analytics", C.c_uint32), ("num_textures", C.c_uint32), ("textures", C.c_void_p)]
 
 
 class vr_scene_info(C.Structure):

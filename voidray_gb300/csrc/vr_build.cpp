@@ -270,6 +270,35 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             err = "material " + std::to_string(i) + ": unsupported kind";
             return VR_ERR_UNSUPPORTED;
         }
+        const Material& mt = hs.materials[i];
+        for (int32_t tix : {mt.albedo_tex, mt.normal_tex})
+            if (tix < -1 || tix >= (int32_t)d->num_textures) {
+                err = "material " + std::to_string(i) + ": texture index out of range";
+                return VR_ERR_INVALID;
+            }
+        if ((mt.albedo_tex >= 0 || mt.normal_tex >= 0) && mt.kind != M_LAMB) {
+            err = "material " + std::to_string(i) + ": only Lambertian materials take textures";
+            return VR_ERR_UNSUPPORTED;
+        }
+    }
+    // image textures (texture.rs:28-98)
+    if (d->num_textures && !d->textures) { err = "textures is NULL"; return VR_ERR_INVALID; }
+    hs.tex_info.clear();
+    hs.texels.clear();
+    for (uint32_t i = 0; i < d->num_textures; ++i) {
+        const vr_texture_desc& t = d->textures[i];
+        if (!t.image || !t.width || !t.height) {
+            err = "texture " + std::to_string(i) + ": empty image";
+            return VR_ERR_INVALID;
+        }
+        if (t.sampling != VR_TEX_NEAREST && t.sampling != VR_TEX_BILINEAR) {
+            err = "texture " + std::to_string(i) + ": unknown sampling";
+            return VR_ERR_INVALID;
+        }
+        const size_t n = 3 * (size_t)t.width * t.height;
+        if (hs.texels.size() + n >= (size_t)INT32_MAX) { err = "textures too large"; return VR_ERR_INVALID; }
+        hs.tex_info.push_back(make_int4((int)hs.texels.size(), (int)t.width, (int)t.height, t.sampling));
+        hs.texels.insert(hs.texels.end(), t.image, t.image + n);
     }
     uint64_t np = 0;
     bool any_uv = false;
@@ -473,6 +502,7 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     }
     v.num_analytic = d->num_analytics;
     v.num_tris = (uint32_t)np;
+    v.num_textures = d->num_textures;
     set_camera(v, d->camera);
     hs.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return VR_OK;

@@ -529,6 +529,8 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if ((st = upload(s, hs.uvs, &s->view.uvs)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.materials, &s->view.materials)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.analytic, &s->view.analytic)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.tex_info, &s->view.tex_info)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.texels, &s->view.texels)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.env_img, &s->view.env_img)) != VR_OK) return cleanup(st);
     if (hs.has_tables) {
         if ((st = upload(s, hs.tables.marginal, &s->view.env_marg)) != VR_OK) return cleanup(st);

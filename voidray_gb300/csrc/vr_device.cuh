@@ -29,6 +29,7 @@ struct Material {  // same layout as vr_material
     float color[3];
     float fuzz, ir, roughness, metallic, emittance;
     int32_t transparent;
+    int32_t albedo_tex, normal_tex;  // -1: none
 };
 
 // Flattened BVH2: node = 4 x float4 (64 bytes)
@@ -55,6 +56,11 @@ struct SceneView {
     const float4* analytic;
     uint32_t num_analytic;
     uint32_t num_tris;
+    // image textures: per texture (texel offset, width, height, sampling) as
+    // int bits; texels RGB f32
+    const int4* tex_info;
+    const float* texels;
+    uint32_t num_textures;
     // environment
     int32_t env_kind;
     float env_color[3];

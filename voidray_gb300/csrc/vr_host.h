@@ -30,6 +30,8 @@ struct HostScene {
     std::vector<float2> uvs;    // 3 per prim, empty if no mesh has uvs
     std::vector<Material> materials;
     std::vector<float4> analytic;  // 2 per analytic surface
+    std::vector<int4> tex_info;    // per texture: texel offset, width, height, sampling
+    std::vector<float> texels;
     std::vector<float> env_img;
     EnvTables tables;
     bool has_tables = false;

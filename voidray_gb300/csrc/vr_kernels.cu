@@ -141,6 +141,7 @@ __device__ float env_pdf(const SceneView& s, V3 d) {
 // ----------------------------------------------------------------------------
 struct SurfHit {
     V3 point, normal;
+    V3 snormal;  // normal the Lambertian scatter uses (the normal map's raw RGB when there is one)
     float t;
     bool front;
 };
@@ -154,6 +155,25 @@ __device__ __forceinline__ V3 local_to_world_mul(V3 n, V3 h) {  // math.rs:50-60
     V3 nss = cross(n, ns);
     return v3(dot(ns, h), dot(nss, h), dot(n, h));
 }
+// ImageTexture::sample (texture.rs:82-98): u, v wrapped into [0, 1) the
+// reference's way, then nearest_sample (:52-57) or bilinear_sample (:59-78),
+// both with the linear-index modulo at the edges.
+__device__ V3 tex_sample(const SceneView& s, int32_t tix, float u, float v) {
+    const int4 ti = __ldg(s.tex_info + tix);
+    const size_t W = (uint32_t)ti.y, H = (uint32_t)ti.z, len = W * H;
+    const float* img = s.texels + ti.x;
+    if (u < 0.0f) u -= truncf(u) - 1.0f;
+    if (v < 0.0f) v -= truncf(v) - 1.0f;
+    const float x = fmodf(u, 1.0f) * (float)W;
+    const float y = (1.0f - fmodf(v, 1.0f)) * (float)H;
+    const size_t x0 = min(sat_usize(x), W - 1), y0 = min(sat_usize(y), H - 1);
+    if (ti.w == 0) return env_px(img, (y0 * W + x0) % len);
+    const float ax = x - (float)x0, ay = y - (float)y0;
+    return lerp3(lerp3(env_px(img, (y0 * W + x0) % len), env_px(img, (y0 * W + x0 + 1) % len), ax),
+                 lerp3(env_px(img, ((y0 + 1) * W + x0) % len), env_px(img, ((y0 + 1) * W + x0 + 1) % len), ax),
+                 ay);
+}
+
 __device__ __forceinline__ float lerpf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 __device__ __forceinline__ float signum_f(float x) {
     if (isnan(x)) return x;
@@ -266,8 +286,8 @@ __device__ bool micro_sample(const Material& m, V3 n, V3 wo, Rng& rng, V3* wi_ou
 __device__ bool scatter(const Material& m, V3 ro, V3 rd, const SurfHit& hit, Rng& rng, V3* att, V3* out_dir) {
     switch (m.kind) {
     case M_LAMB: {
-        V3 dir = hit.normal + unit_sphere(rng);
-        if (near_zero(dir)) dir = hit.normal;
+        V3 dir = hit.snormal + unit_sphere(rng);
+        if (near_zero(dir)) dir = hit.snormal;
         *out_dir = normalize(dir);
         *att = load3(m.color);
         return true;
@@ -605,6 +625,7 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                 const V3 point = ro + rd * t;
                 Material m;
                 V3 normal;
+                float uvx = 0.0f, uvy = 0.0f;  // HitRecord::uv
                 if (prim < s.num_tris) {
                     // shading record and normal (mesh.rs:176-188, ray.rs:34-49)
                     const float4* sh = s.shade + 4 * (size_t)prim;
@@ -616,19 +637,38 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                     const V3 fnm = xyz(s3);
                     const float ang = acosf(dot(normal, fnm) / (sqrtf(mag2(normal)) * sqrtf(mag2(fnm))));
                     if (ang > 30.0f * PI_F / 180.0f) normal = fnm;
+                    if (s.uvs && s.num_textures) {  // u v1.uv + v v2.uv + (1 - u - v) v0.uv (mesh.rs:177)
+                        const float2 t0 = __ldg(s.uvs + 3 * (size_t)prim), t1 = __ldg(s.uvs + 3 * (size_t)prim + 1),
+                                     t2 = __ldg(s.uvs + 3 * (size_t)prim + 2);
+                        uvx = u * t1.x + v * t2.x + wb * t0.x;
+                        uvy = u * t1.y + v * t2.y + wb * t0.y;
+                    }
                 } else {
-                    // analytic surface: sphere normal (p - c) / r, ground plane +y (surfaces.rs:74-75, 98-102)
+                    // analytic surface: sphere normal (p - c) / r, uv 0; ground plane +y, uv (x, z)
+                    // (surfaces.rs:74-75, 98-102)
                     const float4 a0 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris));
                     const float4 a1 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris) + 1);
                     m = s.materials[__float_as_uint(a1.y)];
-                    normal = __float_as_uint(a1.x) == A_SPHERE ? (point - v3(a0.x, a0.y, a0.z)) / a0.w
-                                                                : v3(0.0f, 1.0f, 0.0f);
+                    const bool sphere = __float_as_uint(a1.x) == A_SPHERE;
+                    normal = sphere ? (point - v3(a0.x, a0.y, a0.z)) / a0.w : v3(0.0f, 1.0f, 0.0f);
+                    if (!sphere) {
+                        uvx = point.x;
+                        uvy = point.z;
+                    }
                 }
                 SurfHit hit;
                 hit.point = point;
                 hit.t = t;
                 hit.front = dot(rd, normal) < 0.0f;
                 hit.normal = hit.front ? normal : -normal;
+                hit.snormal = hit.normal;
+                if (m.albedo_tex >= 0) {  // ColorType::Texture: the albedo is the texture at the hit's uv
+                    const V3 c = tex_sample(s, m.albedo_tex, uvx, uvy);
+                    m.color[0] = c.x;
+                    m.color[1] = c.y;
+                    m.color[2] = c.z;
+                }
+                if (m.normal_tex >= 0) hit.snormal = tex_sample(s, m.normal_tex, uvx, uvy);
                 if (k == 0 && j.aov_psum) {  // first-hit AOVs: surface colour (1 for glass), shading normal
                     const V3 al = (m.kind == M_DIEL) ? v3(1.0f, 1.0f, 1.0f)
                                                      : v3(fminf(m.color[0], 1.0f), fminf(m.color[1], 1.0f),
@@ -642,7 +682,9 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                     if (nee_mode) rad_add(ps, p, clampc(vmul(T, c), fc));
                     else unwind(ps, p, k, clampc(c, fc), fc);
                 } else {
-                    const bool lamb = (m.kind == M_LAMB) &&
+                    // next event estimation at Lambertian vertices whose scatter is
+                    // cosine-distributed around the shading normal (not with a normal map)
+                    const bool lamb = (m.kind == M_LAMB) && m.normal_tex < 0 &&
                                       !(hit.normal.x == 0.0f && hit.normal.y == 0.0f && hit.normal.z == 0.0f);
                     if (nee_mode && lamb && s.env_is) {
                         const float u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform(), u4 = rng.uniform();

@@ -132,6 +132,8 @@ class Material:
     metallic: float = 0.0
     emittance: float = 0.0
     transparent: bool = False
+    albedo_texture: int = -1   # TextureHandle of ColorType::Texture, -1: use `color`
+    normal_texture: int = -1   # TextureHandle of the normal map, -1: none
 
     def to_c(self) -> N.vr_material:
         m = N.vr_material()
@@ -140,7 +142,27 @@ class Material:
             m.color[i] = float(self.color[i])
         m.fuzz, m.ir, m.roughness = float(self.fuzz), float(self.ir), float(self.roughness)
         m.metallic, m.emittance, m.transparent = float(self.metallic), float(self.emittance), int(self.transparent)
+        m.albedo_texture, m.normal_texture = int(self.albedo_texture), int(self.normal_texture)
         return m
+
+
+class SampleType(enum.IntEnum):
+    """texture.rs:23-26."""
+    Nearest = 0
+    Bilinear = 1
+
+
+@dataclass
+class ImageTexture:
+    """ImageTexture (texture.rs:28-98) from a decoded RGB f32 image (H x W x 3,
+    row 0 first); file decoding is not on the GPU path."""
+    image: np.ndarray
+    sample_type: SampleType = SampleType.Bilinear
+
+    def __post_init__(self):
+        self.image = np.ascontiguousarray(self.image, dtype=np.float32)
+        if self.image.ndim != 3 or self.image.shape[2] != 3 or self.image.size == 0:
+            raise VoidrayError(1, "texture image must be H x W x 3")
 
 
 LAMBERTIAN, METAL, DIELECTRIC, EMISSION, LAMBERTIAN_BSDF, MICROFACET = range(6)
@@ -175,10 +197,14 @@ class Materials:
         return Material(EMISSION, (_v(color) * f32(strength)).astype(np.float32))
 
     @staticmethod
-    def lambertian_texture(*_a, **_k):
-        raise VoidrayError(2, "textured materials are not supported by the GPU path")
+    def lambertian_texture(albedo: int, normal: int) -> Material:
+        """simple.rs:36-41: albedo texture and normal map (TextureHandles)."""
+        return Material(LAMBERTIAN, np.zeros(3, np.float32), albedo_texture=int(albedo), normal_texture=int(normal))
 
-    lambertian_texture_no_normal = lambertian_texture
+    @staticmethod
+    def lambertian_texture_no_normal(albedo: int) -> Material:
+        """simple.rs:29-34."""
+        return Material(LAMBERTIAN, np.zeros(3, np.float32), albedo_texture=int(albedo))
 
 
 class MicrofacetBSDF:
@@ -351,6 +377,7 @@ class Scene:
         self.meshes: list[Mesh] = []
         self.surfaces: list[int] = []  # surface -> mesh index
         self.objects: list[Object] = []
+        self.textures: list[ImageTexture] = []
         self.environment: Optional[Environment] = None
 
     @staticmethod
@@ -360,6 +387,11 @@ class Scene:
     def add_material(self, material: Material) -> int:
         self.materials.append(material)
         return len(self.materials) - 1
+
+    def add_texture(self, texture: ImageTexture) -> int:
+        """scene.rs: textures are addressed by TextureHandle."""
+        self.textures.append(texture)
+        return len(self.textures) - 1
 
     def add_mesh(self, mesh: Mesh) -> int:
         self.meshes.append(mesh)
@@ -428,6 +460,13 @@ class Scene:
         desc.num_meshes = len(mesh_surfs)
         desc.analytics = C.addressof(anas)
         desc.num_analytics = len(ana_surfs)
+        texs = (N.vr_texture_desc * max(1, len(self.textures)))()
+        for i, t in enumerate(self.textures):
+            keep.append(t.image)
+            texs[i] = N.vr_texture_desc(ptr(t.image), t.image.shape[1], t.image.shape[0], int(t.sample_type), 0)
+        desc.textures = C.addressof(texs)
+        desc.num_textures = len(self.textures)
+        keep.append(texs)
         desc.materials = C.addressof(cm)
         desc.num_materials = len(self.materials)
         env = self.environment

@@ -311,3 +311,43 @@ def spheres_scene(ground: bool = True, hdri: bool = False, seed: int = 3):
     st = RenderSettings(total_samples=16, max_bounces=8, rr_depth=0, estimator=Estimator.REFERENCE,
                         firefly_clamp=float("inf"))
     return s, st
+
+
+def textured_scene(seed: int = 4):
+    """Lambertian quads with image textures (nearest and bilinear, uvs running
+    outside [0, 1] and negative to exercise the reference's wrapping), one
+    with a normal map, a textured ground plane (uv = world x, z) and a
+    sphere, under a uniform sky (texture.rs, simple.rs:83-133)."""
+    from .scene import ImageTexture, SampleType
+
+    rng = np.random.default_rng(seed)
+    s = Scene()
+    checker = ((np.indices((8, 8)).sum(0) % 2)[..., None] * np.array([0.7, 0.6, 0.2]) + 0.1).astype(f32)
+    noise = rng.uniform(0.05, 0.95, (13, 17, 3)).astype(f32)
+    nmap = np.zeros((4, 4, 3), f32)
+    nmap[..., 1] = 1.0
+    nmap[..., 0] = rng.uniform(-0.4, 0.4, (4, 4))
+    t_check = s.add_texture(ImageTexture(checker, SampleType.Nearest))
+    t_noise = s.add_texture(ImageTexture(noise, SampleType.Bilinear))
+    t_nmap = s.add_texture(ImageTexture(nmap, SampleType.Nearest))
+    m_check = s.add_material(Materials.lambertian_texture_no_normal(t_check))
+    m_noise = s.add_material(Materials.lambertian_texture(t_noise, t_nmap))
+    m_plain = s.add_material(Materials.lambertian((0.5, 0.5, 0.5)))
+    quads = [([(-2.0, -1.0, -2.0), (2.0, -1.0, -2.0), (2.0, 1.5, -2.0), (-2.0, 1.5, -2.0)],
+              [(-1.3, -0.7), (2.6, -0.7), (2.6, 1.9), (-1.3, 1.9)], m_noise),
+             ([(-2.0, -1.0, -2.0), (-2.0, 1.5, -2.0), (-2.0, 1.5, 1.0), (-2.0, -1.0, 1.0)],
+              [(0.0, 0.0), (0.0, 3.0), (3.0, 3.0), (3.0, 0.0)], m_check)]
+    for q, uv, m in quads:
+        pos = np.array(q, f32)
+        nrm = _face_normals(pos[0], pos[1], pos[2])
+        mesh = Mesh(pos, np.array([0, 1, 2, 2, 3, 0], np.uint32), np.repeat(nrm[None], 4, 0).astype(f32),
+                    np.array(uv, f32))
+        s.add_object(m, s.add_mesh(mesh))
+    ground = s.add_material(Materials.lambertian_texture_no_normal(t_noise))
+    s.add_object(ground, s.add_analytic_surface(Surfaces.ground_plane(-1.0)))
+    s.add_object(m_plain, s.add_analytic_surface(Surfaces.sphere((0.4, -0.4, -0.8), 0.6)))
+    s.environment = Environments.uniform((0.9, 0.95, 1.0))
+    s.camera = Camera.look_at((0.8, 0.5, 3.5), (-0.4, -0.2, -1.0), (0.0, 1.0, 0.0), degrees_to_radians(60.0))
+    st = RenderSettings(total_samples=8, max_bounces=6, rr_depth=0, estimator=Estimator.REFERENCE,
+                        firefly_clamp=float("inf"))
+    return s, st
