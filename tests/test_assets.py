@@ -1,0 +1,286 @@
+"""Host-side asset loaders (OBJ, PNG, EXR) on the CPU.  The PNG and EXR files
+are written by small encoders in this file, which follow the published
+formats independently of the decoders (forward filters, Adam7 pass split,
+OpenEXR chunk layout with RLE / ZIP predictor)."""
+import os
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from voidray_gb300 import assets as A
+from voidray_gb300._native import VoidrayError
+from voidray_gb300.scene import Mesh, Scene, ImageTexture, Environments, SampleType
+
+OBJ = """# comment line
+mtllib x.mtl
+o thing
+v 0 0 0
+v 1 0 0
+v 0 1 0 1.0
+v 1 1 0
+vt 0 0
+vt 1 0
+vt 0.5
+vt 1 1 0
+vn 0 0 1
+vn 0 0 -1
+s 1
+usemtl m
+f 1/1/1 2/2/1 3/3/1
+f 2/2/1 4/4/1 3/3/1   # shares two corners with the first face
+f -3/-3/-1 -1/-1/-1 -2/-2/-2   # the last corner is (3, 3, 1) again
+"""
+
+
+def test_obj_numbering_follows_first_use_of_each_triple():
+    pos, uv, nrm, idx = A.parse_obj(OBJ)
+    assert idx.tolist() == [[0, 1, 2], [1, 3, 2], [4, 5, 2]]
+    assert pos.tolist() == [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [1, 0, 0], [1, 1, 0]]
+    assert uv.tolist() == [[0, 0], [1, 0], [0.5, 0], [1, 1], [1, 0], [1, 1]]
+    assert nrm.tolist() == [[0, 0, 1]] * 4 + [[0, 0, -1]] * 2
+    assert pos.dtype == np.float32 and idx.dtype == np.uint32
+
+
+@pytest.mark.parametrize("face, what", [
+    ("f 1/1/1 2/1/1 3/1/1 1/1/1", "triangulated"),
+    ("f 1 2 3", "lacks"),
+    ("f 1//1 2//1 3//1", "lacks"),
+    ("f 1/1/1 2/1/1 9/1/1", "out of range"),
+    ("f 0/1/1 2/1/1 3/1/1", "out of range"),
+])
+def test_obj_rejects_what_texturedvertex_rejects(face, what):
+    text = "v 0 0 0\nv 1 0 0\nv 0 1 0\nvt 0 0\nvn 0 0 1\n" + face + "\n"
+    with pytest.raises(VoidrayError, match=what):
+        A.parse_obj(text)
+
+
+def test_mesh_from_file_and_scene(tmp_path):
+    p = tmp_path / "m.obj"
+    p.write_text(OBJ)
+    m = Mesh.from_file(str(p))
+    assert m.num_triangles == 3 and m.normals is not None and m.uvs is not None
+    s = Scene()
+    assert s.add_mesh_from_file(str(p)) == 0
+
+
+REF_ASSET = os.path.join(os.environ.get("VOIDRAY_REFERENCE", "/root/reference"), "assets", "mushroom.obj")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_ASSET), reason="reference assets not present")
+def test_obj_reads_a_blender_export():
+    """The reference's own demo mesh: every triangle corner carries the
+    position, uv and normal of the OBJ lines it names."""
+    with open(REF_ASSET) as f:
+        text = f.read()
+    pos, uv, nrm, idx = A.parse_obj(text)
+    lines = text.splitlines()
+    v = np.array([l.split()[1:4] for l in lines if l.startswith("v ")], np.float64).astype(np.float32)
+    vt = np.array([l.split()[1:3] for l in lines if l.startswith("vt ")], np.float64).astype(np.float32)
+    faces = [l.split()[1:] for l in lines if l.startswith("f ")]
+    assert len(idx) == len(faces) == 4448
+    for f, tri in zip(faces[::97], idx[::97]):
+        for corner, k in zip(f, tri):
+            pi, ti, _ = (int(x) - 1 for x in corner.split("/"))
+            assert np.array_equal(pos[k], v[pi]) and np.array_equal(uv[k], vt[ti])
+    assert len(np.unique(idx)) == len(pos)
+
+
+# -------------------------------------------------------------------- PNG ---
+def _png_chunk(kind: bytes, body: bytes) -> bytes:
+    return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body))
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    return a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+
+
+def _filter_rows(rows: np.ndarray, bpp: int) -> bytes:
+    """Forward PNG filters, cycling through the five types row by row."""
+    out = bytearray()
+    prev = np.zeros(rows.shape[1], np.int64)
+    for y, row in enumerate(rows.astype(np.int64)):
+        ft = y % 5
+        enc = []
+        for i, x in enumerate(row):
+            a = row[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            pred = [0, a, b, (a + b) >> 1, _paeth(a, b, c)][ft]
+            enc.append((x - pred) & 0xFF)
+        out.append(ft)
+        out += bytes(enc)
+        prev = row
+    return bytes(out)
+
+
+def _pack(samples: np.ndarray, depth: int) -> np.ndarray:
+    """[h, w*ch] integer samples -> [h, stride] bytes."""
+    h, n = samples.shape
+    if depth == 8:
+        return samples.astype(np.uint8)
+    if depth == 16:
+        s = samples.astype(np.uint16)
+        return np.stack([s >> 8, s & 0xFF], -1).reshape(h, 2 * n).astype(np.uint8)
+    bits = ((samples[..., None] >> np.arange(depth - 1, -1, -1)) & 1).reshape(h, n * depth).astype(np.uint8)
+    return np.packbits(bits, axis=1)
+
+
+def encode_png(samples: np.ndarray, depth: int, ctype: int, palette=None, interlace=False) -> bytes:
+    h, w, ch = samples.shape
+    bpp = max(1, ch * depth // 8)
+    raw = b""
+    passes = A._ADAM7 if interlace else [(0, 0, 1, 1)]
+    for x0, y0, dx, dy in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.size == 0:
+            continue
+        raw += _filter_rows(_pack(sub.reshape(sub.shape[0], -1), depth), bpp)
+    out = A._PNG_MAGIC + _png_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, int(interlace)))
+    if palette is not None:
+        out += _png_chunk(b"PLTE", palette.astype(np.uint8).tobytes())
+    z = zlib.compress(raw)
+    out += _png_chunk(b"IDAT", z[:len(z) // 2]) + _png_chunk(b"IDAT", z[len(z) // 2:])
+    return out + _png_chunk(b"IEND", b"")
+
+
+@pytest.mark.parametrize("depth, ctype, interlace", [
+    (8, 2, False), (8, 6, False), (16, 2, False), (16, 6, True), (8, 0, True), (1, 0, False),
+    (2, 0, False), (4, 0, True), (16, 0, False), (8, 4, False), (16, 4, True), (8, 3, False), (4, 3, True),
+])
+def test_png_decodes_like_to_rgb32f(depth, ctype, interlace):
+    rng = np.random.default_rng(depth * 10 + ctype)
+    h, w = 11, 13
+    ch = A._PNG_CHANNELS[ctype]
+    maxv = (1 << depth) - 1
+    samples = rng.integers(0, maxv + 1, (h, w, ch))
+    palette = rng.integers(0, 256, (1 << depth, 3)) if ctype == 3 else None
+    img = A.decode_png(encode_png(samples, depth, ctype, palette, interlace))
+    assert img.shape == (h, w, 3) and img.dtype == np.float32
+    if ctype == 3:
+        want = palette[samples[..., 0]].astype(np.float32) / np.float32(255)
+    else:
+        s = samples if depth >= 8 else samples * (255 // maxv)
+        full = np.float32(65535 if depth == 16 else 255)
+        col = s[..., :3] if ch >= 3 else np.repeat(s[..., :1], 3, -1)
+        want = col.astype(np.float32) / full
+    assert np.array_equal(img, want)
+
+
+def test_png_rejects_corruption():
+    data = bytearray(encode_png(np.zeros((2, 2, 3), int), 8, 2))
+    data[20] ^= 1  # inside IHDR: CRC no longer matches
+    with pytest.raises(VoidrayError, match="CRC"):
+        A.decode_png(bytes(data))
+
+
+# -------------------------------------------------------------------- EXR ---
+def _exr_attr(name, typ, value: bytes) -> bytes:
+    return name.encode() + b"\0" + typ.encode() + b"\0" + struct.pack("<i", len(value)) + value
+
+
+def _rle(b: bytes) -> bytes:
+    out, i = bytearray(), 0
+    while i < len(b):
+        j = i
+        while j + 1 < len(b) and b[j + 1] == b[i] and j - i < 126:
+            j += 1
+        if j > i:  # run of j-i+1 equal bytes
+            out += struct.pack("b", j - i) + b[i:i + 1]
+            i = j + 1
+        else:
+            k = i
+            while k < len(b) and k - i < 127 and not (k + 1 < len(b) and b[k + 1] == b[k]):
+                k += 1
+            k = max(k, i + 1)
+            out += struct.pack("b", -(k - i)) + b[i:k]
+            i = k
+    return bytes(out)
+
+
+def _predict(raw: bytes) -> bytes:
+    d = np.frombuffer(raw, np.uint8)
+    t = np.concatenate([d[0::2], d[1::2]]).astype(np.int64)
+    p = t.copy()
+    p[1:] = (t[1:] - t[:-1] + 128) & 0xFF
+    return p.astype(np.uint8).tobytes()
+
+
+def encode_exr(planes: dict, types: dict, comp: int, y_origin: int = 5) -> bytes:
+    names = sorted(planes)
+    h, w = planes[names[0]].shape
+    dts = {0: "<u4", 1: "<f2", 2: "<f4"}
+    ch = b"".join(n.encode() + b"\0" + struct.pack("<iB3xii", types[n], 0, 1, 1) for n in names) + b"\0"
+    box = struct.pack("<iiii", 2, y_origin, 2 + w - 1, y_origin + h - 1)
+    hdr = (_exr_attr("channels", "chlist", ch) + _exr_attr("compression", "compression", bytes([comp]))
+           + _exr_attr("dataWindow", "box2i", box) + _exr_attr("displayWindow", "box2i", box)
+           + _exr_attr("lineOrder", "lineOrder", b"\0") + _exr_attr("pixelAspectRatio", "float", struct.pack("<f", 1))
+           + b"\0")
+    lines = A._EXR_LINES[comp]
+    chunks = []
+    for y0 in range(0, h, lines):
+        raw = b"".join(planes[n][y].astype(dts[types[n]]).tobytes()
+                       for y in range(y0, min(h, y0 + lines)) for n in names)
+        if comp == 1:
+            data = _rle(_predict(raw))
+        elif comp in (2, 3):
+            data = zlib.compress(_predict(raw))
+        else:
+            data = raw
+        if len(data) >= len(raw):
+            data = raw
+        chunks.append(struct.pack("<ii", y_origin + y0, len(data)) + data)
+    head = struct.pack("<ii", A._EXR_MAGIC, 2) + hdr
+    table_end = len(head) + 8 * len(chunks)
+    offs, o = [], table_end
+    for c in chunks:
+        offs.append(o)
+        o += len(c)
+    return head + struct.pack(f"<{len(chunks)}Q", *offs) + b"".join(chunks)
+
+
+@pytest.mark.parametrize("comp", [0, 1, 2, 3])
+@pytest.mark.parametrize("ptype", [1, 2])
+def test_exr_scanline_round_trip(comp, ptype):
+    rng = np.random.default_rng(comp * 7 + ptype)
+    h, w = 37, 21
+    planes = {}
+    for c in "RGBA":
+        x = rng.gamma(0.7, 3.0, (h, w)).astype(np.float32)
+        x[:4] = 1.5  # flat rows: runs for RLE and chunks that compress
+        planes[c] = x.astype(np.float16).astype(np.float32) if ptype == 1 else x
+    types = {c: ptype for c in planes}
+    types["A"] = 1
+    img = A.decode_exr(encode_exr(planes, types, comp))
+    want = np.stack([planes["R"], planes["G"], planes["B"]], -1)
+    assert img.shape == (h, w, 3) and np.array_equal(img, want)
+
+
+def test_exr_rejects_unsupported():
+    p = {c: np.zeros((4, 4), np.float32) for c in "RGB"}
+    data = bytearray(encode_exr(p, {c: 2 for c in p}, 0))
+    i = data.index(b"compression\0compression\0") + len(b"compression\0compression\0") + 4
+    data[i] = 4  # PIZ
+    with pytest.raises(VoidrayError, match="not supported"):
+        A.decode_exr(bytes(data))
+    with pytest.raises(VoidrayError, match="needs R, G and B"):
+        A.decode_exr(encode_exr({"Y": np.zeros((2, 2), np.float32)}, {"Y": 2}, 0))
+
+
+def test_files_reach_textures_and_environments(tmp_path):
+    rgb = np.random.default_rng(3).integers(0, 256, (5, 6, 3))
+    (tmp_path / "t.png").write_bytes(encode_png(rgb, 8, 2))
+    (tmp_path / "e.exr").write_bytes(encode_exr({c: np.full((3, 4), i + 1.0, np.float32) for i, c in enumerate("RGB")},
+                                                {c: 2 for c in "RGB"}, 3))
+    (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff")
+    t = ImageTexture.from_file(str(tmp_path / "t.png"), SampleType.Nearest)
+    assert np.array_equal(t.image, rgb.astype(np.float32) / np.float32(255))
+    s = Scene()
+    assert s.add_image_texture(str(tmp_path / "t.png")) == 0
+    env = Environments.hdri(str(tmp_path / "e.exr"))
+    assert env.image.shape == (3, 4, 3) and env.image[0, 0].tolist() == [1.0, 2.0, 3.0]
+    with pytest.raises(VoidrayError, match="not decoded here"):
+        A.load_image_rgb32f(str(tmp_path / "x.jpg"))

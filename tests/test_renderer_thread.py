@@ -70,3 +70,106 @@ def test_cancel_stops_the_render_early(gpu, monkeypatch):
     r.wait(120)
     done, total = r.samples()
     assert 1 <= done < total and not r.currently_rendering()
+
+
+class _FakeAccel:
+    def destroy(self):
+        pass
+
+
+def _fake_render(calls):
+    """Stands in for the GPU call: adds a value that depends on the sample
+    range only, in float32 like the accumulator, and records the chunks."""
+    def render(target, accel, st, samples, seed=0, first_sample=0):
+        calls.append((first_sample, samples))
+        h, w = target.buffer.shape[:2]
+        idx = np.arange(first_sample, first_sample + samples, dtype=np.float64)
+        val = np.float32(np.sum(np.sin(idx * 0.37 + seed)) / st.total_samples)
+        target.buffer[...] += val + np.arange(h * w * 4, dtype=np.float32).reshape(h, w, 4) * np.float32(1e-3)
+    return render
+
+
+def _fake_renderer(monkeypatch, tmp_path, total, seed=3):
+    calls = []
+    monkeypatch.setattr(R, "iterative_render", _fake_render(calls))
+    monkeypatch.setattr(R, "chunk_size", lambda f, s, rem: 3)
+    scene, st = W.cornell_box()
+    monkeypatch.setattr(type(scene), "build_acceleration", lambda self: _FakeAccel())
+    st.total_samples = total
+    r = vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(5, 4), seed=seed,
+                    checkpoint_path=str(tmp_path / "ck.npz"))
+    return r, calls
+
+
+def test_checkpoint_resume_continues_the_chunk_sequence(monkeypatch, tmp_path):
+    full, calls_full = _fake_renderer(monkeypatch, tmp_path, 11)
+    full.execute(vr.RenderAction.RENDER)
+    full.wait(60)
+    assert calls_full == [(0, 1), (1, 3), (4, 3), (7, 3), (10, 3)]
+    ck = vr.Checkpoint.load(str(tmp_path / "ck.npz"))
+    assert (ck.samples, ck.total, ck.per_frame, ck.seed) == (11, 11, 3, 3)
+    assert np.array_equal(ck.buffer, full.target.buffer)
+
+    # stop after the chunk that ends at sample 7, then resume in a new renderer
+    part, calls = _fake_renderer(monkeypatch, tmp_path, 11)
+    orig = R.iterative_render
+
+    def stop_at_7(target, accel, st, samples, seed=0, first_sample=0):
+        orig(target, accel, st, samples, seed=seed, first_sample=first_sample)
+        if first_sample + samples == 7:
+            part.thread.execute(vr.RenderAction.CANCEL)
+    monkeypatch.setattr(R, "iterative_render", stop_at_7)
+    part.execute(vr.RenderAction.RENDER)
+    part.wait(60)
+    assert part.samples() == (7, 11)
+    monkeypatch.setattr(R, "iterative_render", orig)
+    resumed = vr.Renderer(part.scene, part.settings, vr.CpuRenderTarget(5, 4),
+                          checkpoint_path=str(tmp_path / "ck2.npz"))
+    resumed.resume(str(tmp_path / "ck.npz"))
+    resumed.wait(60)
+    assert calls == [(0, 1), (1, 3), (4, 3), (7, 3), (10, 3)]
+    assert resumed.samples() == (11, 11) and resumed.seed == 3
+    assert np.array_equal(resumed.target.buffer, full.target.buffer)
+
+
+def test_resume_rejects_a_mismatched_checkpoint(monkeypatch, tmp_path):
+    r, _ = _fake_renderer(monkeypatch, tmp_path, 5)
+    r.execute(vr.RenderAction.RENDER)
+    r.wait(60)
+    scene, st = W.cornell_box()
+    st.total_samples = 5
+    with pytest.raises(vr.VoidrayError, match="shape"):
+        vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(6, 4)).resume(str(tmp_path / "ck.npz"))
+    st.total_samples = 6
+    with pytest.raises(vr.VoidrayError, match="total samples"):
+        vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(5, 4)).resume(str(tmp_path / "ck.npz"))
+
+
+@pytest.mark.gpu
+def test_resumed_render_is_bit_identical(gpu, monkeypatch, tmp_path):
+    scene, st = W.cornell_box(rr_depth=3)
+    st.total_samples = 14
+    w, h = 40, 32
+    monkeypatch.setattr(R, "chunk_size", lambda f, s, rem: 3)
+    full = vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(w, h), seed=9)
+    full.execute(vr.RenderAction.RENDER)
+    full.wait(120)
+
+    ck_path = str(tmp_path / "ck.npz")
+    part = vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(w, h), seed=9, checkpoint_path=ck_path)
+    orig = R.iterative_render
+
+    def stop_at_7(target, accel, st_, samples, seed=0, first_sample=0):
+        orig(target, accel, st_, samples, seed=seed, first_sample=first_sample)
+        if first_sample + samples == 7:
+            part.thread.execute(vr.RenderAction.CANCEL)
+    monkeypatch.setattr(R, "iterative_render", stop_at_7)
+    part.execute(vr.RenderAction.RENDER)
+    part.wait(120)
+    monkeypatch.setattr(R, "iterative_render", orig)
+    assert part.samples() == (7, 14)
+    resumed = vr.Renderer(scene, vr.Settings(render=st), vr.CpuRenderTarget(w, h))
+    resumed.resume(ck_path)
+    resumed.wait(120)
+    assert resumed.samples() == (14, 14)
+    assert np.array_equal(resumed.target.buffer, full.target.buffer)

@@ -5,7 +5,7 @@ The compute path is the native library ``_lib/libvoidray_gb300.so`` (C ABI in
 camera, material and settings API on top of it.
 """
 from ._native import EXPORTED, VR_MISS, VoidrayError, lib
-from .renderer import Renderer, RenderAction, RendererStats
+from .renderer import Checkpoint, Renderer, RenderAction, RendererStats
 from .scene import (AnalyticSurface, ImageTexture, SampleType, Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
                     Materials, Mesh, MicrofacetBSDF, RenderMode, RenderSettings, Scene, SceneAcceleration, Settings,
                     Surfaces, Tonemap, Vertex, degrees_to_radians, hex_color, iterative_render, render_device, tonemap)
@@ -15,5 +15,5 @@ __all__ = [
     "Environment", "Environments", "Estimator", "Material", "Materials", "Mesh", "MicrofacetBSDF", "RenderMode",
     "RenderSettings", "Scene", "SceneAcceleration", "Settings", "Surfaces", "Tonemap", "Vertex",
     "degrees_to_radians", "hex_color", "iterative_render", "render_device", "tonemap", "Renderer", "RenderAction",
-    "RendererStats",
+    "RendererStats", "Checkpoint",
 ]

@@ -1,0 +1,349 @@
+"""Host-side asset loaders: the file formats voidray reads before a scene
+reaches the renderer.
+
+- `load_obj` follows `Mesh::from_file` (voidray_renderer/src/core/mesh.rs:46-74),
+  which calls `obj::load_obj::<TexturedVertex, u32>` of the obj-rs crate
+  (version 0.7.0 in the reference's Cargo.lock; not vendored).  The crate's
+  published behaviour for that vertex type is restated here: `v x y z [w]`,
+  `vt u [v [w]]` (missing components 0), `vn x y z`; face corners `p/t/n`
+  with 1-based indices, negative indices counting back from the current end
+  of their list; every face must be a triangle with all three of position,
+  texture and normal indices, else the load fails (the crate's
+  `UntriangulatedModel` / `InsufficientData` errors); each distinct
+  (position, normal, texture) index triple becomes one vertex, numbered in
+  order of first use; other statements (`o`, `g`, `s`, `usemtl`, `mtllib`,
+  `l`, `p`) do not change the mesh.  Numbers are parsed as f64 and rounded
+  to f32, which equals a direct decimal-to-f32 conversion for the short
+  decimals OBJ writers emit.
+- `load_image_rgb32f` follows `image::open(path).to_rgb32f()` as
+  `ImageTexture::new` (voidray_renderer/src/core/texture.rs:36-50) and
+  `HDRIEnvironment::new` (voidray_common/src/environments.rs:42-55) call it
+  (image 0.24): row 0 at the top, RGB f32, alpha dropped, grey replicated,
+  integer samples divided by their maximum (255 or 65535).  Formats read
+  here: PNG (every colour type and bit depth, Adam7 interlacing) and
+  OpenEXR scanline files with NONE, RLE, ZIPS or ZIP compression and HALF,
+  FLOAT or UINT channels.  JPEG and TIFF decoding and the other EXR
+  compressions are not restated; decode those elsewhere and pass float RGB
+  arrays (`Scene.add_texture`, `Environments.hdri`).
+"""
+from __future__ import annotations
+
+import os
+import struct
+import zlib
+
+import numpy as np
+
+from ._native import VoidrayError
+
+
+# -------------------------------------------------------------------- OBJ ---
+def _obj_index(tok: str, count: int, what: str, line: int) -> int:
+    try:
+        i = int(tok)
+    except ValueError:
+        raise VoidrayError(1, f"OBJ line {line}: bad {what} index {tok!r}") from None
+    j = count + i if i < 0 else i - 1
+    if i == 0 or not 0 <= j < count:
+        raise VoidrayError(1, f"OBJ line {line}: {what} index {i} out of range (have {count})")
+    return j
+
+
+def parse_obj(text: str):
+    """Returns (positions f32 [V,3], uvs f32 [V,2], normals f32 [V,3],
+    indices u32 [F,3]) with the obj-rs TexturedVertex numbering."""
+    pos: list[tuple[float, float, float]] = []
+    tex: list[tuple[float, float]] = []
+    nrm: list[tuple[float, float, float]] = []
+    cache: dict[tuple[int, int, int], int] = {}
+    order: list[tuple[int, int, int]] = []
+    indices: list[int] = []
+    for ln, raw in enumerate(text.splitlines(), 1):
+        line = raw.split("#", 1)[0].split()
+        if not line:
+            continue
+        key, args = line[0], line[1:]
+        try:
+            if key == "v":
+                if len(args) < 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: vertex needs 3 coordinates")
+                pos.append((float(args[0]), float(args[1]), float(args[2])))
+            elif key == "vt":
+                if not args:
+                    raise VoidrayError(1, f"OBJ line {ln}: texture coordinate needs u")
+                tex.append((float(args[0]), float(args[1]) if len(args) > 1 else 0.0))
+            elif key == "vn":
+                if len(args) < 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: normal needs 3 components")
+                nrm.append((float(args[0]), float(args[1]), float(args[2])))
+            elif key == "f":
+                if len(args) != 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: face with {len(args)} corners "
+                                          "(the model must be triangulated)")
+                for corner in args:
+                    parts = corner.split("/")
+                    if len(parts) != 3 or not parts[1] or not parts[2]:
+                        raise VoidrayError(1, f"OBJ line {ln}: face corner {corner!r} lacks texture "
+                                              "or normal indices")
+                    k = (_obj_index(parts[0], len(pos), "position", ln),
+                         _obj_index(parts[2], len(nrm), "normal", ln),
+                         _obj_index(parts[1], len(tex), "texture", ln))
+                    v = cache.get(k)
+                    if v is None:
+                        v = cache[k] = len(order)
+                        order.append(k)
+                    indices.append(v)
+        except ValueError:
+            raise VoidrayError(1, f"OBJ line {ln}: cannot parse {raw.strip()!r}") from None
+    n = len(order)
+    p = np.asarray(pos, np.float64).reshape(-1, 3)
+    t = np.asarray(tex, np.float64).reshape(-1, 2)
+    q = np.asarray(nrm, np.float64).reshape(-1, 3)
+    ix = np.asarray(order, np.int64).reshape(-1, 3)
+    positions = p[ix[:, 0]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
+    normals = q[ix[:, 1]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
+    uvs = t[ix[:, 2]].astype(np.float32) if n else np.zeros((0, 2), np.float32)
+    return positions, uvs, normals, np.asarray(indices, np.uint32).reshape(-1, 3)
+
+
+def load_obj(path: str):
+    with open(path, "r", encoding="utf-8", errors="replace") as f:
+        return parse_obj(f.read())
+
+
+# -------------------------------------------------------------------- PNG ---
+_PNG_MAGIC = b"\x89PNG\r\n\x1a\n"
+_ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+_PNG_CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
+
+
+def _paeth(a: int, b: int, c: int) -> int:
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def _png_unfilter(data: bytes, pos: int, rows: int, stride: int, bpp: int):
+    """Undoes the five PNG scanline filters; returns (uint8 [rows, stride], new pos)."""
+    out = np.zeros((rows, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    for y in range(rows):
+        ftype = data[pos]
+        line = np.frombuffer(data, np.uint8, stride, pos + 1).astype(np.int32)
+        pos += 1 + stride
+        if ftype == 0:
+            cur = line
+        elif ftype == 2:
+            cur = (line + prev) & 0xFF
+        elif ftype == 1:  # Sub: a running sum per byte lane of the pixel
+            cur = line.copy()
+            for k in range(min(bpp, stride)):
+                cur[k::bpp] = np.cumsum(line[k::bpp]) & 0xFF
+        elif ftype in (3, 4):  # Average and Paeth depend on the byte just decoded
+            lst = line.tolist()
+            up = prev.tolist()
+            for i in range(stride):
+                a = lst[i - bpp] if i >= bpp else 0
+                if ftype == 3:
+                    lst[i] = (lst[i] + ((a + up[i]) >> 1)) & 0xFF
+                else:
+                    lst[i] = (lst[i] + _paeth(a, up[i], up[i - bpp] if i >= bpp else 0)) & 0xFF
+            cur = np.asarray(lst, np.int32)
+        else:
+            raise VoidrayError(1, f"PNG: unknown filter type {ftype}")
+        out[y] = cur
+        prev = cur
+    return out, pos
+
+
+def _png_samples(rows: np.ndarray, width: int, depth: int, channels: int) -> np.ndarray:
+    """Unpacks filtered-out scanlines into integer samples [h, w, channels]."""
+    h = rows.shape[0]
+    if depth == 8:
+        return rows[:, :width * channels].reshape(h, width, channels).astype(np.uint16)
+    if depth == 16:
+        s = rows[:, :width * channels * 2].reshape(h, width * channels, 2).astype(np.uint16)
+        return ((s[..., 0] << 8) | s[..., 1]).reshape(h, width, channels)
+    bits = np.unpackbits(rows, axis=1)[:, :width * channels * depth].reshape(h, width * channels, depth)
+    weights = (1 << np.arange(depth - 1, -1, -1)).astype(np.uint16)
+    return (bits.astype(np.uint16) * weights).sum(-1).astype(np.uint16).reshape(h, width, channels)
+
+
+def decode_png(data: bytes) -> np.ndarray:
+    if data[:8] != _PNG_MAGIC:
+        raise VoidrayError(1, "PNG: bad signature")
+    pos, ihdr, idat, plte, trns = 8, None, [], None, None
+    while pos + 8 <= len(data):
+        length, ctype = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + length]
+        if len(body) != length:
+            raise VoidrayError(1, "PNG: truncated chunk")
+        if zlib.crc32(ctype + body) != struct.unpack(">I", data[pos + 8 + length:pos + 12 + length])[0]:
+            raise VoidrayError(1, f"PNG: CRC mismatch in {ctype!r}")
+        pos += 12 + length
+        if ctype == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif ctype == b"PLTE":
+            plte = np.frombuffer(body, np.uint8).reshape(-1, 3)
+        elif ctype == b"tRNS":
+            trns = body
+        elif ctype == b"IDAT":
+            idat.append(body)
+        elif ctype == b"IEND":
+            break
+    if ihdr is None:
+        raise VoidrayError(1, "PNG: no IHDR")
+    width, height, depth, ctype, comp, filt, interlace = ihdr
+    if ctype not in _PNG_CHANNELS or comp != 0 or filt != 0 or interlace not in (0, 1):
+        raise VoidrayError(1, f"PNG: unsupported header {ihdr}")
+    if ctype == 3 and plte is None:
+        raise VoidrayError(1, "PNG: palette image without PLTE")
+    ch = _PNG_CHANNELS[ctype]
+    raw = zlib.decompress(b"".join(idat))
+    bpp = max(1, ch * depth // 8)
+    img = np.zeros((height, width, ch), np.uint16)
+    passes = _ADAM7 if interlace else [(0, 0, 1, 1)]
+    p = 0
+    for x0, y0, dx, dy in passes:
+        pw = (width - x0 + dx - 1) // dx if width > x0 else 0
+        ph = (height - y0 + dy - 1) // dy if height > y0 else 0
+        if pw == 0 or ph == 0:
+            continue
+        stride = (pw * ch * depth + 7) // 8
+        rows, p = _png_unfilter(raw, p, ph, stride, bpp)
+        img[y0::dy, x0::dx] = _png_samples(rows, pw, depth, ch)
+    if ctype == 3:
+        return plte[img[..., 0]].astype(np.float32) / np.float32(255.0)
+    maxv = 65535 if depth == 16 else 255
+    if depth < 8:
+        img = img * (255 // ((1 << depth) - 1))  # low bit depths expand to 8 bits
+    f = img.astype(np.float32) / np.float32(maxv)
+    if ch in (1, 2):
+        return np.repeat(f[..., :1], 3, axis=-1)
+    return np.ascontiguousarray(f[..., :3])
+
+
+# -------------------------------------------------------------------- EXR ---
+_EXR_MAGIC = 20000630
+_EXR_LINES = {0: 1, 1: 1, 2: 1, 3: 16}  # compression -> scanlines per chunk (NONE, RLE, ZIPS, ZIP)
+_EXR_TYPES = {0: (np.dtype("<u4"), 4), 1: (np.dtype("<f2"), 2), 2: (np.dtype("<f4"), 4)}
+
+
+def _exr_header(data: bytes):
+    magic, version = struct.unpack("<ii", data[:8])
+    if magic != _EXR_MAGIC:
+        raise VoidrayError(1, "EXR: bad magic number")
+    if version & 0x200 or version & 0x800 or version & 0x1000:
+        raise VoidrayError(2, "EXR: tiled, deep or multi-part files are not supported")
+    pos, attrs = 8, {}
+    while data[pos] != 0:
+        end = data.index(b"\0", pos)
+        name = data[pos:end].decode()
+        tend = data.index(b"\0", end + 1)
+        typ = data[end + 1:tend].decode()
+        size = struct.unpack("<i", data[tend + 1:tend + 5])[0]
+        attrs[name] = (typ, data[tend + 5:tend + 5 + size])
+        pos = tend + 5 + size
+    return attrs, pos + 1
+
+
+def _exr_channels(value: bytes):
+    chans, pos = [], 0
+    while value[pos] != 0:
+        end = value.index(b"\0", pos)
+        name = value[pos:end].decode()
+        ptype, _linear, xs, ys = struct.unpack("<iB3xii", value[end + 1:end + 17])
+        if ptype not in _EXR_TYPES or xs != 1 or ys != 1:
+            raise VoidrayError(2, f"EXR: channel {name!r} type {ptype} sampling {xs}x{ys} not supported")
+        chans.append((name, ptype))
+        pos = end + 17
+    return chans
+
+
+def _exr_rle_decode(src: bytes, size: int) -> bytes:
+    out, i = bytearray(), 0
+    while i < len(src) and len(out) < size:
+        n = struct.unpack("b", src[i:i + 1])[0]
+        i += 1
+        if n < 0:
+            out += src[i:i - n]
+            i -= n
+        else:
+            out += src[i:i + 1] * (n + 1)
+            i += 1
+    if len(out) != size:
+        raise VoidrayError(1, "EXR: RLE chunk has the wrong size")
+    return bytes(out)
+
+
+def _exr_unpredict(t: bytes) -> bytes:
+    """The ZIP/RLE post-pass: undo the byte delta, then re-interleave the two
+    halves (even bytes were stored first, odd bytes second)."""
+    d = np.frombuffer(t, np.uint8).astype(np.int64)
+    if d.size:
+        d[1:] -= 128
+        d = np.cumsum(d) & 0xFF
+    d = d.astype(np.uint8)
+    out = np.empty_like(d)
+    half = (d.size + 1) // 2
+    out[0::2] = d[:half]
+    out[1::2] = d[half:]
+    return out.tobytes()
+
+
+def decode_exr(data: bytes) -> np.ndarray:
+    attrs, pos = _exr_header(data)
+    for req in ("channels", "compression", "dataWindow"):
+        if req not in attrs:
+            raise VoidrayError(1, f"EXR: header lacks {req!r}")
+    chans = _exr_channels(attrs["channels"][1])
+    comp = attrs["compression"][1][0]
+    if comp not in _EXR_LINES:
+        raise VoidrayError(2, f"EXR: compression {comp} not supported (NONE, RLE, ZIPS, ZIP are)")
+    xmin, ymin, xmax, ymax = struct.unpack("<iiii", attrs["dataWindow"][1])
+    w, h = xmax - xmin + 1, ymax - ymin + 1
+    if w <= 0 or h <= 0:
+        raise VoidrayError(1, "EXR: empty data window")
+    lines = _EXR_LINES[comp]
+    nchunks = (h + lines - 1) // lines
+    offsets = struct.unpack(f"<{nchunks}Q", data[pos:pos + 8 * nchunks])
+    planes = {name: np.zeros((h, w), np.float32) for name, _ in chans}
+    row_bytes = sum(_EXR_TYPES[t][1] for _, t in chans) * w
+    for off in offsets:
+        y, size = struct.unpack("<ii", data[off:off + 8])
+        blob = data[off + 8:off + 8 + size]
+        y0 = y - ymin
+        if not 0 <= y0 < h:
+            raise VoidrayError(1, f"EXR: chunk for line {y} outside the data window")
+        n = min(lines, h - y0)
+        want = row_bytes * n
+        if size < want and comp == 1:
+            blob = _exr_unpredict(_exr_rle_decode(blob, want))
+        elif size < want and comp in (2, 3):
+            blob = _exr_unpredict(zlib.decompress(blob))
+        if len(blob) != want:
+            raise VoidrayError(1, "EXR: chunk has the wrong size")
+        p = 0
+        for r in range(n):
+            for name, t in chans:
+                dt, sz = _EXR_TYPES[t]
+                planes[name][y0 + r] = np.frombuffer(blob, dt, w, p).astype(np.float32)
+                p += sz * w
+    if not all(c in planes for c in "RGB"):
+        raise VoidrayError(2, "EXR: needs R, G and B channels")
+    return np.ascontiguousarray(np.stack([planes["R"], planes["G"], planes["B"]], axis=-1))
+
+
+def load_image_rgb32f(path: str) -> np.ndarray:
+    """Decodes an image file to float32 RGB [height, width, 3], row 0 at the top."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] == _PNG_MAGIC:
+        return decode_png(data)
+    if len(data) >= 4 and struct.unpack("<i", data[:4])[0] == _EXR_MAGIC:
+        return decode_exr(data)
+    ext = os.path.splitext(path)[1].lower()
+    raise VoidrayError(2, f"image format of {os.path.basename(path)!r} ({ext or 'unknown'}) is not "
+                          "decoded here: pass float RGB arrays instead")

@@ -164,12 +164,19 @@ class ImageTexture:
         if self.image.ndim != 3 or self.image.shape[2] != 3 or self.image.size == 0:
             raise VoidrayError(1, "texture image must be H x W x 3")
 
+    @staticmethod
+    def from_file(path: str, sample_type: SampleType = SampleType.Bilinear) -> "ImageTexture":
+        """ImageTexture::new (texture.rs:36-50): `image::open(path).to_rgb32f()`."""
+        from .assets import load_image_rgb32f
+
+        return ImageTexture(load_image_rgb32f(path), sample_type)
+
 
 LAMBERTIAN, METAL, DIELECTRIC, EMISSION, LAMBERTIAN_BSDF, MICROFACET = range(6)
 
 
 class Materials:
-    """voidray_common/src/simple.rs:15-58 (textured variants are not supported)."""
+    """voidray_common/src/simple.rs:15-58."""
 
     @staticmethod
     def lambertian(albedo) -> Material:
@@ -271,6 +278,15 @@ class Mesh:
         uv = np.stack([v.uv for v in vertices]).astype(np.float32)
         return Mesh(pos, indices, None if not nrm.any() else nrm, None if not uv.any() else uv)
 
+    @staticmethod
+    def from_file(path: str) -> "Mesh":
+        """Mesh::from_file (mesh.rs:46-74): the OBJ's vertices numbered as obj-rs
+        numbers (position, texture, normal) triples, then Mesh::from_buffers."""
+        from .assets import load_obj
+
+        pos, uv, nrm, idx = load_obj(path)
+        return Mesh(pos, idx, None if not nrm.any() else nrm, None if not uv.any() else uv)
+
     @property
     def num_triangles(self) -> int:
         return len(self.indices)
@@ -328,6 +344,14 @@ class Environments:
         if img.ndim != 3 or img.shape[2] != 3:
             raise VoidrayError(1, "HDRI image must be H x W x 3")
         return Environment(2, np.zeros(3, np.float32), img, importance_sample)
+
+    @staticmethod
+    def hdri(path: str, importance_sample: bool = True) -> Environment:
+        """Environments::hdri (environments.rs:14-16, 42-55): decodes the file
+        (EXR or PNG) to RGB f32."""
+        from .assets import load_image_rgb32f
+
+        return Environments.hdri_image(load_image_rgb32f(path), importance_sample)
 
 
 # ------------------------------------------------------------------ camera ---
@@ -406,7 +430,13 @@ class Scene:
         return len(self.surfaces) - 1
 
     def add_mesh_from_file(self, path: str) -> int:
-        raise VoidrayError(2, "OBJ loading is not part of the GPU path; pass Mesh arrays")
+        """scene.rs:137-144 with Mesh::from_file (OBJ, obj-rs TexturedVertex rules)."""
+        return self.add_mesh(Mesh.from_file(path))
+
+    def add_image_texture(self, path: str, sample_type: "SampleType" = None) -> int:
+        """scene.rs:154-160: decodes the file (PNG or EXR) to RGB f32."""
+        return self.add_texture(ImageTexture.from_file(path, SampleType.Bilinear if sample_type is None
+                                                       else sample_type))
 
     def add_object(self, material: int, surface: int) -> int:
         self.objects.append(Object(surface, material))
