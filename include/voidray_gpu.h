@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define VR_ABI_VERSION 3
+#define VR_ABI_VERSION 4
 
 typedef enum vr_status {
     VR_OK = 0,
@@ -62,9 +62,17 @@ typedef enum vr_material_kind {
     VR_MAT_EMISSION = 3,        /* Materials::{emissive,colored_emissive}; color
                                    already multiplied by strength               */
     VR_MAT_LAMBERTIAN_BSDF = 4, /* Materials::lambertian_bsdf(albedo)           */
-    VR_MAT_MICROFACET = 5       /* MicrofacetBSDF {color,index,roughness,
+    VR_MAT_MICROFACET = 5,      /* MicrofacetBSDF {color,index,roughness,
                                    metallic,emittance,transparent}              */
+    VR_MAT_MIX = 6              /* MixMaterial {first, second, factor} of the
+                                   legacy crate (voidray/src/common/materials.rs:
+                                   188-203): one uniform draw u per hit; u >=
+                                   factor shades with `mix_first`, else with
+                                   `mix_second`.  Children may be mixes, at most
+                                   VR_MAX_MIX_DEPTH levels deep (no cycles).    */
 } vr_material_kind;
+
+#define VR_MAX_MIX_DEPTH 8
 
 typedef struct vr_material {
     int32_t kind;       /* vr_material_kind                                     */
@@ -81,6 +89,9 @@ typedef struct vr_material {
     int32_t normal_texture;  /* Lambertian: normal map (its raw RGB replaces the
                                 shading normal of the scatter, simple.rs:109-113),
                                 -1 = none                                        */
+    int32_t mix_first;       /* VR_MAT_MIX: material indices of the two children */
+    int32_t mix_second;
+    float mix_factor;        /* VR_MAT_MIX: probability of `mix_second`          */
 } vr_material;
 
 /* One triangle mesh: Mesh::from_buffers (voidray_renderer/src/core/mesh.rs:76-116).
@@ -385,6 +396,26 @@ vr_status vr_tonemap(const float* rgba_in, float* rgba_out, uint32_t width,
 vr_status vr_tonemap_device(const float* rgba_in_device, float* rgba_out_device,
                             uint32_t width, uint32_t height,
                             const vr_color_management* cm, float scale, void* stream);
+
+/* The legacy viewport's post-processing (voidray/src/shaders/
+ * viewport_fragment.glsl:27-67 with tonemapping.glsl:1-69): its own tonemap
+ * numbering, exposure as a linear factor, gamma 1 for Filmic, and with
+ * `transparent` the output alpha is the scaled input alpha (else 1). */
+typedef enum vr_legacy_tonemap {
+    VR_LEGACY_TONEMAP_NONE = 0,
+    VR_LEGACY_TONEMAP_SIMPLE_ACES = 1,
+    VR_LEGACY_TONEMAP_SIMPLE_REINHARD = 2,
+    VR_LEGACY_TONEMAP_LUMA_REINHARD = 3,
+    VR_LEGACY_TONEMAP_LUMA_WHITEPRESERVING_REINHARD = 4,
+    VR_LEGACY_TONEMAP_ROM_BIN_DA_HOUSE = 5,
+    VR_LEGACY_TONEMAP_FILMIC = 6,
+    VR_LEGACY_TONEMAP_UNCHARTED_2 = 7
+} vr_legacy_tonemap;
+vr_status vr_tonemap_legacy(const float* rgba_in, float* rgba_out, uint32_t width, uint32_t height,
+                            int32_t tonemap, float gamma, float exposure, int32_t transparent, float scale);
+vr_status vr_tonemap_legacy_device(const float* rgba_in_device, float* rgba_out_device, uint32_t width,
+                                   uint32_t height, int32_t tonemap, float gamma, float exposure,
+                                   int32_t transparent, float scale, void* stream);
 
 /* relative MSE over RGB: mean((x-r)^2/(r^2+eps)), eps = 1e-2; each image is
  * RGBA f32 scaled by its own factor first. */

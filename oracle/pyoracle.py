@@ -42,7 +42,8 @@ class orc_object(C.Structure):
 class orc_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("fuzz", C.c_float), ("ir", C.c_float),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("emittance", C.c_float),
-                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32)]
+                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32),
+                ("mix_first", C.c_int32), ("mix_second", C.c_int32), ("mix_factor", C.c_float)]
 
 
 class orc_texture(C.Structure):
@@ -84,6 +85,7 @@ _SIGS = {
                           C.c_uint32, C.c_int32, P]),
     "orc_trace_path": (None, [P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, P]),
     "orc_tonemap": (None, [P, P, C.c_uint64, C.c_int32, C.c_float, C.c_float, C.c_float]),
+    "orc_tonemap_legacy": (None, [P, P, C.c_uint64, C.c_int32, C.c_float, C.c_float, C.c_int32, C.c_float]),
     "orc_env_eval": (None, [P, P, P]),
     "orc_env_sample": (C.c_int32, [P, P, P, P]),
     "orc_env_pdf": (C.c_float, [P, P]),
@@ -134,9 +136,11 @@ class OracleScene:
             anas[k].kind, anas[k].radius, anas[k].height, anas[k].surface = a.kind, a.radius, a.height, s
             for j in range(3):
                 anas[k].center[j] = float(a.center[j])
-        mats = (orc_material * max(1, len(scene.materials)))()
-        for i, m in enumerate(scene.materials):
+        flat = scene.flat_materials()
+        mats = (orc_material * max(1, len(flat)))()
+        for i, (m, first, second) in enumerate(flat):
             c = mats[i]
+            c.mix_first, c.mix_second, c.mix_factor = first, second, m.factor
             c.kind = m.kind
             for k in range(3):
                 c.color[k] = float(m.color[k])
@@ -153,7 +157,7 @@ class OracleScene:
         d.meshes, d.num_meshes = C.addressof(meshes), n
         d.analytics, d.num_analytics = C.addressof(anas), len(ana_surfs)
         d.textures, d.num_textures = C.addressof(texs), len(scene.textures)
-        d.materials, d.num_materials = C.addressof(mats), len(scene.materials)
+        d.materials, d.num_materials = C.addressof(mats), len(flat)
         d.objects, d.num_objects = C.addressof(objs), len(scene.objects)
         env = scene.environment
         if env is not None:
@@ -239,6 +243,14 @@ def tonemap(rgba: np.ndarray, tonemap: int, gamma: float, exposure: float, scale
     rgba = np.ascontiguousarray(rgba, np.float32)
     out = np.empty_like(rgba)
     lib().orc_tonemap(_p(rgba), _p(out), rgba.size // 4, tonemap, gamma, exposure, scale)
+    return out
+
+
+def tonemap_legacy(rgba: np.ndarray, tonemap: int, gamma: float, exposure: float, transparent: bool,
+                   scale: float) -> np.ndarray:
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.empty_like(rgba)
+    lib().orc_tonemap_legacy(_p(rgba), _p(out), rgba.size // 4, tonemap, gamma, exposure, int(transparent), scale)
     return out
 
 

@@ -616,7 +616,7 @@ float env_pdf(const Scene& s, V3 d) {
 }
 
 // ------------------------------------------------------------- materials --
-enum { M_LAMB = 0, M_METAL = 1, M_DIEL = 2, M_EMIT = 3, M_LBSDF = 4, M_MICRO = 5 };
+enum { M_LAMB = 0, M_METAL = 1, M_DIEL = 2, M_EMIT = 3, M_LBSDF = 4, M_MICRO = 5, M_MIX = 6 };
 
 // local_to_world (math.rs:50-60).  QUIRK: cgmath's Matrix3::new is column
 // major, so the matrix built there has rows ns, nss, n and M*h = (ns.h, nss.h, n.h).
@@ -752,6 +752,16 @@ V3 tex_sample(const Scene& s, int tix, float u, float v) {
                  lerp3(px(((y0 + 1) * W + x0) % len), px(((y0 + 1) * W + x0 + 1) % len), ax), ay);
 }
 // Lambertian textures (simple.rs:102-133): the albedo and the scatter normal from the hit's uv
+// MixMaterial::scatter (legacy voidray/src/common/materials.rs:195-203):
+// `gen_range(0.0..1.0) >= factor` picks the first child, else the second;
+// one draw per level of mixing, before the child's own draws.
+void resolve_mix(const Scene& s, orc_material& m, Pcg32& rng) {
+    for (int d = 0; m.kind == M_MIX && d < 8; ++d) {
+        float u = rng.uniform();
+        m = s.materials[u >= m.mix_factor ? m.mix_first : m.mix_second];
+    }
+}
+
 void apply_textures(const Scene& s, orc_material& m, Hit& hit) {
     if (m.albedo_texture >= 0) {
         V3 c = tex_sample(s, m.albedo_texture, hit.uvx, hit.uvy);
@@ -877,6 +887,7 @@ V3 trace_ref(const Scene& s, const orc_settings& st, const Ray& ray, uint32_t de
         if (!hp.ok) return env_eval(s, ray.d);
         Hit hit = hp.best;
         orc_material m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        resolve_mix(s, m, rng);
         apply_textures(s, m, hit);
         V3 att;
         Ray sc;
@@ -925,6 +936,7 @@ V3 trace_nee(const Scene& s, const orc_settings& st, Ray ray, Pcg32& rng, Counte
         }
         Hit hit = hp.best;
         orc_material m = s.materials[s.surface_material[surface_of_prim(s, hit.prim)]];
+        resolve_mix(s, m, rng);
         apply_textures(s, m, hit);
         if (st.render_mode != 1) {
             V3 nn = normalize(hit.normal);
@@ -1051,11 +1063,17 @@ orc_scene* orc_scene_create(const orc_scene_desc* d) {
         t.img.assign(td.image, td.image + 3 * (size_t)td.width * td.height);
         s.textures.push_back(std::move(t));
     }
-    for (const orc_material& m : s.materials)
+    for (const orc_material& m : s.materials) {
         if (m.albedo_texture >= (int)d->num_textures || m.normal_texture >= (int)d->num_textures) {
             g_err = "texture index out of range";
             return nullptr;
         }
+        if (m.kind == M_MIX && (m.mix_first < 0 || m.mix_first >= (int)d->num_materials || m.mix_second < 0 ||
+                                m.mix_second >= (int)d->num_materials)) {
+            g_err = "mix child out of range";
+            return nullptr;
+        }
+    }
     uint64_t prim = 0;
     for (uint32_t mi = 0; mi < d->num_meshes; ++mi) {
         const orc_mesh& md = d->meshes[mi];
@@ -1339,6 +1357,46 @@ void orc_tonemap(const float* in, float* out, uint64_t n, int32_t tonemap, float
         o[1] = std::pow(c.y, g);
         o[2] = std::pow(c.z, g);
         o[3] = 1.0f;
+    }
+}
+
+// Legacy viewport (voidray/src/shaders/viewport_fragment.glsl:27-67,
+// tonemapping.glsl:17-45): its numbering, linear exposure, Filmic without
+// gamma, alpha kept when transparent.
+void orc_tonemap_legacy(const float* in, float* out, uint64_t n, int32_t tonemap, float gamma, float exposure,
+                        int32_t transparent, float scale) {
+    if (tonemap == 6) gamma = 1.0f;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* p = in + 4 * i;
+        V3 c = v3(p[0] * scale, p[1] * scale, p[2] * scale) * exposure;
+        switch (tonemap) {
+        case 1: c = tm_aces(c); break;
+        case 2: {
+            const float e = 1.5f;
+            c = v3(c.x * (e / (1.0f + c.x / e)), c.y * (e / (1.0f + c.y / e)), c.z * (e / (1.0f + c.z / e)));
+            break;
+        }
+        case 3: {
+            float luma = c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f;
+            float tml = luma / (1.0f + luma);
+            c = c * (tml / luma);
+            break;
+        }
+        case 4: c = tm_reinhard(c); break;
+        case 5:
+            c = v3(std::exp(-1.0f / (2.72f * c.x + 0.15f)), std::exp(-1.0f / (2.72f * c.y + 0.15f)),
+                   std::exp(-1.0f / (2.72f * c.z + 0.15f)));
+            break;
+        case 6: c = v3(filmic1(c.x), filmic1(c.y), filmic1(c.z)); break;
+        case 7: c = tm_uncharted2(c); break;
+        default: break;
+        }
+        float g = 1.0f / gamma;
+        float* o = out + 4 * i;
+        o[0] = std::pow(c.x, g);
+        o[1] = std::pow(c.y, g);
+        o[2] = std::pow(c.z, g);
+        o[3] = transparent ? p[3] * scale : 1.0f;
     }
 }
 

@@ -63,6 +63,7 @@ typedef struct orc_material {
     int32_t kind; float color[3]; float fuzz; float ir; float roughness;
     float metallic; float emittance; int32_t transparent;
     int32_t albedo_texture; int32_t normal_texture;  /* -1: none */
+    int32_t mix_first; int32_t mix_second; float mix_factor;  /* kind 6: MixMaterial */
 } orc_material;
 
 /* ImageTexture (voidray_renderer/src/core/texture.rs) */
@@ -134,6 +135,9 @@ void orc_trace_path(const orc_scene* s, const orc_settings* st, uint32_t width,
 /* post_process.glsl + tonemapping.glsl restated. */
 void orc_tonemap(const float* rgba_in, float* rgba_out, uint64_t num_pixels,
                  int32_t tonemap, float gamma, float exposure, float scale);
+/* The legacy viewport's post-processing (voidray/src/shaders/viewport_fragment.glsl). */
+void orc_tonemap_legacy(const float* rgba_in, float* rgba_out, uint64_t num_pixels, int32_t tonemap,
+                        float gamma, float exposure, int32_t transparent, float scale);
 
 /* Environment lookup (HDRIEnvironment::sample / UniformEnvironment::sample). */
 void orc_env_eval(const orc_scene* s, const float* dir, float* rgb_out);

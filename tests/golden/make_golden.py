@@ -2,6 +2,10 @@
 post_process.glsl:23-49 and tonemapping.glsl:2-40 (reference files of
 LevKruglyak/voidray, voidray_renderer/src/shaders/), independent of the C++
 oracle.  GLSL mat3(a,...,i) is column major: columns (a,b,c), (d,e,f), (g,h,i).
+Also tests/golden/tonemap_legacy_f64.npz: the legacy viewport's
+post-processing (voidray/src/shaders/viewport_fragment.glsl:27-67 with
+voidray/src/shaders/tonemapping.glsl:1-69): linear exposure, Filmic without
+gamma, alpha scaled and kept when transparent.
 
 Run: python tests/golden/make_golden.py
 """
@@ -50,6 +54,32 @@ def main():
         o[:, :3] = y
         out[f"out_{k}"] = o
     np.savez(Path(__file__).with_name("tonemap_f64.npz"), **out)
+
+    # legacy viewport: numbering 0..7, exposure multiplies, transparent keeps alpha
+    def simple_reinhard(c):
+        e = 1.5
+        return c * (e / (1.0 + c / e))
+
+    def luma_reinhard(c):
+        luma = c @ np.array([0.2126, 0.7152, 0.0722])
+        return c * ((luma / (1.0 + luma)) / luma)[..., None]
+
+    def rombindahouse(c):
+        return np.exp(-1.0 / (2.72 * c + 0.15))
+
+    legacy = [lambda v: v, aces, simple_reinhard, luma_reinhard, reinhard, rombindahouse, filmic, uncharted2]
+    gamma, exposure, scale = 2.2, 1.3, 0.8
+    c = x[:, :3].astype(np.float64) * scale * exposure
+    lout = {"input": x, "gamma": gamma, "exposure": exposure, "scale": scale}
+    for k, fn in enumerate(legacy):
+        g = 1.0 if k == 6 else gamma
+        with np.errstate(all="ignore"):
+            y = np.power(fn(c), 1.0 / g)
+        o = np.empty((len(x), 4))
+        o[:, :3] = y
+        o[:, 3] = x[:, 3].astype(np.float64) * scale  # transparent
+        lout[f"out_{k}"] = o
+    np.savez(Path(__file__).with_name("tonemap_legacy_f64.npz"), **lout)
 
 
 if __name__ == "__main__":

@@ -28,7 +28,7 @@ def test_exports_every_declared_symbol(native):
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(native.EXPORTED)
-    assert lib.vr_abi_version() == 3
+    assert lib.vr_abi_version() == 4
 
 
 def test_no_device_is_an_error_not_a_fallback(native):

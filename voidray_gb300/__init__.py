@@ -8,12 +8,13 @@ from ._native import EXPORTED, VR_MISS, VoidrayError, lib
 from .renderer import Checkpoint, Renderer, RenderAction, RendererStats
 from .scene import (AnalyticSurface, ImageTexture, SampleType, Camera, ColorManagementSettings, CpuRenderTarget, Environment, Environments, Estimator, Material,
                     Materials, Mesh, MicrofacetBSDF, RenderMode, RenderSettings, Scene, SceneAcceleration, Settings,
-                    Surfaces, Tonemap, Vertex, degrees_to_radians, hex_color, iterative_render, render_device, tonemap)
+                    Surfaces, Tonemap, LegacyTonemap, Vertex, degrees_to_radians, hex_color, iterative_render, render_device,
+                    tonemap, tonemap_legacy)
 
 __all__ = [
     "EXPORTED", "VR_MISS", "VoidrayError", "lib", "AnalyticSurface", "ImageTexture", "SampleType", "Camera", "ColorManagementSettings", "CpuRenderTarget",
     "Environment", "Environments", "Estimator", "Material", "Materials", "Mesh", "MicrofacetBSDF", "RenderMode",
     "RenderSettings", "Scene", "SceneAcceleration", "Settings", "Surfaces", "Tonemap", "Vertex",
     "degrees_to_radians", "hex_color", "iterative_render", "render_device", "tonemap", "Renderer", "RenderAction",
-    "RendererStats", "Checkpoint",
+    "RendererStats", "Checkpoint", "LegacyTonemap", "tonemap_legacy",
 ]

@@ -32,7 +32,8 @@ class VoidrayError(RuntimeError):
 class vr_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("color", C.c_float * 3), ("fuzz", C.c_float), ("ir", C.c_float),
                 ("roughness", C.c_float), ("metallic", C.c_float), ("emittance", C.c_float),
-                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32)]
+                ("transparent", C.c_int32), ("albedo_texture", C.c_int32), ("normal_texture", C.c_int32),
+                ("mix_first", C.c_int32), ("mix_second", C.c_int32), ("mix_factor", C.c_float)]
 
 
 class vr_texture_desc(C.Structure):
@@ -135,6 +136,10 @@ _SIGS = [
     ("vr_render_stats_get", C.c_int, [P, P]),
     ("vr_tonemap", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float]),
     ("vr_tonemap_device", C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_float, P]),
+    ("vr_tonemap_legacy", C.c_int, [P, P, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float, C.c_int32,
+                                    C.c_float]),
+    ("vr_tonemap_legacy_device", C.c_int, [P, P, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float,
+                                           C.c_int32, C.c_float, P]),
     ("vr_relmse_device", C.c_int, [P, C.c_float, P, C.c_float, C.c_uint32, C.c_uint32, P, P]),
     ("vr_intersect", C.c_int, [P, P, C.c_uint64, P, C.c_int32]),
     ("vr_intersect_device", C.c_int, [P, P, C.c_uint64, P, C.c_int32, P]),

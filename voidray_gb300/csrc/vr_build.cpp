@@ -266,7 +266,7 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         static_assert(sizeof(Material) == sizeof(vr_material), "material layout");
         std::memcpy(&hs.materials[i], &d->materials[i], sizeof(Material));
-        if (hs.materials[i].kind < 0 || hs.materials[i].kind > M_MICRO) {
+        if (hs.materials[i].kind < 0 || hs.materials[i].kind > M_MIX) {
             err = "material " + std::to_string(i) + ": unsupported kind";
             return VR_ERR_UNSUPPORTED;
         }
@@ -280,6 +280,28 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             err = "material " + std::to_string(i) + ": only Lambertian materials take textures";
             return VR_ERR_UNSUPPORTED;
         }
+        if (mt.kind == M_MIX && (mt.mix_first < 0 || mt.mix_first >= (int32_t)d->num_materials ||
+                                 mt.mix_second < 0 || mt.mix_second >= (int32_t)d->num_materials)) {
+            err = "material " + std::to_string(i) + ": mix child index out of range";
+            return VR_ERR_INVALID;
+        }
+    }
+    // MixMaterial chains end in a plain material within MAX_MIX_DEPTH levels (this also
+    // rules out cycles), so the kernels resolve a mix with a bounded loop
+    {
+        std::vector<int> depth(hs.materials.size(), -1);  // levels of mixing below material i
+        for (size_t pass = 0; pass <= MAX_MIX_DEPTH + 1; ++pass)
+            for (size_t i = 0; i < hs.materials.size(); ++i) {
+                const Material& mt = hs.materials[i];
+                if (mt.kind != M_MIX) { depth[i] = 0; continue; }
+                const int a = depth[mt.mix_first], b = depth[mt.mix_second];
+                if (a >= 0 && b >= 0) depth[i] = 1 + std::max(a, b);
+            }
+        for (size_t i = 0; i < hs.materials.size(); ++i)
+            if (depth[i] < 0 || depth[i] > MAX_MIX_DEPTH) {
+                err = "material " + std::to_string(i) + ": mix chain deeper than VR_MAX_MIX_DEPTH or cyclic";
+                return VR_ERR_INVALID;
+            }
     }
     // image textures (texture.rs:28-98)
     if (d->num_textures && !d->textures) { err = "textures is NULL"; return VR_ERR_INVALID; }

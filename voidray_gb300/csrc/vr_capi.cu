@@ -982,7 +982,21 @@ vr_status vr_tonemap_device(const float* in, float* out, uint32_t w, uint32_t h,
     const float ex = std::pow(2.0f, cm->exposure);
     const float inv_gamma = 1.0f / cm->gamma;
     VR_CK(vr::launch_tonemap(reinterpret_cast<const float4*>(in), reinterpret_cast<float4*>(out), w * h, cm->tonemap,
-                             inv_gamma, ex, scale, static_cast<cudaStream_t>(stream)));
+                             inv_gamma, ex, scale, 0, static_cast<cudaStream_t>(stream)));
+    return VR_OK;
+}
+
+vr_status vr_tonemap_legacy_device(const float* in, float* out, uint32_t w, uint32_t h, int32_t tonemap, float gamma,
+                                   float exposure, int32_t transparent, float scale, void* stream) {
+    if (!in || !out) return fail(VR_ERR_INVALID, "null argument");
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    // legacy numbering (viewport_fragment.glsl:10-17) -> kernel curve codes
+    static const int32_t code[8] = {0, 1, 5, 6, 2, 7, 3, 4};
+    if (tonemap < 0 || tonemap > 7) return fail(VR_ERR_INVALID, "legacy tonemap");
+    if (tonemap == VR_LEGACY_TONEMAP_FILMIC) gamma = 1.0f;  // "Filmic doesn't have gamma"
+    VR_CK(vr::launch_tonemap(reinterpret_cast<const float4*>(in), reinterpret_cast<float4*>(out), w * h,
+                             code[tonemap], 1.0f / gamma, exposure, scale, transparent ? 1 : 0,
+                             static_cast<cudaStream_t>(stream)));
     return VR_OK;
 }
 
@@ -1000,6 +1014,30 @@ vr_status vr_tonemap(const float* in, float* out, uint32_t w, uint32_t h, const 
     vr_status r = VR_OK;
     if (cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy in");
     if (r == VR_OK) r = vr_tonemap_device(static_cast<float*>(din), static_cast<float*>(dout), w, h, cm, scale, nullptr);
+    if (r == VR_OK && cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy out");
+    cudaFree(din);
+    cudaFree(dout);
+    return r;
+}
+
+vr_status vr_tonemap_legacy(const float* in, float* out, uint32_t w, uint32_t h, int32_t tonemap, float gamma,
+                            float exposure, int32_t transparent, float scale) {
+    if (!in || !out) return fail(VR_ERR_INVALID, "null argument");
+    if (!device_ok()) return fail(VR_ERR_NO_DEVICE, "no CUDA device");
+    if (tonemap < 0 || tonemap > 7) return fail(VR_ERR_INVALID, "legacy tonemap");
+    const size_t bytes = (size_t)w * h * 16;
+    if (bytes == 0) return VR_OK;
+    void *din = nullptr, *dout = nullptr;
+    VR_CK(cudaMalloc(&din, bytes));
+    if (cudaMalloc(&dout, bytes) != cudaSuccess) {
+        cudaFree(din);
+        return fail(VR_ERR_OOM, "tonemap buffer");
+    }
+    vr_status r = VR_OK;
+    if (cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy in");
+    if (r == VR_OK)
+        r = vr_tonemap_legacy_device(static_cast<float*>(din), static_cast<float*>(dout), w, h, tonemap, gamma,
+                                     exposure, transparent, scale, nullptr);
     if (r == VR_OK && cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) r = fail(VR_ERR_CUDA, "copy out");
     cudaFree(din);
     cudaFree(dout);

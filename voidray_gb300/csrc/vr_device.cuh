@@ -22,7 +22,8 @@ constexpr uint32_t MISS = 0xFFFFFFFFu;
 // device status word bits
 enum : uint32_t { ERRF_STACK = 1u, ERRF_QUEUE = 2u, ERRF_TIMEOUT = 4u };
 
-enum MatKind : int32_t { M_LAMB = 0, M_METAL = 1, M_DIEL = 2, M_EMIT = 3, M_LBSDF = 4, M_MICRO = 5 };
+enum MatKind : int32_t { M_LAMB = 0, M_METAL = 1, M_DIEL = 2, M_EMIT = 3, M_LBSDF = 4, M_MICRO = 5, M_MIX = 6 };
+constexpr int MAX_MIX_DEPTH = 8;  // VR_MAX_MIX_DEPTH
 
 struct Material {  // same layout as vr_material
     int32_t kind;
@@ -30,6 +31,8 @@ struct Material {  // same layout as vr_material
     float fuzz, ir, roughness, metallic, emittance;
     int32_t transparent;
     int32_t albedo_tex, normal_tex;  // -1: none
+    int32_t mix_first, mix_second;   // M_MIX children
+    float mix_factor;
 };
 
 // Flattened BVH2: node = 4 x float4 (64 bytes)

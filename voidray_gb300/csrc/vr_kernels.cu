@@ -12,7 +12,8 @@
 //   k_shadow         any-hit visibility of the NEE shadow rays
 //   k_accumulate     per-pixel sum in sample order (iterative.rs:37-43)
 //   k_finalize       rgba += sum / total_samples, alpha += 1 (iterative.rs:45-51)
-//   k_tonemap        post_process.glsl:23-49 + tonemapping.glsl:2-40
+//   k_tonemap        post_process.glsl:23-49 + tonemapping.glsl:2-40; the legacy
+//                    viewport's curves (voidray/src/shaders/viewport_fragment.glsl:27-67)
 //   k_relmse         relative MSE reduction
 //
 // No tensor cores: traversal and shading are FP32 SIMT, bound by memory
@@ -172,6 +173,17 @@ __device__ V3 tex_sample(const SceneView& s, int32_t tix, float u, float v) {
     return lerp3(lerp3(env_px(img, (y0 * W + x0) % len), env_px(img, (y0 * W + x0 + 1) % len), ax),
                  lerp3(env_px(img, ((y0 + 1) * W + x0) % len), env_px(img, ((y0 + 1) * W + x0 + 1) % len), ax),
                  ay);
+}
+
+// MixMaterial::scatter (legacy voidray/src/common/materials.rs:195-203): one
+// uniform draw per level picks the child that shades this hit; the scene
+// builder guarantees every chain ends within MAX_MIX_DEPTH levels.
+__device__ __forceinline__ void resolve_mix(const SceneView& s, Material& m, Rng& rng) {
+#pragma unroll 1
+    for (int d = 0; m.kind == M_MIX && d < MAX_MIX_DEPTH; ++d) {
+        const float u = rng.uniform();
+        m = s.materials[u >= m.mix_factor ? m.mix_first : m.mix_second];
+    }
 }
 
 __device__ __forceinline__ float lerpf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
@@ -656,6 +668,7 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                         uvy = point.z;
                     }
                 }
+                resolve_mix(s, m, rng);
                 SurfHit hit;
                 hit.point = point;
                 hit.t = t;
@@ -916,8 +929,11 @@ __device__ __forceinline__ float unch1(float x) {
     const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
     return ((x * (A * x + C * B) + D * E) / (x * (A * x + B) + D * F)) - E / F;
 }
+// Codes 0-4 are Tonemap::as_i32 of voidray_renderer; 5-7 are the curves only
+// the legacy viewport has (voidray/src/shaders/tonemapping.glsl:17-45).
+// `transparent` keeps the scaled input alpha (legacy viewport_fragment.glsl:62-66).
 __global__ void k_tonemap(const float4* __restrict__ in, float4* __restrict__ out, uint32_t np, int32_t tonemap,
-                          float inv_gamma, float ex, float scale) {
+                          float inv_gamma, float ex, float scale, int32_t transparent) {
     const float A[9] = {0.59719f, 0.076f, 0.0284f, 0.35458f, 0.90834f, 0.13383f, 0.04823f, 0.01566f, 0.83777f};
     const float B[9] = {1.60475f, -0.10208f, -0.00327f, -0.53108f, 1.10813f, -0.07276f, -0.07367f, -0.00605f, 1.07602f};
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -943,8 +959,19 @@ __global__ void k_tonemap(const float4* __restrict__ in, float4* __restrict__ ou
             c = c * 2.0f;
             V3 r = v3(unch1(c.x), unch1(c.y), unch1(c.z));
             c = r / unch1(11.2f);
+        } else if (tonemap == 5) {  // legacy tonemap_simple_reinhard: color *= e / (1 + color / e), e = 1.5
+            const float e = 1.5f;
+            c = v3(c.x * (e / (1.0f + c.x / e)), c.y * (e / (1.0f + c.y / e)), c.z * (e / (1.0f + c.z / e)));
+        } else if (tonemap == 6) {  // legacy tonemap_luma_reinhard
+            const float luma = c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f;
+            const float tml = luma / (1.0f + luma);
+            c = c * (tml / luma);
+        } else if (tonemap == 7) {  // legacy tonemap_rombindahouse: exp(-1 / (2.72 color + 0.15))
+            c = v3(expf(-1.0f / (2.72f * c.x + 0.15f)), expf(-1.0f / (2.72f * c.y + 0.15f)),
+                   expf(-1.0f / (2.72f * c.z + 0.15f)));
         }
-        out[i] = make_float4(powf(c.x, inv_gamma), powf(c.y, inv_gamma), powf(c.z, inv_gamma), 1.0f);
+        out[i] = make_float4(powf(c.x, inv_gamma), powf(c.y, inv_gamma), powf(c.z, inv_gamma),
+                             transparent ? p.w * scale : 1.0f);
     }
 }
 
@@ -1110,9 +1137,9 @@ cudaError_t launch_finalize(const float4* psum, float4* rgba, uint32_t np, float
 }
 
 cudaError_t launch_tonemap(const float4* in, float4* out, uint32_t np, int32_t tonemap, float inv_gamma, float ex,
-                           float scale, cudaStream_t st) {
+                           float scale, int32_t transparent, cudaStream_t st) {
     if (np == 0) return cudaSuccess;
-    k_tonemap<<<grid_for(np, 256, 8), 256, 0, st>>>(in, out, np, tonemap, inv_gamma, ex, scale);
+    k_tonemap<<<grid_for(np, 256, 8), 256, 0, st>>>(in, out, np, tonemap, inv_gamma, ex, scale, transparent);
     return cudaGetLastError();
 }
 

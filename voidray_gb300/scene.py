@@ -134,9 +134,13 @@ class Material:
     transparent: bool = False
     albedo_texture: int = -1   # TextureHandle of ColorType::Texture, -1: use `color`
     normal_texture: int = -1   # TextureHandle of the normal map, -1: none
+    first: Optional["Material"] = None   # MixMaterial children and factor
+    second: Optional["Material"] = None
+    factor: float = 0.0
 
-    def to_c(self) -> N.vr_material:
+    def to_c(self, first: int = -1, second: int = -1) -> N.vr_material:
         m = N.vr_material()
+        m.mix_first, m.mix_second, m.mix_factor = int(first), int(second), float(self.factor)
         m.kind = self.kind
         for i in range(3):
             m.color[i] = float(self.color[i])
@@ -172,7 +176,8 @@ class ImageTexture:
         return ImageTexture(load_image_rgb32f(path), sample_type)
 
 
-LAMBERTIAN, METAL, DIELECTRIC, EMISSION, LAMBERTIAN_BSDF, MICROFACET = range(6)
+LAMBERTIAN, METAL, DIELECTRIC, EMISSION, LAMBERTIAN_BSDF, MICROFACET, MIX = range(7)
+MAX_MIX_DEPTH = 8  # VR_MAX_MIX_DEPTH
 
 
 class Materials:
@@ -212,6 +217,15 @@ class Materials:
     def lambertian_texture_no_normal(albedo: int) -> Material:
         """simple.rs:29-34."""
         return Material(LAMBERTIAN, np.zeros(3, np.float32), albedo_texture=int(albedo))
+
+    @staticmethod
+    def mix(first: Material, second: Material, factor: float) -> Material:
+        """MixMaterial::new(first, second, factor) of the legacy crate
+        (voidray/src/common/materials.rs:188-203): each hit draws u in [0, 1)
+        and shades with `first` when u >= factor, else with `second`."""
+        if not isinstance(first, Material) or not isinstance(second, Material):
+            raise VoidrayError(1, "MixMaterial children must be materials")
+        return Material(MIX, np.zeros(3, np.float32), first=first, second=second, factor=float(f32(factor)))
 
 
 class MicrofacetBSDF:
@@ -412,6 +426,33 @@ class Scene:
         self.materials.append(material)
         return len(self.materials) - 1
 
+    def flat_materials(self) -> list:
+        """The material table the library receives: the scene's materials at
+        their handles, then the children of MixMaterials (one entry per
+        distinct child object), as (material, first, second) index triples."""
+        out = [[m, -1, -1] for m in self.materials]
+        index = {id(m): i for i, m in enumerate(self.materials)}
+
+        def place(m: Material, depth: int) -> int:
+            if depth > MAX_MIX_DEPTH:
+                raise VoidrayError(1, f"MixMaterial nested deeper than {MAX_MIX_DEPTH} levels")
+            k = index.get(id(m))
+            if k is None:
+                k = index[id(m)] = len(out)
+                out.append([m, -1, -1])
+                expand(k, depth)
+            return k
+
+        def expand(k: int, depth: int) -> None:
+            m = out[k][0]
+            if m.kind == MIX:
+                out[k][1] = place(m.first, depth + 1)
+                out[k][2] = place(m.second, depth + 1)
+
+        for k in range(len(self.materials)):
+            expand(k, 0)
+        return [tuple(e) for e in out]
+
     def add_texture(self, texture: ImageTexture) -> int:
         """scene.rs: textures are addressed by TextureHandle."""
         self.textures.append(texture)
@@ -484,7 +525,8 @@ class Scene:
             d.num_vertices = len(m.positions)
             d.num_triangles = len(m.indices)
             d.material = mats[s]
-        cm = (N.vr_material * max(1, len(self.materials)))(*[m.to_c() for m in self.materials])
+        flat = self.flat_materials()
+        cm = (N.vr_material * max(1, len(flat)))(*[m.to_c(a, b) for m, a, b in flat])
         desc = N.vr_scene_desc()
         desc.meshes = C.addressof(meshes)
         desc.num_meshes = len(mesh_surfs)
@@ -498,7 +540,7 @@ class Scene:
         desc.num_textures = len(self.textures)
         keep.append(texs)
         desc.materials = C.addressof(cm)
-        desc.num_materials = len(self.materials)
+        desc.num_materials = len(flat)
         env = self.environment
         if env is not None:
             desc.environment.kind = env.kind
@@ -626,4 +668,29 @@ def tonemap(rgba: np.ndarray, cm: ColorManagementSettings, scale: float) -> np.n
     h, w = rgba.shape[0], rgba.shape[1]
     c = cm.to_c()
     check(lib().vr_tonemap(ptr(rgba), ptr(out), w, h, C.byref(c), float(scale)))
+    return out
+
+
+class LegacyTonemap(enum.IntEnum):
+    """The legacy crate's Tonemap (voidray/src/pipeline.rs:59-68), numbered as
+    its viewport shader numbers them (viewport_fragment.glsl:10-17)."""
+    NONE = 0
+    SimpleACES = 1
+    SimpleReinhard = 2
+    LumaReinhard = 3
+    LumaWhitePreservingReinhard = 4
+    RomBinDaHouse = 5
+    Filmic = 6
+    Uncharted2 = 7
+
+
+def tonemap_legacy(rgba: np.ndarray, tonemap: LegacyTonemap, gamma: float, exposure: float, transparent: bool,
+                   scale: float) -> np.ndarray:
+    """viewport_fragment.glsl:27-67 on the GPU: exposure is a linear factor,
+    Filmic ignores gamma, `transparent` keeps the scaled alpha."""
+    rgba = np.ascontiguousarray(rgba, dtype=np.float32)
+    out = np.empty_like(rgba)
+    h, w = rgba.shape[0], rgba.shape[1]
+    check(lib().vr_tonemap_legacy(ptr(rgba), ptr(out), w, h, int(tonemap), float(gamma), float(exposure),
+                                  int(bool(transparent)), float(scale)))
     return out

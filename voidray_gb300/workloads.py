@@ -351,3 +351,33 @@ def textured_scene(seed: int = 4):
     st = RenderSettings(total_samples=8, max_bounces=6, rr_depth=0, estimator=Estimator.REFERENCE,
                         firefly_clamp=float("inf"))
     return s, st
+
+
+def mix_scene(hdri: bool = False, seed: int = 5):
+    """Spheres and a box with MixMaterials of the legacy crate
+    (voidray/src/common/materials.rs:188-203): Lambertian/metal, nested
+    dielectric/Lambertian/emitter mixes and a mix whose children are shared,
+    over a ground plane."""
+    rng = np.random.default_rng(seed)
+    s = Scene()
+    red = Materials.lambertian((0.8, 0.25, 0.2))
+    gold = Materials.metal((0.9, 0.75, 0.4), 0.2)
+    glass = Materials.dielectric(1.5)
+    lamp = Materials.colored_emissive((3.0, 2.5, 2.0), 1.0)
+    m0 = s.add_material(Materials.mix(red, gold, 0.3))
+    m1 = s.add_material(Materials.mix(Materials.mix(glass, red, 0.5), lamp, 0.1))
+    m2 = s.add_material(Materials.mix(gold, gold, 0.7))
+    grey = s.add_material(Materials.lambertian((0.6, 0.6, 0.6)))
+    s.add_object(grey, s.add_analytic_surface(Surfaces.ground_plane(-1.0)))
+    for k in range(5):
+        c = (float(rng.uniform(-2, 2)), float(rng.uniform(-0.6, 0.4)), float(rng.uniform(-2.5, 0.5)))
+        s.add_object([m0, m1, m2][k % 3], s.add_analytic_surface(Surfaces.sphere(c, float(rng.uniform(0.25, 0.5)))))
+    s.add_object(m0, s.add_mesh(_box_mesh((0.9, -0.6, -1.0), (0.6, 0.8, 0.6), 20.0)))
+    if hdri:
+        s.environment = Environments.hdri_image(sky_hdri(128, 64, peak=200.0, sigma_deg=4.0))
+    else:
+        s.environment = Environments.uniform((0.5, 0.6, 0.8))
+    s.camera = Camera.look_at((0.0, 0.6, 4.0), (0.0, -0.3, -0.8), (0.0, 1.0, 0.0), degrees_to_radians(55.0))
+    st = RenderSettings(total_samples=16, max_bounces=8, rr_depth=0, estimator=Estimator.REFERENCE,
+                        firefly_clamp=float("inf"))
+    return s, st
