@@ -20,10 +20,25 @@
 //
 // Every mbarrier wait is bounded: a wait that runs out sets an error bit in
 // the caller's status word and the CTA still drains and frees its TMEM.
+//
+// k_conv3x3_halo is the default variant.  Its tile is 16 rows x 8 columns of
+// output pixels (M = 128, one 8-pixel row segment per 8-row core matrix).
+// Per K chunk it loads one 18 x 10 halo of the input (BK/8 TMA boxes of
+// 8 channels x 10 x 18) into the no-swizzle canonical K-major layout
+// [channel group][halo pixel][8 channels]: the nine taps are then nine
+// descriptor start addresses into the same buffer (start + (dy * 10 + dx) *
+// 16 B; leading byte offset = one channel group, stride byte offset = one
+// halo row), so each input pixel is staged 1.4 times instead of 9 times.
+// When the CTA's weight slice fits it is loaded once and stays resident; the
+// CTAs are persistent over tiles, and the accumulator is double-buffered in
+// TMEM so that the epilogue of one tile overlaps the MMAs of the next.  Warp
+// roles: warp 0 TMA producer, warp 1 MMA issuer, warps 2-5 epilogue.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 
 #include "dn_kernels.h"
@@ -93,6 +108,28 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t row_bytes
     d |= 1ull << 46;
     d |= swz << 61;
     return d;
+}
+
+// Descriptor of a K-major operand in the no-swizzle canonical layout: core
+// matrices of 8 rows x 16 B stored contiguously; `lbo` = byte distance of
+// core matrices adjacent in K, `sbo` = of core matrices adjacent in M/N.
+__device__ __forceinline__ uint64_t smem_desc_noswz(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+    d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+    d |= 1ull << 46;
+    return d;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                     smem_addr(bar))
+                 : "memory");
 }
 
 // Instruction descriptor, kind::f16: fp32 accumulator, bf16 A and B, both
@@ -271,6 +308,251 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
+
+// ---------------------------------------------------------- halo variant --
+constexpr int HALO_THREADS = 192;
+constexpr int HALO_MAX_STAGES = 4;
+constexpr int HALO_W = 10, HALO_H = 18, HALO_PIX = HALO_W * HALO_H;  // 16 x 8 outputs + 1-pixel border
+constexpr uint32_t HALO_GROUP_BYTES = HALO_PIX * 16u;                 // one 8-channel group
+
+struct HaloArgs {
+    const float* bias;
+    const bf16* mask;
+    bf16* out;
+    float* out_f32;
+    uint32_t* status;
+    int n, h, w;
+    int c1, cin, cout;
+    int ntile, bk, stages, resident;
+    int relu;
+    int tiles_x, tiles_y, ntiles;
+    uint32_t a_stage;  // bytes per A stage (bk / 8 channel groups of a halo, rounded to 1024)
+    uint32_t b_box;    // bytes per weight box (ntile x bk, rounded to 1024)
+    uint32_t b_off;    // offset of the weight region
+};
+
+// bias, ReLU, ReLU-backward mask and the bf16 / fp32 store of 16 accumulator
+// columns of one pixel
+__device__ __forceinline__ void store16(const HaloArgs& a, const uint32_t* r, size_t pix, int ch) {
+    float v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        v[j] = __uint_as_float(r[j]) + (a.bias ? a.bias[ch + j] : 0.0f);
+        if (a.relu) v[j] = fmaxf(v[j], 0.0f);
+    }
+    const size_t o0 = pix * (size_t)a.cout + ch;
+    if (a.mask) {
+        union {
+            uint4 u[2];
+            bf16 h[16];
+        } mk;
+        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + o0);
+        mk.u[0] = mp[0];
+        mk.u[1] = mp[1];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (!(__bfloat162float(mk.h[j]) > 0.0f)) v[j] = 0.0f;
+    }
+    if (a.out_f32) {
+        float4* o = reinterpret_cast<float4*>(a.out_f32 + o0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    } else {
+        union {
+            uint4 u[2];
+            bf16 h[16];
+        } pk;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) pk.h[j] = __float2bfloat16_rn(v[j]);
+        uint4* o = reinterpret_cast<uint4*>(a.out + o0);
+        o[0] = pk.u[0];
+        o[1] = pk.u[1];
+    }
+}
+
+__device__ __forceinline__ void halo_tile(const HaloArgs& a, int t, int& img, int& y0, int& x0) {
+    x0 = (t % a.tiles_x) * 8;
+    t /= a.tiles_x;
+    y0 = (t % a.tiles_y) * 16;
+    img = t / a.tiles_y;
+}
+
+__global__ void __launch_bounds__(HALO_THREADS, 1)
+    k_conv3x3_halo(const __grid_constant__ CUtensorMap map_a1, const __grid_constant__ CUtensorMap map_a2,
+                   const __grid_constant__ CUtensorMap map_b, const HaloArgs a) {
+    extern __shared__ __align__(1024) uint8_t dsmem[];
+    __shared__ uint64_t full_bar[HALO_MAX_STAGES], empty_bar[HALO_MAX_STAGES];
+    __shared__ uint64_t acc_full[2], acc_empty[2], w_bar, mma_done;
+    __shared__ uint32_t tmem_base;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = a.ntile;
+    const int n0 = blockIdx.y * N;
+    const int S = a.stages;
+    const int KG = a.cin / a.bk;  // K chunks per tile
+    const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
+    const uint32_t tmem_cols = 2u * ncols;  // two accumulators
+    const uint32_t wbox_bytes = (uint32_t)N * a.bk * 2u;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 4);
+        }
+        mbar_init(&w_bar, 1);
+        mbar_init(&mma_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&tmem_base)),
+                     "r"(tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // ------------------------------------------------ TMA producer
+        if (a.resident) {
+            mbar_expect_tx(&w_bar, (uint32_t)KG * 9u * wbox_bytes);
+            for (int kg = 0; kg < KG; ++kg)
+                for (int tap = 0; tap < 9; ++tap)
+                    tma_load_2d(smem + a.b_off + (size_t)(kg * 9 + tap) * a.b_box, &map_b, &w_bar,
+                                tap * a.cin + kg * a.bk, n0);
+        }
+        const uint32_t a_tx = (uint32_t)(a.bk / 8) * HALO_GROUP_BYTES;
+        const uint32_t tx = a_tx + (a.resident ? 0u : 9u * wbox_bytes);
+        uint32_t it = 0;
+        for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+            int img, y0, x0;
+            halo_tile(a, t, img, y0, x0);
+            for (int kg = 0; kg < KG; ++kg, ++it) {
+                const int s = (int)(it % (uint32_t)S);
+                if (it >= (uint32_t)S && !mbar_wait(&empty_bar[s], ((it / S) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* sa = smem + (size_t)s * a.a_stage;
+                mbar_expect_tx(&full_bar[s], tx);
+                const int c0 = kg * a.bk;
+                for (int g = 0; g < a.bk / 8; ++g) {
+                    const int cc = c0 + 8 * g;
+                    if (cc < a.c1) tma_load_4d(sa + g * HALO_GROUP_BYTES, &map_a1, &full_bar[s], cc, x0 - 1, y0 - 1, img);
+                    else tma_load_4d(sa + g * HALO_GROUP_BYTES, &map_a2, &full_bar[s], cc - a.c1, x0 - 1, y0 - 1, img);
+                }
+                if (!a.resident)
+                    for (int tap = 0; tap < 9; ++tap)
+                        tma_load_2d(smem + a.b_off + (size_t)(s * 9 + tap) * a.b_box, &map_b, &full_bar[s],
+                                    tap * a.cin + c0, n0);
+            }
+        }
+        // no copy may still be in flight when the CTA exits: wait for the last
+        // phase of every stage this thread filled (bounded)
+        const uint32_t first = it > (uint32_t)S ? it - S : 0u;
+        for (uint32_t j = first; j < it; ++j)
+            if (!mbar_wait(&full_bar[j % S], (j / S) & 1)) ok = false;
+        if (a.resident && !mbar_wait(&w_bar, 0)) ok = false;
+    } else if (warp == 1 && lane == 0) {
+        // ------------------------------------------------ MMA issuer
+        const uint32_t idesc = instr_desc(128, (uint32_t)N);
+        const uint32_t row_bytes = (uint32_t)a.bk * 2u;
+        if (a.resident && !mbar_wait(&w_bar, 0)) ok = false;
+        uint32_t it = 0;
+        int local = 0;
+        for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, ++local) {
+            const int acc = local & 1;
+            if (local >= 2 && !mbar_wait(&acc_empty[acc], ((local >> 1) & 1) ^ 1)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t d_tmem = tmem + (uint32_t)acc * ncols;
+            for (int kg = 0; kg < KG; ++kg, ++it) {
+                const int s = (int)(it % (uint32_t)S);
+                if (!mbar_wait(&full_bar[s], (it / S) & 1)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t sa = smem_addr(smem + (size_t)s * a.a_stage);
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int dy = tap / 3, dx = tap % 3;
+                    const uint32_t sb =
+                        smem_addr(smem + a.b_off + (size_t)((a.resident ? kg : s) * 9 + tap) * a.b_box);
+                    for (int kk = 0; kk < a.bk / 16; ++kk) {
+                        const uint64_t da = smem_desc_noswz(sa + (uint32_t)(dy * HALO_W + dx) * 16u +
+                                                                (uint32_t)kk * 2u * HALO_GROUP_BYTES,
+                                                            HALO_GROUP_BYTES, HALO_W * 16u);
+                        const uint64_t db = smem_desc(sb + kk * 32, row_bytes);
+                        const uint32_t accum = (kg > 0 || tap > 0 || kk > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+                            "l"(da), "l"(db), "r"(idesc), "r"(accum));
+                    }
+                }
+                mma_commit(&empty_bar[s]);  // frees the stage once these MMAs have read it
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[acc]);
+        }
+        mma_commit(&mma_done);  // arrives when every MMA above has completed
+    } else if (warp >= 2) {
+        // ------------------------------------------------ epilogue (warps 2-5)
+        const int q = warp & 3;  // TMEM lane quadrant this warp may read
+        const int m = q * 32 + lane;
+        int local = 0;
+        for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++local) {
+            const int acc = local & 1;
+            if (!mbar_wait(&acc_full[acc], (local >> 1) & 1)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            int img, y0, x0;
+            halo_tile(a, t, img, y0, x0);
+            const int y = y0 + (m >> 3), x = x0 + (m & 7);
+            const bool in_img = y < a.h && x < a.w;
+            const size_t pix = ((size_t)img * a.h + y) * a.w + x;
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                uint32_t r[16];
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)acc * ncols + (uint32_t)c0;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (in_img) store16(a, r, pix, n0 + c0);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+        }
+    }
+    if (!ok && a.status) atomicOr(a.status, 1u);
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        // every MMA has completed before the accumulator is freed (bounded wait)
+        const bool drained = mbar_wait(&mma_done, 0);
+        if (!drained && lane == 0 && a.status) atomicOr(a.status, 2u);
+        __syncwarp();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tmem_cols));
+    }
+}
+
 // ------------------------------------------------------------- host side --
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -308,6 +590,18 @@ bool encode_act(CUtensorMap* m, const bf16* p, int n, int h, int w, int c, int b
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// NHWC activation as a 4-D map with halo boxes of 8 channels x 10 x 18 x 1,
+// unswizzled: a box lands as [18][10][8 channels], one core-matrix row per pixel
+bool encode_act_halo(CUtensorMap* m, const bf16* p, int n, int h, int w, int c) {
+    const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)c * w * 2, (cuuint64_t)c * w * h * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)HALO_W, (cuuint32_t)HALO_H, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(p), dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // weights [cout][9 * cin] as a 2-D map with boxes of bk x ntile
 bool encode_wgt(CUtensorMap* m, const bf16* p, int cout, int cin, int bk, int ntile) {
     const cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};
@@ -342,8 +636,129 @@ bool conv3x3_tc_supported(const ConvArgs& a) {
     return true;
 }
 
+namespace {
+
+constexpr size_t HALO_SMEM_BUDGET = 200 * 1024;
+constexpr size_t HALO_RESIDENT_MAX = 128 * 1024;
+
+size_t round1k(size_t x) { return (x + 1023) & ~size_t(1023); }
+
+struct HaloPlan {
+    int bk = 0, stages = 0, resident = 0;
+    size_t a_stage = 0, b_box = 0, b_off = 0, smem = 0;
+};
+
+// chunk size, stage count and weight residency within the shared-memory budget:
+// resident weights when they fit in 128 KB with at least two A stages beside
+// them, else streamed weights with the largest chunk that leaves two stages
+HaloPlan plan_halo(int c1, int c2, int ntile) {
+    const int cin = c1 + c2;
+    HaloPlan p;
+    for (int bk = 64; bk >= 16; bk >>= 1) {
+        if (c1 % bk || c2 % bk) continue;
+        const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
+        const size_t b_box = round1k((size_t)ntile * bk * 2);
+        const size_t w = (size_t)(cin / bk) * 9 * b_box;
+        if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= HALO_SMEM_BUDGET) {
+            p.bk = bk;
+            p.resident = 1;
+            p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, (HALO_SMEM_BUDGET - w) / a_stage);
+            p.a_stage = a_stage;
+            p.b_box = b_box;
+            p.b_off = (size_t)p.stages * a_stage;
+            p.smem = p.b_off + w + 1024;
+            return p;
+        }
+    }
+    for (int bk = 64; bk >= 16; bk >>= 1) {
+        if (c1 % bk || c2 % bk) continue;
+        const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
+        const size_t b_box = round1k((size_t)ntile * bk * 2);
+        const size_t stage = a_stage + 9 * b_box;
+        if (2 * stage > HALO_SMEM_BUDGET) continue;
+        p.bk = bk;
+        p.resident = 0;
+        p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, HALO_SMEM_BUDGET / stage);
+        p.a_stage = a_stage;
+        p.b_box = b_box;
+        p.b_off = (size_t)p.stages * a_stage;
+        p.smem = p.b_off + (size_t)p.stages * 9 * b_box + 1024;
+        return p;
+    }
+    return p;
+}
+
+bool use_tile_variant() {
+    static const int v = [] {
+        const char* e = std::getenv("VR_DN_TC_VARIANT");
+        return (e && std::strcmp(e, "tile") == 0) ? 1 : 0;
+    }();
+    return v == 1;
+}
+
+cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
+    const int cin = a.c1 + a.c2;
+    const int ntile = ntile_for(a.cout);
+    const HaloPlan pl = plan_halo(a.c1, a.c2, ntile);
+    if (!pl.bk) return cudaErrorInvalidValue;
+    CUtensorMap ma1, ma2, mb;
+    std::memset(&ma2, 0, sizeof ma2);
+    if (!encode_act_halo(&ma1, a.src1, a.n, a.h, a.w, a.c1)) return cudaErrorInvalidValue;
+    if (a.c2 && !encode_act_halo(&ma2, a.src2, a.n, a.h, a.w, a.c2)) return cudaErrorInvalidValue;
+    if (!a.c2) ma2 = ma1;
+    if (!encode_wgt(&mb, a.weight, a.cout, cin, pl.bk, ntile)) return cudaErrorInvalidValue;
+    HaloArgs t{};
+    t.bias = a.bias;
+    t.mask = a.mask;
+    t.out = a.out;
+    t.out_f32 = a.out_f32;
+    t.status = status;
+    t.n = a.n;
+    t.h = a.h;
+    t.w = a.w;
+    t.c1 = a.c1;
+    t.cin = cin;
+    t.cout = a.cout;
+    t.ntile = ntile;
+    t.bk = pl.bk;
+    t.stages = pl.stages;
+    t.resident = pl.resident;
+    t.relu = a.relu;
+    t.tiles_x = (a.w + 7) / 8;
+    t.tiles_y = (a.h + 15) / 16;
+    t.ntiles = t.tiles_x * t.tiles_y * a.n;
+    t.a_stage = (uint32_t)pl.a_stage;
+    t.b_box = (uint32_t)pl.b_box;
+    t.b_off = (uint32_t)pl.b_off;
+    static size_t configured = 0;
+    if (pl.smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+        if (e != cudaSuccess) return e;
+        configured = pl.smem;
+    }
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_halo, HALO_THREADS, pl.smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const int ncols = ntile <= 32 ? 32 : ntile <= 64 ? 64 : ntile <= 128 ? 128 : 256;
+    per_sm = std::min(per_sm, 512 / (2 * ncols));  // the accumulators of co-resident CTAs fit in TMEM
+    const int ny = a.cout / ntile;
+    const int gx = std::max(1, std::min(t.ntiles, (sms * per_sm + ny - 1) / ny));
+    k_conv3x3_halo<<<dim3((unsigned)gx, (unsigned)ny), HALO_THREADS, pl.smem, st>>>(ma1, ma2, mb, t);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (!conv3x3_tc_supported(a)) return cudaErrorInvalidValue;
+    if (!use_tile_variant()) return conv3x3_halo(a, status, st);
     const int cin = a.c1 + a.c2;
     // largest chunk that divides both sources (a chunk never straddles them)
     int bk = 64;
