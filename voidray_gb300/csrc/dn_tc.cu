@@ -313,7 +313,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 constexpr int HALO_THREADS = 192;
 constexpr int HALO_MAX_STAGES = 4;
 constexpr int HALO_W = 10, HALO_H = 18, HALO_PIX = HALO_W * HALO_H;  // 16 x 8 outputs + 1-pixel border
-constexpr uint32_t HALO_GROUP_BYTES = HALO_PIX * 16u;                 // one 8-channel group
+constexpr uint32_t HALO_BOX_BYTES = HALO_PIX * 16u;                   // one 8-channel group: 2880 B
+// distance between channel groups: a TMA tensor copy writes to a 128-byte
+// aligned shared-memory address, so each group starts on a 128-byte boundary
+constexpr uint32_t HALO_GROUP_BYTES = (HALO_BOX_BYTES + 127u) & ~127u;  // 2944 B
+static_assert(HALO_GROUP_BYTES % 128u == 0, "TMA destinations are 128-byte aligned");
 
 struct HaloArgs {
     const float* bias;
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(HALO_THREADS, 1)
                     tma_load_2d(smem + a.b_off + (size_t)(kg * 9 + tap) * a.b_box, &map_b, &w_bar,
                                 tap * a.cin + kg * a.bk, n0);
         }
-        const uint32_t a_tx = (uint32_t)(a.bk / 8) * HALO_GROUP_BYTES;
+        const uint32_t a_tx = (uint32_t)(a.bk / 8) * HALO_BOX_BYTES;
         const uint32_t tx = a_tx + (a.resident ? 0u : 9u * wbox_bytes);
         uint32_t it = 0;
         for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {

@@ -302,7 +302,7 @@ def spheres_scene(ground: bool = True, hdri: bool = False, seed: int = 3):
     for k in range(6):
         c = (float(rng.uniform(-2, 2)), float(rng.uniform(-0.7, 0.5)), float(rng.uniform(-2.5, 0.5)))
         s.add_object(mats[k % 4], s.add_analytic_surface(Surfaces.sphere(c, float(rng.uniform(0.2, 0.5)))))
-    s.add_object(grey, s.add_mesh(_box_mesh((0.9, -0.6, -1.0), (0.6, 0.8, 0.6), 20.0)))
+    s.add_object(grey, s.add_mesh(_box_mesh((0.9, -0.55, -1.0), (0.6, 0.8, 0.6), 20.0)))
     if hdri:
         s.environment = Environments.hdri_image(sky_hdri(128, 64, peak=200.0, sigma_deg=4.0))
     else:
@@ -372,7 +372,7 @@ def mix_scene(hdri: bool = False, seed: int = 5):
     for k in range(5):
         c = (float(rng.uniform(-2, 2)), float(rng.uniform(-0.6, 0.4)), float(rng.uniform(-2.5, 0.5)))
         s.add_object([m0, m1, m2][k % 3], s.add_analytic_surface(Surfaces.sphere(c, float(rng.uniform(0.25, 0.5)))))
-    s.add_object(m0, s.add_mesh(_box_mesh((0.9, -0.6, -1.0), (0.6, 0.8, 0.6), 20.0)))
+    s.add_object(m0, s.add_mesh(_box_mesh((0.9, -0.55, -1.0), (0.6, 0.8, 0.6), 20.0)))
     if hdri:
         s.environment = Environments.hdri_image(sky_hdri(128, 64, peak=200.0, sigma_deg=4.0))
     else:
