@@ -354,6 +354,31 @@ vr_status vr_tuning_set(const vr_tuning* tuning);
 vr_status vr_batch_set_graphs(vr_batch* batch, int32_t enable);
 vr_status vr_batch_graph_stats(vr_batch* batch, uint64_t* captures, uint64_t* replays);
 
+/* --------------------------------------------------------- serving stats --
+ * Per-pass error statistics of many progressive jobs in one launch (no
+ * reference counterpart; used by the serving loop).  Each job keeps two
+ * half-buffers of RGBA f32 sample sums A and B (n_a, n_b samples) and, when
+ * it is denoised, the denoiser outputs DA, DB of the half means.  With
+ * a = A/n_a, b = B/n_b, m = (A + B)/(n_a + n_b), d = m^2 + 1e-2 and the sums
+ * over RGB, the kernel writes for every 16 x 16 pixel tile t of job j, at
+ * out[tile_offset + k * tiles + t] (tiles = ceil(h/16) * ceil(w/16)):
+ *   k = 0: SUM over the tile of (a-b)^2 n_a n_b / n^2 / d   (the plain estimate)
+ *   k = 1..5 (denoised jobs only): MEANS over the tile's pixels and channels
+ *          of (a-b)^2/d, (DA-b)^2/d, (DB-a)^2/d, (DA-DB)^2/d, (DA-DB)(a-b)/d.
+ * Sums are in fp64 in a fixed order (deterministic). */
+typedef struct vr_stats_job {
+    const float* sum_a;
+    const float* sum_b;
+    const float* den_a;       /* NULL: plain statistic only                     */
+    const float* den_b;
+    uint32_t n_a, n_b;
+    uint32_t width, height;
+    uint64_t tile_offset;
+} vr_stats_job;
+#define VR_STATS_TILE 16
+#define VR_STATS_MAX_JOBS 128  /* per call */
+vr_status vr_serve_stats_device(const vr_stats_job* jobs, uint32_t count, double* out_device, void* stream);
+
 typedef struct vr_render_stats {
     uint64_t paths;          /* camera paths traced                            */
     uint64_t extend_rays;    /* closest-hit rays                               */

@@ -23,16 +23,22 @@ def test_mix_scene_bit_parity(gpu, oracle):
 def test_mix_scene_nee_matches_reference_estimator(gpu):
     """With the NEE estimator under an importance-sampled HDRI, mixed
     Lambertian vertices take light samples; both estimators converge to the
-    same image."""
+    same image.  The reference estimator rarely finds the small sun, so its
+    own noise dominates: on the oracle, two reference renders of this scene
+    differ by relMSE 0.36 at 256 spp and 0.07 at 1024, NEE against reference
+    by 0.10 and 0.030 (the 1/spp decay of noise, no bias); at 4096 spp the
+    expected gap is about 0.008."""
     s, st = W.mix_scene(hdri=True)
     acc = s.build_acceleration()
-    st.total_samples = 256
-    ref = gpu_render(s, st, 256, 32, 24, acc=acc)
+    spp = 4096
+    st.total_samples = spp
+    ref = gpu_render(s, st, spp, 32, 24, acc=acc, seed=1)
     st.estimator = vr.Estimator.NEE
-    nee = gpu_render(s, st, 256, 32, 24, acc=acc)
+    nee = gpu_render(s, st, spp, 32, 24, acc=acc, seed=2)
     a, b = ref[..., :3].astype(np.float64), nee[..., :3].astype(np.float64)
     rel = np.mean((a - b) ** 2 / (b ** 2 + 1e-2))
-    assert rel < 0.05, rel
+    assert rel < 0.025, rel
+    assert abs(a.mean() - b.mean()) < 0.01 * b.mean()
 
 
 @pytest.mark.parametrize("tm", range(8))

@@ -86,3 +86,51 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
         assert np.array_equal(r0[0], r1[0])
     finally:
         net.destroy()
+
+
+@pytest.mark.parametrize("denoised", [False, True])
+def test_stats_kernel_matches_numpy(gpu, denoised):
+    """vr_serve_stats_device against the numpy formulas the CPU scheduler uses
+    (_estimate and blend_tile_moments): ragged tiles, several jobs of
+    different sizes and sample counts in one launch."""
+    import ctypes as C
+
+    import torch
+
+    from voidray_gb300 import _native as N
+    from voidray_gb300.serve import BLEND_TILE, _estimate, blend_tile_moments
+
+    rng = np.random.default_rng(3)
+    shapes = [(40, 24, 8, 8), (17, 33, 5, 12), (64, 64, 32, 32)]
+    bufs, table, offs, off = [], (N.vr_stats_job * len(shapes))(), [], 0
+    for i, (h, w, na, nb) in enumerate(shapes):
+        A = (rng.gamma(1.0, 0.4, (h, w, 4)) * na).astype(np.float32)
+        B = (rng.gamma(1.0, 0.4, (h, w, 4)) * nb).astype(np.float32)
+        DA = rng.gamma(1.0, 0.4, (h, w, 4)).astype(np.float32)
+        DB = rng.gamma(1.0, 0.4, (h, w, 4)).astype(np.float32)
+        t = [torch.from_numpy(x).cuda() for x in (A, B, DA, DB)]
+        bufs.append((A, B, DA, DB, t))
+        e = table[i]
+        e.sum_a, e.sum_b = t[0].data_ptr(), t[1].data_ptr()
+        e.den_a, e.den_b = (t[2].data_ptr(), t[3].data_ptr()) if denoised else (None, None)
+        e.n_a, e.n_b, e.width, e.height, e.tile_offset = na, nb, w, h, off
+        nt = -(-h // BLEND_TILE) * -(-w // BLEND_TILE)
+        offs.append((off, nt))
+        off += (6 if denoised else 1) * nt
+    out = torch.full((off,), -1.0, dtype=torch.float64, device="cuda")
+    N.check(N.lib().vr_serve_stats_device(table, len(shapes), C.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    v = out.cpu().numpy()
+    for (h, w, na, nb), (A, B, DA, DB, _), (o, nt) in zip(shapes, bufs, offs):
+        a, b = A[..., :3].astype(np.float64) / na, B[..., :3].astype(np.float64) / nb
+        plain = float(v[o:o + nt].sum()) / (3 * h * w)
+        assert plain == pytest.approx(_estimate(a, b, na, nb), rel=1e-12)
+        if denoised:
+            m = (A[..., :3].astype(np.float64) + B[..., :3]) / (na + nb)
+            ref = blend_tile_moments(a, b, m, DA[..., :3].astype(np.float64), DB[..., :3].astype(np.float64))
+            got = v[o + nt:o + 6 * nt].reshape(ref.shape)
+            assert np.allclose(got, ref, rtol=1e-12, atol=0)
+    out2 = torch.full((off,), -1.0, dtype=torch.float64, device="cuda")
+    N.check(N.lib().vr_serve_stats_device(table, len(shapes), C.c_void_p(out2.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert np.array_equal(out2.cpu().numpy(), v)   # deterministic

@@ -106,6 +106,16 @@ class vr_denoiser_layer(C.Structure):
                 ("relu", C.c_uint32), ("level", C.c_uint32), ("w_offset", C.c_uint64), ("b_offset", C.c_uint64)]
 
 
+class vr_stats_job(C.Structure):
+    _fields_ = [("sum_a", C.c_void_p), ("sum_b", C.c_void_p), ("den_a", C.c_void_p), ("den_b", C.c_void_p),
+                ("n_a", C.c_uint32), ("n_b", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("tile_offset", C.c_uint64)]
+
+
+STATS_TILE = 16
+STATS_MAX_JOBS = 128
+
+
 class vr_tuning(C.Structure):
     _fields_ = [("shade_block", C.c_uint32), ("shade_blocks_per_sm", C.c_uint32), ("raygen_block", C.c_uint32),
                 ("generation", C.c_uint32)]
@@ -157,6 +167,7 @@ _SIGS = [
     ("vr_tuning_set", C.c_int, [P]),
     ("vr_batch_set_graphs", C.c_int, [P, C.c_int32]),
     ("vr_batch_graph_stats", C.c_int, [P, P, P]),
+    ("vr_serve_stats_device", C.c_int, [P, C.c_uint32, P, P]),
     ("vr_batch_stats_get", C.c_int, [P, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),

@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libvoidray_gb300.so"
 
-SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu"]
+SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "vr_serve.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
