@@ -2,6 +2,10 @@
 FP64 CPU restatement, with the same bound as the mma.sync kernel: half a bf16
 ulp of the exact result plus the fp32 accumulation error; and the whole
 network's forward pass on tcgen05 against its mma.sync forward pass."""
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 
@@ -54,6 +58,18 @@ def test_conv3x3_tc_matches_fp64(gpu, case):
     tol = (0.0 if f32 else 0.5 * ulp_bf16(y)) + 2.0 ** -20 * s + 1e-30
     bad = np.abs(g - y) > tol
     assert not bad.any(), (np.argwhere(bad)[:5], g[bad][:5], y[bad][:5])
+
+
+@pytest.mark.parametrize("variant", ["tile", "halo"])
+def test_conv3x3_tc_each_variant_on_every_case(gpu, variant):
+    """The library picks the tile or the halo kernel by output-channel count;
+    forcing one variant (VR_DN_TC_VARIANT, read once per process) runs every
+    case above through it, in a child process."""
+    env = dict(os.environ, VR_DN_TC_VARIANT=variant)
+    r = subprocess.run([sys.executable, "-m", "pytest", os.path.abspath(__file__), "-q", "-p", "no:cacheprovider",
+                        "-k", "test_conv3x3_tc_matches_fp64"], env=env, capture_output=True, text=True,
+                       timeout=900, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
 
 
 def test_tc_rejects_what_it_does_not_cover(gpu):

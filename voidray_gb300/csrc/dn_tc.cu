@@ -692,12 +692,20 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
     return p;
 }
 
-bool use_tile_variant() {
-    static const int v = [] {
+// Variant per shape, from per-layer launch lists of the 1080p forward pass on
+// GB300: the halo kernel is 10-40% faster where a CTA computes 64 or 128
+// output channels; with 16 or 32 its 16-byte TMA rows cannot keep the tensor
+// pipe busy and with 256 the streamed weights dominate, so those shapes run
+// the tile kernel.  VR_DN_TC_VARIANT=tile / halo forces one variant.
+bool use_tile_variant(int ntile) {
+    static const int forced = [] {
         const char* e = std::getenv("VR_DN_TC_VARIANT");
-        return (e && std::strcmp(e, "tile") == 0) ? 1 : 0;
+        if (e && std::strcmp(e, "tile") == 0) return 1;
+        if (e && std::strcmp(e, "halo") == 0) return 2;
+        return 0;
     }();
-    return v == 1;
+    if (forced) return forced == 1;
+    return !(ntile >= 64 && ntile <= 128);
 }
 
 cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
@@ -762,7 +770,7 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
 
 cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (!conv3x3_tc_supported(a)) return cudaErrorInvalidValue;
-    if (!use_tile_variant()) return conv3x3_halo(a, status, st);
+    if (!use_tile_variant(ntile_for(a.cout))) return conv3x3_halo(a, status, st);
     const int cin = a.c1 + a.c2;
     // largest chunk that divides both sources (a chunk never straddles them)
     int bk = 64;
