@@ -21,14 +21,14 @@
 // Every mbarrier wait is bounded: a wait that runs out sets an error bit in
 // the caller's status word and the CTA still drains and frees its TMEM.
 //
-// k_conv3x3_halo, the variant for 64-128 output channels per CTA: its tile
-// is 16 rows x 8 columns of output pixels (M = 128, one 8-pixel row segment
-// per 8-row group).  Per K chunk of BK channels it loads one 18 x 10 halo of
-// the input with a single TMA box (BK channels x 10 x 18) into the same
-// swizzled K-major layout as the tile boxes, one row per halo pixel: the
-// nine taps are then nine descriptor start addresses into that buffer
-// (start + (dy * 10 + dx) rows, stride byte offset = one halo row of 10
-// rows), so each input pixel is staged 1.4 times instead of 9 times.
+// k_conv3x3_halo is the default variant.  Its tile is 16 rows x 8 columns of
+// output pixels (M = 128, one 8-pixel row segment per 8-row core matrix).
+// Per K chunk it loads one 18 x 10 halo of the input (BK/8 TMA boxes of
+// 8 channels x 10 x 18) into the no-swizzle canonical K-major layout
+// [channel group][halo pixel][8 channels]: the nine taps are then nine
+// descriptor start addresses into the same buffer (start + (dy * 10 + dx) *
+// 16 B; leading byte offset = one channel group, stride byte offset = one
+// halo row), so each input pixel is staged 1.4 times instead of 9 times.
 // When the CTA's weight slice fits it is loaded once and stays resident; the
 // CTAs are persistent over tiles, and the accumulator is double-buffered in
 // TMEM so that the epilogue of one tile overlaps the MMAs of the next.  Warp
@@ -110,19 +110,15 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t row_bytes
     return d;
 }
 
-// Swizzled K-major descriptor with an explicit stride byte offset (distance
-// of 8-row groups): the halo operand's 8-row groups are one halo row apart.
-// The swizzle is a function of the shared-memory address bits, the same one
-// TMA applied when it wrote the rows, so a start address inside a swizzle
-// atom (a tap shift, a K step) reads the rows as written.
-__device__ __forceinline__ uint64_t smem_desc_sbo(uint32_t saddr, uint32_t row_bytes, uint32_t sbo) {
-    const uint64_t swz = row_bytes == 128 ? 2ull : row_bytes == 64 ? 4ull : 6ull;
+// Descriptor of a K-major operand in the no-swizzle canonical layout: core
+// matrices of 8 rows x 16 B stored contiguously; `lbo` = byte distance of
+// core matrices adjacent in K, `sbo` = of core matrices adjacent in M/N.
+__device__ __forceinline__ uint64_t smem_desc_noswz(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
     d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
     d |= 1ull << 46;
-    d |= swz << 61;
     return d;
 }
 
@@ -317,6 +313,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 constexpr int HALO_THREADS = 192;
 constexpr int HALO_MAX_STAGES = 4;
 constexpr int HALO_W = 10, HALO_H = 18, HALO_PIX = HALO_W * HALO_H;  // 16 x 8 outputs + 1-pixel border
+constexpr uint32_t HALO_BOX_BYTES = HALO_PIX * 16u;                   // one 8-channel group: 2880 B
+// distance between channel groups: a TMA tensor copy writes to a 128-byte
+// aligned shared-memory address, so each group starts on a 128-byte boundary
+constexpr uint32_t HALO_GROUP_BYTES = (HALO_BOX_BYTES + 127u) & ~127u;  // 2944 B
+static_assert(HALO_GROUP_BYTES % 128u == 0, "TMA destinations are 128-byte aligned");
 
 struct HaloArgs {
     const float* bias;
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(HALO_THREADS, 1)
                     tma_load_2d(smem + a.b_off + (size_t)(kg * 9 + tap) * a.b_box, &map_b, &w_bar,
                                 tap * a.cin + kg * a.bk, n0);
         }
-        const uint32_t a_tx = (uint32_t)HALO_PIX * (uint32_t)a.bk * 2u;
+        const uint32_t a_tx = (uint32_t)(a.bk / 8) * HALO_BOX_BYTES;
         const uint32_t tx = a_tx + (a.resident ? 0u : 9u * wbox_bytes);
         uint32_t it = 0;
         for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
@@ -445,8 +446,11 @@ __global__ void __launch_bounds__(HALO_THREADS, 1)
                 uint8_t* sa = smem + (size_t)s * a.a_stage;
                 mbar_expect_tx(&full_bar[s], tx);
                 const int c0 = kg * a.bk;
-                if (c0 < a.c1) tma_load_4d(sa, &map_a1, &full_bar[s], c0, x0 - 1, y0 - 1, img);
-                else tma_load_4d(sa, &map_a2, &full_bar[s], c0 - a.c1, x0 - 1, y0 - 1, img);
+                for (int g = 0; g < a.bk / 8; ++g) {
+                    const int cc = c0 + 8 * g;
+                    if (cc < a.c1) tma_load_4d(sa + g * HALO_GROUP_BYTES, &map_a1, &full_bar[s], cc, x0 - 1, y0 - 1, img);
+                    else tma_load_4d(sa + g * HALO_GROUP_BYTES, &map_a2, &full_bar[s], cc - a.c1, x0 - 1, y0 - 1, img);
+                }
                 if (!a.resident)
                     for (int tap = 0; tap < 9; ++tap)
                         tma_load_2d(smem + a.b_off + (size_t)(s * 9 + tap) * a.b_box, &map_b, &full_bar[s],
@@ -487,8 +491,9 @@ __global__ void __launch_bounds__(HALO_THREADS, 1)
                     const uint32_t sb =
                         smem_addr(smem + a.b_off + (size_t)((a.resident ? kg : s) * 9 + tap) * a.b_box);
                     for (int kk = 0; kk < a.bk / 16; ++kk) {
-                        const uint64_t da = smem_desc_sbo(sa + (uint32_t)(dy * HALO_W + dx) * row_bytes + kk * 32,
-                                                          row_bytes, HALO_W * row_bytes);
+                        const uint64_t da = smem_desc_noswz(sa + (uint32_t)(dy * HALO_W + dx) * 16u +
+                                                                (uint32_t)kk * 2u * HALO_GROUP_BYTES,
+                                                            HALO_GROUP_BYTES, HALO_W * 16u);
                         const uint64_t db = smem_desc(sb + kk * 32, row_bytes);
                         const uint32_t accum = (kg > 0 || tap > 0 || kk > 0) ? 1u : 0u;
                         asm volatile(
@@ -589,16 +594,15 @@ bool encode_act(CUtensorMap* m, const bf16* p, int n, int h, int w, int c, int b
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// NHWC activation as a 4-D map with halo boxes of bk channels x 10 x 18 x 1,
-// swizzled like the tile boxes: a box lands as 180 rows of bk channels, row
-// (y * 10 + x), one K-major operand row per halo pixel
-bool encode_act_halo(CUtensorMap* m, const bf16* p, int n, int h, int w, int c, int bk) {
+// NHWC activation as a 4-D map with halo boxes of 8 channels x 10 x 18 x 1,
+// unswizzled: a box lands as [18][10][8 channels], one core-matrix row per pixel
+bool encode_act_halo(CUtensorMap* m, const bf16* p, int n, int h, int w, int c) {
     const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
     const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)c * w * 2, (cuuint64_t)c * w * h * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)bk, (cuuint32_t)HALO_W, (cuuint32_t)HALO_H, 1};
+    const cuuint32_t box[4] = {8, (cuuint32_t)HALO_W, (cuuint32_t)HALO_H, 1};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(p), dims, strides, box, es,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(bk), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -656,7 +660,7 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
     HaloPlan p;
     for (int bk = 64; bk >= 16; bk >>= 1) {
         if (c1 % bk || c2 % bk) continue;
-        const size_t a_stage = round1k((size_t)HALO_PIX * bk * 2);
+        const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t w = (size_t)(cin / bk) * 9 * b_box;
         if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= HALO_SMEM_BUDGET) {
@@ -672,7 +676,7 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
     }
     for (int bk = 64; bk >= 16; bk >>= 1) {
         if (c1 % bk || c2 % bk) continue;
-        const size_t a_stage = round1k((size_t)HALO_PIX * bk * 2);
+        const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t stage = a_stage + 9 * b_box;
         if (2 * stage > HALO_SMEM_BUDGET) continue;
@@ -711,8 +715,8 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (!pl.bk) return cudaErrorInvalidValue;
     CUtensorMap ma1, ma2, mb;
     std::memset(&ma2, 0, sizeof ma2);
-    if (!encode_act_halo(&ma1, a.src1, a.n, a.h, a.w, a.c1, pl.bk)) return cudaErrorInvalidValue;
-    if (a.c2 && !encode_act_halo(&ma2, a.src2, a.n, a.h, a.w, a.c2, pl.bk)) return cudaErrorInvalidValue;
+    if (!encode_act_halo(&ma1, a.src1, a.n, a.h, a.w, a.c1)) return cudaErrorInvalidValue;
+    if (a.c2 && !encode_act_halo(&ma2, a.src2, a.n, a.h, a.w, a.c2)) return cudaErrorInvalidValue;
     if (!a.c2) ma2 = ma1;
     if (!encode_wgt(&mb, a.weight, a.cout, cin, pl.bk, ntile)) return cudaErrorInvalidValue;
     HaloArgs t{};
