@@ -21,7 +21,8 @@
 // Every mbarrier wait is bounded: a wait that runs out sets an error bit in
 // the caller's status word and the CTA still drains and frees its TMEM.
 //
-// k_conv3x3_halo is the default variant.  Its tile is 16 rows x 8 columns of
+// k_conv3x3_halo runs shapes of 64-128 output channels per CTA (the tile
+// kernel above the rest; conv3x3_tc chooses).  Its tile is 16 rows x 8 columns of
 // output pixels (M = 128, one 8-pixel row segment per 8-row core matrix).
 // Per K chunk it loads one 18 x 10 halo of the input (BK/8 TMA boxes of
 // 8 channels x 10 x 18) into the no-swizzle canonical K-major layout
