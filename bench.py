@@ -228,10 +228,10 @@ def serving_benchmark(args):
     served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
                               pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15)
     served_dn_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
-                                 pass_paths=1 << 24, first_pass_spp=128, min_samples=64, overshoot=1.3)
+                                 pass_paths=1 << 24, first_pass_spp=128, min_samples=64, overshoot=1.2)
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
                             "first_pass_spp": {"served": 64, "served_denoised": 128},
-                            "overshoot": {"served": 1.15, "served_denoised": 1.3}}
+                            "overshoot": {"served": 1.15, "served_denoised": 1.2}}
     modes = (("plain", plain_cfg, False), ("served", served_cfg, False), ("served_denoised", served_dn_cfg, True))
     for name, cfg, dn in modes:
         active = cfg.max_active
