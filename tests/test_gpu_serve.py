@@ -134,3 +134,30 @@ def test_stats_kernel_matches_numpy(gpu, denoised):
     N.check(N.lib().vr_serve_stats_device(table, len(shapes), C.c_void_p(out2.data_ptr()), None))
     torch.cuda.synchronize()
     assert np.array_equal(out2.cpu().numpy(), v)   # deterministic
+
+
+def test_backend_estimates_through_the_stats_kernel(gpu):
+    """GpuBackend's per-pass estimate (one vr_serve_stats_device launch) equals
+    the numpy half-buffer formula on the same buffers."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.serve import GpuBackend, JobRequest, JobState, _estimate
+
+    scenes = _scenes(vr, W)
+    be = GpuBackend()
+    jobs = []
+    for k, (w, h) in enumerate([(40, 24), (33, 17)]):
+        acc, st = scenes[k]
+        job = JobState(job_id=k, req=JobRequest(acc, st, w, h, max_samples=64, target_relmse=1e-3, seed=3 + k),
+                       arrival=0.0)
+        job.bufs = be.alloc(job)
+        jobs.append(job)
+    be.render([(j, 0, 0, 8) for j in jobs] + [(j, 1, 8, 6) for j in jobs])
+    for j in jobs:
+        j.n_a, j.n_b, j.samples = 8, 6, 14
+    got = be.estimate_many(jobs)
+    for j, e in zip(jobs, got):
+        a = j.bufs[0][..., :3].double().cpu().numpy() / 8
+        b = j.bufs[1][..., :3].double().cpu().numpy() / 6
+        assert e == pytest.approx(_estimate(a, b, 8, 6), rel=1e-12)
+    be.batch.destroy()

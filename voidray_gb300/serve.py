@@ -470,299 +470,6 @@ class GpuBackend:
         return out
 
     def estimate(self, job: JobState) -> float:
-        a, b = self.means(job)
-        return _estimate(a, b, job.n_a, job.n_b)
-
-    def result(self, job: JobState) -> np.ndarray:
-        a, b = job.bufs
-        return (a + b) / (job.n_a + job.n_b)
-
-    # asynchronous interface (runs synchronously here; the scheduler logic is the same)
-    def render_async(self, work):
-        self.render(work)
-        return None
-
-    def estimate_async(self, jobs, after):
-        return [self.estimate(j) for j in jobs]
-
-    def poll(self, handle, block: bool = False):
-        return handle
-
-
-def _estimate(a, b, na: int, nb: int, xp=np) -> float:
-    n = na + nb
-    m = (a * na + b * nb) / n
-    var = (a - b) ** 2 * (na * nb) / (n * n)
-    return float(xp.mean(var / (m * m + EPS_REL)))
-
-
-BLEND_TILE = 16  # blend weights are chosen per BLEND_TILE x BLEND_TILE pixel tile
-
-
-def _tile_mean(x, tile: int, xp):
-    """Per-tile means over the valid pixels and channels of an (H, W, C) array
-    or tensor -> (ceil(H/tile), ceil(W/tile))."""
-    h, w, c = x.shape
-    th, tw = -(-h // tile), -(-w // tile)
-    ph, pw = th * tile - h, tw * tile - w
-    if xp is np:
-        xs = np.pad(x, ((0, ph), (0, pw), (0, 0)))
-        cnt = np.pad(np.ones((h, w)), ((0, ph), (0, pw)))
-    else:
-        import torch.nn.functional as F
-
-        xs = F.pad(x.permute(2, 0, 1), (0, pw, 0, ph)).permute(1, 2, 0)
-        cnt = F.pad(x.new_ones((1, h, w)), (0, pw, 0, ph))[0]
-    s = xs.reshape(th, tile, tw, tile, c).sum((1, 3, 4))
-    n = cnt.reshape(th, tile, tw, tile).sum((1, 3)) * c
-    return s / n
-
-
-def blend_tile_moments(a, b, p, da, db, tile: int = BLEND_TILE, xp=np):
-    """blend_moments per tile: stacked (5, tiles_y, tiles_x)."""
-    den = p * p + EPS_REL
-    ab = a - b
-    dd = da - db
-    maps = [ab * ab / den, (da - b) ** 2 / den, (db - a) ** 2 / den, dd * dd / den, dd * ab / den]
-    return xp.stack([_tile_mean(m, tile, xp) for m in maps])
-
-
-def tile_blend(mt, na: int, nb: int, k: float = 1.0):
-    """Per-tile best blend at k x (na + nb) samples from blend_tile_moments()
-    values (numpy (5, ty, tx)); returns (plain image error, blend image error,
-    alpha map).  Each tile takes its own optimal weight (alpha = 0 is the
-    plain mean), so the blend is never predicted worse than plain."""
-    s_ab, s_dab, s_dba, s_dd, s_ddab = (np.asarray(x, np.float64) for x in mt)
-    n = na + nb
-    v_p = s_ab * na * nb / (n * n)
-    e_a = s_dab - s_ab * na / n
-    e_b = s_dba - s_ab * nb / n
-    tau2 = s_dd * na * nb / n
-    kap = s_ddab * na * nb / n
-    bias2 = np.maximum(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
-    v_p, v_eta, c = v_p / k, tau2 / n / k, kap / n / k
-    e_d = bias2 + v_eta
-    q = e_d + v_p - 2.0 * c
-    with np.errstate(divide="ignore", invalid="ignore"):
-        alpha = np.where(q > 0, np.clip((v_p - c) / q, 0.0, 1.0), 1.0)
-    blend = np.maximum(alpha * alpha * e_d + (1 - alpha) ** 2 * v_p + 2 * alpha * (1 - alpha) * c, 0.0)
-    return float(v_p.mean()), float(blend.mean()), alpha
-
-
-def tile_samples_needed(mt, na: int, nb: int, target: float) -> int:
-    """Fewest samples at which the per-tile blend's predicted image error reaches `target`."""
-    n = na + nb
-    err = lambda k: tile_blend(mt, na, nb, k)[1]
-    if err(1.0) <= target:
-        return n
-    lo, hi = 1.0, 2.0
-    while err(hi) > target and hi < 1e6:
-        lo, hi = hi, hi * 2.0
-    for _ in range(30):
-        mid = 0.5 * (lo + hi)
-        if err(mid) > target:
-            lo = mid
-        else:
-            hi = mid
-    return int(math.ceil(n * hi))
-
-
-def blend_moments(a, b, p, da, db, xp=np) -> list:
-    """The five pixel means the blend prediction needs (arrays or tensors,
-    not yet converted to floats, so a caller can read many at once)."""
-    den = p * p + EPS_REL
-    ab = a - b
-    dd = da - db
-    return [xp.mean(ab * ab / den), xp.mean((da - b) ** 2 / den), xp.mean((db - a) ** 2 / den),
-            xp.mean(dd * dd / den), xp.mean(dd * ab / den)]
-
-
-def _blend_terms(m, na: int, nb: int):
-    """(v_p, bias2, v_eta, c) at n = na + nb samples from blend_moments() values."""
-    s_ab, s_dab, s_dba, s_dd, s_ddab = (float(x) for x in m)
-    n = na + nb
-    v_p = s_ab * na * nb / (n * n)
-    var_a, var_b = s_ab * nb / n, s_ab * na / n
-    e_a = s_dab - var_b
-    e_b = s_dba - var_a
-    tau2 = s_dd * na * nb / n
-    kap = s_ddab * na * nb / n
-    bias2 = max(0.0, 0.5 * ((e_a - tau2 / na) + (e_b - tau2 / nb)))
-    return v_p, bias2, tau2 / n, kap / n
-
-
-def _best_blend(v_p, bias2, v_eta, c):
-    e_d = bias2 + v_eta
-    q = e_d + v_p - 2.0 * c
-    alpha = min(1.0, max(0.0, (v_p - c) / q)) if q > 0 else 1.0
-    blend = alpha * alpha * e_d + (1.0 - alpha) ** 2 * v_p + 2.0 * alpha * (1.0 - alpha) * c
-    return max(blend, 0.0), alpha
-
-
-def blend_samples_needed(m, na: int, nb: int, target: float) -> int:
-    """Fewest samples n' >= n at which the predicted error of the best of the
-    plain mean and the blend reaches `target`: the noise terms (plain
-    variance, residual denoiser noise, covariance) scale as n / n', the bias
-    stays."""
-    v_p, bias2, v_eta, c = _blend_terms(m, na, nb)
-    n = na + nb
-
-    def err(k):  # k = n' / n
-        b, _ = _best_blend(v_p / k, bias2, v_eta / k, c / k)
-        return min(b, v_p / k)
-
-    if err(1.0) <= target:
-        return n
-    lo, hi = 1.0, 2.0
-    while err(hi) > target and hi < 1e6:
-        lo, hi = hi, hi * 2.0
-    for _ in range(30):
-        mid = 0.5 * (lo + hi)
-        if err(mid) > target:
-            lo = mid
-        else:
-            hi = mid
-    return int(math.ceil(n * hi))
-
-
-def blend_from_moments(m, na: int, nb: int):
-    """(plain, blend, alpha) from blend_moments() values."""
-    # Var(P) from the halves; D(A)'s error is E|D(A)-B|^2 - Var(B); the
-    # residual denoiser noise x samples (tau2) from E|D(A)-D(B)|^2; its
-    # covariance with the plain noise x samples from E[(D(A)-D(B))(A-B)]
-    v_p, bias2, v_eta, c = _blend_terms(m, na, nb)
-    blend, alpha = _best_blend(v_p, bias2, v_eta, c)
-    return v_p, blend, alpha
-
-
-def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
-    """Predicted relMSE of the plain mean P and of the best blend
-    alpha D(P) + (1 - alpha) P, from the half means a, b (na, nb samples),
-    the full mean p and the denoised half means da, db.  Returns
-    (plain, blend, alpha)."""
-    return blend_from_moments(blend_moments(a, b, p, da, db, xp), na, nb)
-
-
-class GpuBackend:
-    """Device accumulation buffers (torch) and one vr_batch for every pass;
-    with a denoiser, jobs that ask for it also get AOV buffers and blended
-    outputs (the module docstring describes the prediction)."""
-
-    def __init__(self, max_wave_paths: int = 0, denoiser=None):
-        import torch
-
-        from .batch import Batch
-
-        self.torch = torch
-        self.batch = Batch(max_wave_paths)
-        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
-        self.stream = torch.cuda.Stream()      # renders
-        self.est_stream = torch.cuda.Stream()  # estimates (pipelined mode)
-        self.res_stream = torch.cuda.Stream()  # final images: never queued behind later estimates
-        self.dn = denoiser
-        # final images run on their own stream, so they get their own handle
-        # (a handle's workspace must not be shared by concurrent streams)
-        self.dn_result = denoiser.clone() if denoiser is not None else None
-        self.denoise_calls = 0
-        self.time = {"render": 0.0, "estimate": 0.0, "result": 0.0}  # host wall seconds per phase
-
-    def alloc(self, job: JobState):
-        t = self.torch
-        h, w = job.req.height, job.req.width
-        k = 6 if (job.req.denoise and self.dn is not None) else 2
-        # [A, B] radiance sums, then albedo A/B and normal A/B sums; zeroed on
-        # the render stream so the first pass is ordered after the fill
-        with t.cuda.stream(self.stream):
-            return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
-
-    def free(self, job: JobState) -> None:
-        job.bufs = None
-
-    # -- rendering -------------------------------------------------------
-    def _enqueue(self, work: list[tuple[JobState, int, int, int]]) -> None:
-        from dataclasses import replace
-
-        from .batch import RenderJob
-
-        jobs = []
-        for job, b, first, n in work:
-            # buffers accumulate raw sums: total_samples = 1
-            st = replace(job.req.settings, total_samples=1)
-            aov = len(job.bufs) == 6
-            jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
-                                  job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
-                                  job.bufs[4 + b].data_ptr() if aov else 0))
-        self.batch.render(jobs, self.stream.cuda_stream)
-
-    def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
-        t0 = time.perf_counter()
-        self._enqueue(work)
-        self.batch.synchronize(self.stream.cuda_stream)
-        self.time["render"] += time.perf_counter() - t0
-
-    def render_async(self, work):
-        """Enqueues the pass; returns an event recorded after it on the render stream."""
-        t0 = time.perf_counter()
-        self._enqueue(work)
-        ev = self.torch.cuda.Event()
-        ev.record(self.stream)
-        self.time["render"] += time.perf_counter() - t0
-        return ev
-
-    # -- error estimates -------------------------------------------------
-    def _stats(self, jobs: list[JobState], stream):
-        """Enqueues on `stream`: every job's plain estimate and, for denoising
-        jobs, the denoiser over both half-buffers (one batch per image size)
-        and the per-tile blend moments.  Returns (one flat device tensor,
-        layout of the denoising jobs' tile moments)."""
-        t = self.torch
-        with t.cuda.stream(stream):
-            plain, halves = [], []
-            for job in jobs:
-                na, nb = job.n_a, job.n_b
-                a = job.bufs[0][..., :3].double() / na
-                b = job.bufs[1][..., :3].double() / nb
-                n = na + nb
-                m = (a * na + b * nb) / n
-                plain.append(t.mean((a - b) ** 2 * (na * nb / (n * n)) / (m * m + EPS_REL)))
-                halves.append((job, a, b, m))
-            parts, layout, off = [t.stack(plain)], [], len(jobs)
-            groups = {}
-            for item in halves:
-                if len(item[0].bufs) == 6:
-                    groups.setdefault((item[0].req.height, item[0].req.width), []).append(item)
-            for (h, w), items in groups.items():
-                rad = t.stack([x for j, *_ in items for x in (j.bufs[0], j.bufs[1])])
-                alb = t.stack([x for j, *_ in items for x in (j.bufs[2], j.bufs[3])])
-                nrm = t.stack([x for j, *_ in items for x in (j.bufs[4], j.bufs[5])])
-                scales = [s for j, *_ in items for s in (1.0 / j.n_a, 1.0 / j.n_b)]
-                den = t.empty_like(rad)
-                self.dn.denoise_batch(rad, alb, nrm, scales, den, w, h, stream=stream.cuda_stream)
-                self.denoise_calls += 1
-                for k, (job, a, b, m) in enumerate(items):
-                    mt = blend_tile_moments(a, b, m, den[2 * k][..., :3].double(), den[2 * k + 1][..., :3].double(),
-                                            BLEND_TILE, t)
-                    parts.append(mt.reshape(-1))
-                    layout.append((job, off, mt.shape[1], mt.shape[2]))
-                    off += mt.numel()
-            return t.cat(parts), layout
-
-    def _apply(self, jobs: list[JobState], v: np.ndarray, layout) -> list[float]:
-        out = [float(x) for x in v[:len(jobs)]]
-        for job, e in zip(jobs, out):
-            job.plain_estimate, job.alpha, job.need_spp = e, 0.0, 0
-        pos = {id(j): i for i, j in enumerate(jobs)}
-        for job, off, ty, tx in layout:
-            mt = v[off:off + 5 * ty * tx].reshape(5, ty, tx)
-            _, blend, alpha = tile_blend(mt, job.n_a, job.n_b)
-            job.need_spp = tile_samples_needed(mt, job.n_a, job.n_b, job.req.target_relmse)
-            i = pos[id(job)]
-            if blend < out[i]:
-                job.alpha = alpha
-                out[i] = blend
-        return out
-
-    def estimate(self, job: JobState) -> float:
         return self.estimate_many([job])[0]
 
     def estimate_many(self, jobs: list[JobState]) -> list[float]:
