@@ -49,8 +49,9 @@ def test_served_same_alone_and_in_mix(gpu):
     assert r0[1] < 256  # stopped on the error estimate
 
 
-@pytest.mark.parametrize("adaptive,pipelined", [(False, False), (True, False), (True, True)])
-def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
+@pytest.mark.parametrize("adaptive,pipelined,streams", [(False, False, 1), (True, False, 1), (True, True, 1),
+                                                       (True, True, 2)])
+def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined, streams):
     """With the denoiser in the loop (AOV buffers, blended output) a job's
     stopping point, blend weight and image still depend only on the job."""
     import voidray_gb300 as vr
@@ -64,7 +65,7 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
     net = Denoiser.pretrained()
 
     def run(mix):
-        backend = GpuBackend(denoiser=net)
+        backend = GpuBackend(denoiser=net, render_streams=streams)
         srv = Server(backend, cfg)
         acc, st = scenes[1]
         jid = srv.submit(JobRequest(acc, st, 40, 32, max_samples=128, target_relmse=2e-2, seed=5, denoise=True))
@@ -77,6 +78,7 @@ def test_denoised_serving_same_alone_and_in_mix(gpu, adaptive, pipelined):
         backend.finish()
         j = srv.status(jid)
         assert backend.denoise_calls > 0
+        backend.destroy()
         return j.result, j.samples, np.asarray(j.alpha).tolist(), j.estimate
 
     try:
@@ -160,4 +162,4 @@ def test_backend_estimates_through_the_stats_kernel(gpu):
         a = j.bufs[0][..., :3].double().cpu().numpy() / 8
         b = j.bufs[1][..., :3].double().cpu().numpy() / 6
         assert e == pytest.approx(_estimate(a, b, 8, 6), rel=1e-12)
-    be.batch.destroy()
+    be.destroy()

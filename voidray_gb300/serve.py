@@ -340,19 +340,28 @@ def blend_prediction(a, b, p, da, db, na: int, nb: int, xp=np):
 
 
 class GpuBackend:
-    """Device accumulation buffers (torch) and one vr_batch for every pass;
-    with a denoiser, jobs that ask for it also get AOV buffers and blended
-    outputs (the module docstring describes the prediction)."""
+    """Device accumulation buffers (torch) and vr_batch objects that render
+    the passes; with a denoiser, jobs that ask for it also get AOV buffers and
+    blended outputs (the module docstring describes the prediction).
 
-    def __init__(self, max_wave_paths: int = 0, denoiser=None):
+    With render_streams = 2, pipelined passes alternate between two batches
+    (each with its own path-state scratch and graph cache) on two streams, so
+    the deep bounces of one pass, which keep few rays alive, overlap the first
+    bounces of the next.  A job is in at most one pass at a time, so this
+    changes no job's samples."""
+
+    def __init__(self, max_wave_paths: int = 0, denoiser=None, render_streams: int = 1):
         import torch
 
         from .batch import Batch
 
         self.torch = torch
-        self.batch = Batch(max_wave_paths)
-        self.batch.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
-        self.stream = torch.cuda.Stream()      # renders
+        self.batches = [Batch(max_wave_paths) for _ in range(max(1, int(render_streams)))]
+        for b in self.batches:
+            b.set_graphs(True)   # passes of an unchanged job set replay one CUDA graph
+        self.streams = [torch.cuda.Stream() for _ in self.batches]  # renders
+        self.batch, self.stream = self.batches[0], self.streams[0]
+        self._next = 0                         # batch / stream of the next asynchronous pass
         self.est_stream = torch.cuda.Stream()  # estimates (pipelined mode)
         self.res_stream = torch.cuda.Stream()  # final images: never queued behind later estimates
         self.dn = denoiser
@@ -366,29 +375,38 @@ class GpuBackend:
         t = self.torch
         h, w = job.req.height, job.req.width
         k = 6 if (job.req.denoise and self.dn is not None) else 2
-        # [A, B] radiance sums, then albedo A/B and normal A/B sums; zeroed on
-        # the render stream so the first pass is ordered after the fill
+        # [A, B] radiance sums, then albedo A/B and normal A/B sums, zeroed on
+        # the first render stream; a pass on another stream waits for the fill
         with t.cuda.stream(self.stream):
-            return [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
+            bufs = [t.zeros((h, w, 4), dtype=t.float32, device="cuda") for _ in range(k)]
+            job.ready = t.cuda.Event()
+            job.ready.record(self.stream)
+        return bufs
 
     def free(self, job: JobState) -> None:
         job.bufs = None
 
     # -- rendering -------------------------------------------------------
-    def _enqueue(self, work: list[tuple[JobState, int, int, int]]) -> None:
+    def _enqueue(self, work: list[tuple[JobState, int, int, int]], k: int = 0) -> None:
         from dataclasses import replace
 
         from .batch import RenderJob
 
+        stream = self.streams[k]
         jobs = []
         for job, b, first, n in work:
+            ready = getattr(job, "ready", None)
+            if ready is not None:
+                if k != 0:
+                    stream.wait_event(ready)
+                job.ready = None
             # buffers accumulate raw sums: total_samples = 1
             st = replace(job.req.settings, total_samples=1)
             aov = len(job.bufs) == 6
             jobs.append(RenderJob(job.req.scene, st, n, job.bufs[b].data_ptr(), job.req.width, job.req.height,
                                   job.req.seed, first, job.bufs[2 + b].data_ptr() if aov else 0,
                                   job.bufs[4 + b].data_ptr() if aov else 0))
-        self.batch.render(jobs, self.stream.cuda_stream)
+        self.batches[k].render(jobs, stream.cuda_stream)
 
     def render(self, work: list[tuple[JobState, int, int, int]]) -> None:
         t0 = time.perf_counter()
@@ -397,11 +415,14 @@ class GpuBackend:
         self.time["render"] += time.perf_counter() - t0
 
     def render_async(self, work):
-        """Enqueues the pass; returns an event recorded after it on the render stream."""
+        """Enqueues the pass on the next render stream; returns an event
+        recorded after it."""
         t0 = time.perf_counter()
-        self._enqueue(work)
+        k = self._next
+        self._next = (k + 1) % len(self.batches)
+        self._enqueue(work, k)
         ev = self.torch.cuda.Event()
-        ev.record(self.stream)
+        ev.record(self.streams[k])
         self.time["render"] += time.perf_counter() - t0
         return ev
 
@@ -512,7 +533,12 @@ class GpuBackend:
         """Waits for all streams and reports kernel-side errors of the passes."""
         self.est_stream.synchronize()
         self.res_stream.synchronize()
-        self.batch.synchronize(self.stream.cuda_stream)
+        for b, st in zip(self.batches, self.streams):
+            b.synchronize(st.cuda_stream)
+
+    def destroy(self) -> None:
+        for b in self.batches:
+            b.destroy()
 
     # -- results ---------------------------------------------------------
     def result(self, job: JobState) -> np.ndarray:
