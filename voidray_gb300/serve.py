@@ -497,7 +497,8 @@ class GpuBackend:
         """Estimates of all jobs of a pass, read back in one transfer."""
         t0 = time.perf_counter()
         flat, layout = self._stats(jobs, self.stream)
-        v = flat.cpu().numpy()
+        with self.torch.cuda.stream(self.stream):
+            v = flat.cpu().numpy()  # copied on the stream that computed it (then waited for)
         out = self._apply(jobs, v, layout)
         self.time["estimate"] += time.perf_counter() - t0
         return out
