@@ -227,10 +227,12 @@ def serving_benchmark(args):
     # the denoised path starts with a larger first pass: its blend estimate
     # needs a less noisy input, and its per-job sample counts are smaller
     served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
-                              pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15)
+                              pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15, max_inflight=3)
     served_dn_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
-                                 pass_paths=1 << 24, first_pass_spp=128, min_samples=64, overshoot=1.2)
+                                 pass_paths=1 << 24, first_pass_spp=128, min_samples=64, overshoot=1.2,
+                                 max_inflight=3)
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
+                            "max_inflight": 3, "render_streams": args.serve_streams,
                             "first_pass_spp": {"served": 64, "served_denoised": 128},
                             "overshoot": {"served": 1.15, "served_denoised": 1.2}}
     modes = (("plain", plain_cfg, False), ("served", served_cfg, False), ("served_denoised", served_dn_cfg, True))
