@@ -479,6 +479,13 @@ vr_status vr_intersect_device(vr_scene* scene, const vr_ray* rays_device,
                               uint64_t count, vr_hit* hits_device,
                               int32_t any_hit, void* stream);
 
+/* Environment::sample (voidray_renderer/src/core/traits.rs:66-69) of the
+ * scene's environment for `count` directions (3 f32 each, host memory; need
+ * not be normalised): RGB f32 into rgb (3 per direction).  The same lookup
+ * the integrator applies to escaping rays (HDRI: bilinear with the
+ * reference's linear-index wrap and pole saturation). */
+vr_status vr_environment_sample(vr_scene* scene, const float* directions, uint64_t count, float* rgb);
+
 /* Traversal work counters for the same rays and kernels (inner-node visits,
  * triangle tests), used to state the algorithmic bytes of a launch. */
 vr_status vr_intersect_count_device(vr_scene* scene, const vr_ray* rays_device,

@@ -117,3 +117,31 @@ def test_graph_replays_equal_direct_launches(gpu, max_wave):
         batch.destroy()
     for a, b in zip(results[False], results[True]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("max_wave", [0, 20000])
+def test_mixed_job_set_equals_alone(gpu, max_wave):
+    """A many-scene mix (16 scenes of 10k-200k triangles, four image shapes,
+    2-32 spp, depth 8-12, both estimators, clamp on and off) in one batch:
+    every job's image is bit-identical to rendering it alone."""
+    import torch
+
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.batch import Batch, RenderJob
+
+    mix = W.mixed_job_set(16, seed=4)
+    accs = [s.build_acceleration() for s, *_ in mix]
+    alone = [_alone(vr, acc, st, spp, w, h, seed, 0) for acc, (s, st, spp, w, h, seed) in zip(accs, mix)]
+    batch = Batch(max_wave)
+    outs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, _, _, w, h, _ in mix]
+    stream = torch.cuda.Stream()
+    batch.render([RenderJob(acc, st, spp, o.data_ptr(), w, h, seed, 0)
+                  for acc, (s, st, spp, w, h, seed), o in zip(accs, mix, outs)], stream.cuda_stream)
+    batch.synchronize(stream.cuda_stream)
+    for k, (a, o) in enumerate(zip(alone, outs)):
+        assert np.array_equal(o.cpu().numpy(), a), k
+    assert batch.stats().paths == sum(spp * w * h for _, _, spp, w, h, _ in mix)
+    batch.destroy()
+    for acc in accs:
+        acc.destroy()

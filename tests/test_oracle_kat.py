@@ -150,3 +150,72 @@ def test_cornell_energy_sanity(oracle):
     assert rays[0] > 32 * 32 * 4
     assert np.all(img[..., 3] == 1.0)
     assert 0.01 < img[..., :3].mean() < 3.0
+
+
+# HDRIEnvironment::sample (voidray_common/src/environments.rs:57-90) with
+# to_spherical_coords (voidray_renderer/src/util/math.rs:24-29) and lerp
+# (math.rs:41-46), restated in numpy float32 in the reference's operation
+# order; transcendental calls rounded from float64.
+def _env_lookup_f32(img, d):
+    f = np.float32
+    h, w = img.shape[:2]
+    flat = img.reshape(-1, 3)
+    n_pix = len(flat)
+    d = np.asarray(d, f)
+    m2 = f(f(d[0] * d[0]) + f(d[1] * d[1])) + f(d[2] * d[2])
+    inv = f(1.0) / f(np.sqrt(m2))
+    n = d * inv
+    sx = f(np.arccos(np.float64(-n[1])))
+    sy = f(f(np.arctan2(np.float64(-n[2]), np.float64(n[0]))) + f(np.pi))
+    u = sx / f(np.pi)
+    v = sy / f(f(2.0) * f(np.pi))
+    x = v * f(w)
+    y = f(h - 1) - u * f(h)
+
+    def usize(t):  # Rust `as usize`: NaN and negatives saturate to 0
+        return 0 if not t > 0 else int(t)
+
+    x0 = min(usize(x), w - 1)
+    y0 = min(usize(y), h - 1)
+    ax = x - f(x0)
+    ay = y - f(y0)
+
+    def lerp(a, b, t):
+        return a * (f(1.0) - t) + b * t
+
+    px = lambda i: flat[i % n_pix]
+    top = lerp(px(y0 * w + x0), px(y0 * w + x0 + 1), ax)
+    bot = lerp(px((y0 + 1) * w + x0), px((y0 + 1) * w + x0 + 1), ax)
+    return lerp(top, bot, ay), (x0, y0, float(ax), float(ay))
+
+
+ENV_DIRS = [
+    (0.0, -1.0, 0.0),     # bottom pole: y0 = H-1, the next row wraps to row 0 (weight 0)
+    (0.0, 1.0, 0.0),      # top pole: y = -1 saturates to row 0, ay = -1 extrapolates
+    (-1.0, 0.0, 0.0),     # seam with -0.0 = -d.z: atan2(-0, -1) = -pi, x = 0
+    (-1.0, 0.0, -0.0),    # seam with +0.0: atan2(+0, -1) = +pi, x = W, x0 = W-1, ax = 1
+    (-1.0, 0.0, 1e-7), (-1.0, 0.0, -1e-7), (1.0, 0.0, 0.0), (0.0, 0.0, 1.0), (0.0, 0.0, -1.0),
+    (1e-6, -1.0, 0.0), (1e-6, 1.0, -1e-6), (0.3, -0.9, 0.2), (-0.5, 0.5, -0.5),
+]
+
+
+def test_hdri_lookup_at_poles_and_seams(oracle):
+    """The oracle's environment lookup against the float32 restatement, on
+    the directions where the reference's quirks show (poles, the phi seam
+    with either zero sign) and a few ordinary ones."""
+    from voidray_gb300 import Camera, Environments, Scene
+
+    rng = np.random.default_rng(8)
+    img = rng.uniform(0.0, 4.0, (9, 16, 3)).astype(np.float32)
+    s = Scene()
+    s.environment = Environments.hdri_image(img)
+    s.camera = Camera.look_at((0, 0, 1), (0, 0, 0), (0, 1, 0), 1.0)
+    o = oracle.OracleScene(s)
+    seen = set()
+    for d in ENV_DIRS:
+        want, (x0, y0, ax, ay) = _env_lookup_f32(img, d)
+        got = o.env_eval(np.array(d, np.float32))
+        assert np.allclose(got, want, rtol=1e-5, atol=1e-6), (d, got, want, x0, y0, ax, ay)
+        seen.add((x0, y0, ax, ay))
+    # the quirks are exercised: top-pole extrapolation and the x0 = W-1, ax = 1 seam
+    assert any(ay < 0 for *_, ay in seen) and any(x0 == 15 and ax == 1.0 for x0, _, ax, _ in seen)

@@ -154,6 +154,7 @@ _SIGS = [
     ("vr_intersect", C.c_int, [P, P, C.c_uint64, P, C.c_int32]),
     ("vr_intersect_device", C.c_int, [P, P, C.c_uint64, P, C.c_int32, P]),
     ("vr_intersect_count_device", C.c_int, [P, P, C.c_uint64, C.c_int32, P, P, P]),
+    ("vr_environment_sample", C.c_int, [P, P, C.c_uint64, P]),
     ("vr_last_error", C.c_char_p, []),
     ("vr_abi_version", C.c_int32, []),
     ("vr_device_available", C.c_int32, []),

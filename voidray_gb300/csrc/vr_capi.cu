@@ -949,6 +949,22 @@ vr_status vr_intersect(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hit* hits
     return check_status(s);
 }
 
+vr_status vr_environment_sample(vr_scene* s, const float* dirs, uint64_t n, float* rgb) {
+    if (!s) return fail(VR_ERR_INVALID, "null scene");
+    if (n == 0) return VR_OK;
+    if (!dirs || !rgb) return fail(VR_ERR_INVALID, "null directions/rgb");
+    vr_status r;
+    const size_t bytes = n * 3 * sizeof(float);
+    if ((r = ensure_buf(s->stage_a, bytes)) != VR_OK) return r;
+    if ((r = ensure_buf(s->stage_b, bytes)) != VR_OK) return r;
+    VR_CK(cudaMemcpyAsync(s->stage_a.p, dirs, bytes, cudaMemcpyHostToDevice, s->stream));
+    VR_CK(vr::launch_env_sample(s->view, static_cast<const float*>(s->stage_a.p), n, static_cast<float*>(s->stage_b.p),
+                                s->stream));
+    VR_CK(cudaMemcpyAsync(rgb, s->stage_b.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    VR_CK(cudaStreamSynchronize(s->stream));
+    return check_status(s);
+}
+
 vr_status vr_intersect_count_device(vr_scene* s, const vr_ray* rays, uint64_t n, int32_t any_hit,
                                     uint64_t* node_visits, uint64_t* tri_tests, void* stream) {
     if (!s || !node_visits || !tri_tests) return fail(VR_ERR_INVALID, "null argument");

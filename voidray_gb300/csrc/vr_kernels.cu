@@ -1143,6 +1143,22 @@ cudaError_t launch_tonemap(const float4* in, float4* out, uint32_t np, int32_t t
     return cudaGetLastError();
 }
 
+// Environment::sample (core/traits.rs:66-69) for a batch of directions
+__global__ void k_env_sample(SceneView s, const float* __restrict__ dirs, uint64_t n, float* __restrict__ rgb) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const V3 c = env_eval(s, v3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
+}
+
+cudaError_t launch_env_sample(const SceneView& s, const float* dirs, uint64_t n, float* rgb, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_env_sample<<<grid_for((uint32_t)(n < (1u << 30) ? n : (1u << 30)), 256, 4), 256, 0, st>>>(s, dirs, n, rgb);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_relmse(const float4* a, float sa, const float4* r, float sr, uint32_t np, double* out,
                           cudaStream_t st) {
     k_relmse<<<grid_for(np, 256, 4), 256, 0, st>>>(a, sa, r, sr, np, out);

@@ -602,6 +602,13 @@ class SceneAcceleration:
         check(lib().vr_intersect(self.handle, ptr(rays), len(rays), ptr(hits), int(any_hit)))
         return hits
 
+    def environment_sample(self, directions: np.ndarray) -> np.ndarray:
+        """Environment::sample (traits.rs:66-69) for (n, 3) directions -> (n, 3) RGB."""
+        d = np.ascontiguousarray(directions, dtype=np.float32).reshape(-1, 3)
+        out = np.empty_like(d)
+        check(lib().vr_environment_sample(self.handle, ptr(d), len(d), ptr(out)))
+        return out
+
     def stats(self) -> N.vr_render_stats:
         st = N.vr_render_stats()
         check(lib().vr_render_stats_get(self.handle, C.byref(st)))

@@ -381,3 +381,29 @@ def mix_scene(hdri: bool = False, seed: int = 5):
     st = RenderSettings(total_samples=16, max_bounces=8, rr_depth=0, estimator=Estimator.REFERENCE,
                         firefly_clamp=float("inf"))
     return s, st
+
+
+def mixed_job_set(count: int = 16, seed: int = 4, tri_range=(10_000, 200_000), scale: int = 10,
+                  spp_range=(2, 32), depth_range=(8, 12)):
+    """A many-scene job mix: `count` displaced-icosphere scenes with triangle
+    counts log-uniform in `tri_range`, image sizes drawn from {256^2, 512^2,
+    1280x720, 1920x1080} divided by `scale`, spp log-uniform in `spp_range`,
+    depth uniform in `depth_range`, NEE or the reference estimator; every
+    draw is seeded.  Returns [(scene, settings, spp, width, height, seed)]."""
+    rng = np.random.default_rng(seed)
+    sizes = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+    out = []
+    lo, hi = np.log(tri_range[0]), np.log(tri_range[1])
+    for k in range(count):
+        tris = float(np.exp(rng.uniform(lo, hi)))
+        freq = max(2, int(round(math.sqrt(tris / 20.0))))
+        s, st = displaced_icosphere_scene(freq=freq, seed=100 + k, patch=256, hdri_size=(64, 32))
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        w, h = max(8, w // scale), max(8, h // scale)
+        spp = int(round(np.exp(rng.uniform(np.log(spp_range[0]), np.log(spp_range[1])))))
+        st.max_bounces = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        st.total_samples = spp
+        st.estimator = Estimator.NEE if rng.random() < 0.5 else Estimator.REFERENCE
+        st.firefly_clamp = float(rng.choice([3.0, float("inf")]))
+        out.append((s, st, spp, w, h, int(rng.integers(0, 1 << 30))))
+    return out
