@@ -411,6 +411,9 @@ typedef struct vr_instrument {
     uint64_t shadow_tri_tests;
     uint64_t retired_paths;  /* VR_INSTR_WORK: paths that ended (queue conservation:
                                 equals the camera paths traced) */
+    uint64_t metal_fallbacks;/* VR_INSTR_WORK: Metal::scatter's rejection loop (a
+                                direction above the surface, simple.rs:140-161)
+                                ran out of its 64 tries and the path was absorbed */
 } vr_instrument;
 vr_status vr_scene_instrument(vr_scene* scene, uint32_t flags);
 vr_status vr_scene_instrument_get(vr_scene* scene, vr_instrument* out);

@@ -33,3 +33,37 @@ def test_every_path_retired_once(gpu, estimator, rr, wave):
     assert paths == w * h * spp
     assert ins.retired_paths == paths
     assert np.all(np.isfinite(t.buffer))
+
+
+def test_metal_fallbacks_are_counted(gpu):
+    """Metal::scatter resamples until the direction is above the surface
+    (simple.rs:140-161).  On a Surfaces::quad, whose vertex normals are zero
+    (the kept quirk), that never happens: the reference would loop forever,
+    the GPU absorbs the path after 64 tries and counts it.  With real normals
+    the loop always ends early and nothing is counted."""
+    def run(zero_normals):
+        s = vr.Scene()
+        m = s.add_material(vr.Materials.metal((0.9, 0.9, 0.9), 0.3))
+        q = [(-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0)]
+        if zero_normals:
+            mesh = vr.Surfaces.quad(*q)
+        else:
+            mesh = vr.Mesh(np.array(q, np.float32), [0, 1, 2, 2, 0, 3], np.array([(0, 0, 1)] * 4, np.float32))
+        s.add_object(m, s.add_mesh(mesh))
+        s.environment = vr.Environments.uniform((0.5, 0.6, 0.7))
+        s.camera = vr.Camera.look_at((0, 0, 3), (0, 0, -1), (0, 1, 0), vr.degrees_to_radians(30.0))
+        acc = s.build_acceleration()
+        N.check(vr.lib().vr_scene_instrument(acc.handle, N.INSTR_WORK))
+        st = RenderSettings(total_samples=2, max_bounces=4, firefly_clamp=float("inf"))
+        t = vr.CpuRenderTarget(16, 16)
+        vr.iterative_render(t, acc, st, 2, seed=1)
+        ins = N.vr_instrument()
+        N.check(vr.lib().vr_scene_instrument_get(acc.handle, C.byref(ins)))
+        return ins.metal_fallbacks, ins.retired_paths, t.buffer
+
+    n0, paths0, img0 = run(True)
+    n1, paths1, img1 = run(False)
+    assert paths0 == paths1 == 16 * 16 * 2
+    assert n0 == paths0           # every camera path hits the quad (fov 30, quad fills the view)
+    assert np.all(img0[..., :3] == 0.0)
+    assert n1 == 0 and img1[..., :3].mean() > 0.1

@@ -124,7 +124,8 @@ class vr_tuning(C.Structure):
 class vr_instrument(C.Structure):
     _fields_ = [("stage_ms", C.c_double * 8), ("stage_launches", C.c_uint64 * 8),
                 ("extend_node_visits", C.c_uint64), ("extend_tri_tests", C.c_uint64),
-                ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64), ("retired_paths", C.c_uint64)]
+                ("shadow_node_visits", C.c_uint64), ("shadow_tri_tests", C.c_uint64), ("retired_paths", C.c_uint64),
+                ("metal_fallbacks", C.c_uint64)]
 
 
 STAGES = ["raygen", "extend", "shade", "shadow", "accumulate"]

@@ -144,7 +144,8 @@ struct Instr {
     size_t used = 0;
     double stage_ms[8] = {0};
     uint64_t stage_launches[8] = {0};
-    unsigned long long* work = nullptr;  // device: extend visits, tests, shadow visits, tests
+    unsigned long long* work = nullptr;  // device: extend visits, tests, shadow visits, tests, retired paths,
+                                         // metal fallbacks
 
     vr_status mark(int stage, cudaStream_t cs) {
         if (!(flags & VR_INSTR_STAGE_TIMES)) return VR_OK;
@@ -585,8 +586,8 @@ vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
 vr_status vr_scene_instrument(vr_scene* s, uint32_t flags) {
     if (!s) return fail(VR_ERR_INVALID, "null scene");
     VR_CK(cudaStreamSynchronize(s->stream));
-    if (!s->instr.work) VR_CK(cudaMalloc(&s->instr.work, 5 * sizeof(unsigned long long)));
-    VR_CK(cudaMemset(s->instr.work, 0, 5 * sizeof(unsigned long long)));
+    if (!s->instr.work) VR_CK(cudaMalloc(&s->instr.work, 6 * sizeof(unsigned long long)));
+    VR_CK(cudaMemset(s->instr.work, 0, 6 * sizeof(unsigned long long)));
     s->instr.flags = flags;
     s->instr.used = 0;
     for (int i = 0; i < 8; ++i) {
@@ -607,13 +608,14 @@ vr_status vr_scene_instrument_get(vr_scene* s, vr_instrument* out) {
         out->stage_launches[i] = s->instr.stage_launches[i];
     }
     if (s->instr.work) {
-        unsigned long long w[5];
+        unsigned long long w[6];
         VR_CK(cudaMemcpy(w, s->instr.work, sizeof w, cudaMemcpyDeviceToHost));
         out->extend_node_visits = w[0];
         out->extend_tri_tests = w[1];
         out->shadow_node_visits = w[2];
         out->shadow_tri_tests = w[3];
         out->retired_paths = w[4];
+        out->metal_fallbacks = w[5];
     }
     return VR_OK;
 }

@@ -718,6 +718,8 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
                     }
                     V3 att, nd;
                     if (!scatter(m, ro, rd, hit, rng, &att, &nd)) {
+                        // instrumented runs count the metal paths absorbed by the bounded rejection loop
+                        if (retired && m.kind == M_METAL) atomicAdd(retired + 1, 1ull);
                         if (nee_mode) rad_add(ps, p, clampc(vmul(T, att), fc));
                         else unwind(ps, p, k, clampc(att, fc), fc);
                     } else {

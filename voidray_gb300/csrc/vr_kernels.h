@@ -90,7 +90,8 @@ cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint6
 cudaError_t launch_raygen(const Wave& w, const PathState& ps, cudaStream_t st);
 cudaError_t launch_extend(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
                           cudaStream_t st);
-// `retired` (optional) counts the paths that end at this depth
+// `retired` (optional) counts the paths that end at this depth; retired[1]
+// the Metal scatters whose bounded rejection loop ran out
 cudaError_t launch_shade(const Wave& w, const PathState& ps, uint32_t k, unsigned long long* retired,
                          cudaStream_t st);
 cudaError_t launch_shadow(const Wave& w, const PathState& ps, uint32_t k, uint32_t* status, unsigned long long* work,
