@@ -121,16 +121,18 @@ def test_graph_replays_equal_direct_launches(gpu, max_wave):
 
 @pytest.mark.parametrize("max_wave", [0, 20000])
 def test_mixed_job_set_equals_alone(gpu, max_wave):
-    """A many-scene mix (16 scenes of 10k-200k triangles, four image shapes,
-    2-32 spp, depth 8-12, both estimators, clamp on and off) in one batch:
-    every job's image is bit-identical to rendering it alone."""
+    """The batched configuration at test size: 64 scenes of 10k-200k
+    triangles, four image shapes (the 256^2 .. 1920x1080 set divided by 10),
+    2-32 spp, depth 8-12, both estimators, clamp on and off, in one batch
+    (one wave, or split into 20k-path waves): every job's image is
+    bit-identical to rendering it alone."""
     import torch
 
     import voidray_gb300 as vr
     from voidray_gb300 import workloads as W
     from voidray_gb300.batch import Batch, RenderJob
 
-    mix = W.mixed_job_set(16, seed=4)
+    mix = W.mixed_job_set(64, seed=4)
     accs = [s.build_acceleration() for s, *_ in mix]
     alone = [_alone(vr, acc, st, spp, w, h, seed, 0) for acc, (s, st, spp, w, h, seed) in zip(accs, mix)]
     batch = Batch(max_wave)
