@@ -163,3 +163,52 @@ def test_backend_estimates_through_the_stats_kernel(gpu):
         b = j.bufs[1][..., :3].double().cpu().numpy() / 6
         assert e == pytest.approx(_estimate(a, b, 8, 6), rel=1e-12)
     be.destroy()
+
+
+def test_gpu_checkpoint_resume_is_bit_identical(gpu, tmp_path):
+    """A denoised job checkpointed to disk after its first pass and resumed on
+    a new server and backend (two render streams, other jobs in the mix)
+    ends with the same samples, blend weights and image as without the
+    interruption."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.denoise import Denoiser
+    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig
+
+    scenes = _scenes(vr, W)
+    cfg = ServerConfig(min_samples=16, adaptive=True, pass_paths=40 * 32 * 64, first_pass_spp=16)
+    net = Denoiser.pretrained()
+    acc, st = scenes[1]
+    req = lambda: JobRequest(acc, st, 40, 32, max_samples=256, target_relmse=5e-3, seed=21, denoise=True)
+    try:
+        be = GpuBackend(denoiser=net)
+        s = Server(be, cfg)
+        jid = s.submit(req())
+        while not s.idle():
+            s.step()
+        ref = s.status(jid)
+        ref = (ref.result, ref.samples, np.asarray(ref.alpha).tolist(), ref.passes)
+        be.destroy()
+        assert ref[3] >= 2
+
+        be = GpuBackend(denoiser=net)
+        s = Server(be, cfg)
+        jid = s.submit(req())
+        s.step()
+        path = str(tmp_path / "job.npz")
+        s.checkpoint(jid, path)
+        be.destroy()
+
+        be = GpuBackend(denoiser=net, render_streams=2)
+        s = Server(be, cfg)
+        a2, s2 = scenes[0]
+        s.submit(JobRequest(a2, s2, 24, 16, max_samples=64, target_relmse=1e-4, seed=77))
+        rid = s.submit(req(), resume=path)
+        while not s.idle():
+            s.step()
+        j = s.status(rid)
+        assert (j.samples, np.asarray(j.alpha).tolist(), j.passes) == ref[1:]
+        assert np.array_equal(j.result, ref[0])
+        be.destroy()
+    finally:
+        net.destroy()

@@ -360,3 +360,51 @@ def test_tile_blend_beats_global_blend_where_regions_differ():
         assert alpha_map[:, :4].mean() > alpha_map[:, 4:].mean() + 0.2  # smooth half leans on the denoiser
     assert np.mean(true_t) < 0.9 * np.mean(true_g)
     assert 0.9 * np.mean(true_t) <= np.mean(pred) <= 1.8 * np.mean(true_t)
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_checkpoint_resume_finishes_like_uninterrupted(tmp_path, adaptive):
+    """A job checkpointed after a few passes and resumed on a new server (with
+    other jobs in the mix) renders exactly the passes it had left: the same
+    sample count, estimate and image as without the interruption."""
+    cfg = ServerConfig(spp_per_pass=8, min_samples=16, adaptive=adaptive, first_pass_spp=16, pass_paths=8 * 8 * 64)
+    target = 2e-3
+
+    def full():
+        s = Server(FakeBackend(), cfg, clock=Clock())
+        jid = s.submit(req(seed=3, target=target, max_samples=512))
+        while not s.idle():
+            s.step()
+        j = s.status(jid)
+        return j.result, j.samples, j.estimate, j.passes
+
+    ref = full()
+    assert ref[3] >= 2   # at least two passes, so a checkpoint before the last one leaves work to do
+
+    s = Server(FakeBackend(), cfg, clock=Clock())
+    jid = s.submit(req(seed=3, target=target, max_samples=512))
+    for _ in range(ref[3] - 1):
+        s.step()
+    assert s.status(jid).state == "active"
+    path = str(tmp_path / "job.npz")
+    s.checkpoint(jid, path)
+    s2 = Server(FakeBackend(), cfg, clock=Clock())
+    others = [s2.submit(req(seed=50 + k, target=5e-4, max_samples=128)) for k in range(2)]
+    rid = s2.submit(req(seed=3, target=target, max_samples=512), resume=path)
+    while not s2.idle():
+        s2.step()
+    j = s2.status(rid)
+    assert (j.samples, j.estimate, j.passes) == ref[1:]
+    assert np.array_equal(j.result, ref[0])
+    assert all(s2.status(o).state == "done" for o in others)
+
+
+def test_checkpoint_rejects_mismatch_and_in_flight(tmp_path):
+    s = Server(FakeBackend(), ServerConfig(spp_per_pass=8, min_samples=16), clock=Clock())
+    jid = s.submit(req(seed=3, max_samples=256))
+    with pytest.raises(ValueError):
+        s.checkpoint(jid, str(tmp_path / "w.npz"))   # still waiting
+    s.step()
+    s.checkpoint(jid, str(tmp_path / "a.npz"))
+    with pytest.raises(ValueError):
+        Server(FakeBackend()).submit(req(seed=4), resume=str(tmp_path / "a.npz"))

@@ -49,6 +49,7 @@ from __future__ import annotations
 
 import itertools
 import math
+import os
 import time
 from dataclasses import dataclass, field
 from typing import Any, Callable, Optional
@@ -160,6 +161,13 @@ class FakeBackend:
             for k in range(first, first + n):
                 rng = np.random.default_rng([job.req.seed, k])
                 job.bufs[b] += (base + self.noise * rng.standard_normal(npx))[:, None]
+
+    def save_bufs(self, job: JobState) -> list:
+        return [np.array(b, copy=True) for b in job.bufs]
+
+    def load_bufs(self, job: JobState, arrays: list) -> None:
+        for dst, src in zip(job.bufs, arrays):
+            dst[...] = src
 
     def means(self, job: JobState):
         a, b = job.bufs
@@ -386,6 +394,23 @@ class GpuBackend:
     def free(self, job: JobState) -> None:
         job.bufs = None
 
+    def save_bufs(self, job: JobState) -> list:
+        """Host copies of the job's accumulators (after its passes so far)."""
+        for st in self.streams:
+            st.synchronize()
+        with self.torch.cuda.stream(self.stream):
+            return [b.cpu().numpy() for b in job.bufs]
+
+    def load_bufs(self, job: JobState, arrays: list) -> None:
+        """Restores saved accumulators on the first render stream; passes on
+        other streams wait for the copy like for the zero fill."""
+        t = self.torch
+        with t.cuda.stream(self.stream):
+            for dst, src in zip(job.bufs, arrays):
+                dst.copy_(t.from_numpy(np.ascontiguousarray(src, np.float32)))
+            job.ready = t.cuda.Event()
+            job.ready.record(self.stream)
+
     # -- rendering -------------------------------------------------------
     def _enqueue(self, work: list[tuple[JobState, int, int, int]], k: int = 0) -> None:
         from dataclasses import replace
@@ -587,11 +612,38 @@ class Server:
         self.pending: list = []   # pipelined: (estimate handle, jobs) in issue order
 
     # -- requests --------------------------------------------------------
-    def submit(self, req: JobRequest, arrival: Optional[float] = None) -> int:
+    def submit(self, req: JobRequest, arrival: Optional[float] = None, resume: Optional[str] = None) -> int:
+        """Queues a request; with `resume`, the job continues from a checkpoint
+        written by checkpoint() for the same request (scene, settings, size,
+        seed), so it renders exactly the passes it had left."""
         jid = next(self._ids)
-        self.jobs[jid] = JobState(jid, req, self.clock() if arrival is None else arrival)
+        job = JobState(jid, req, self.clock() if arrival is None else arrival)
+        if resume is not None:
+            with np.load(resume, allow_pickle=False) as z:
+                meta = {k: z[k].item() for k in z.files if k.startswith("m_")}
+                job.saved_bufs = [np.array(z[f"buf{i}"]) for i in range(int(meta["m_nbufs"]))]
+            if (meta["m_width"], meta["m_height"], meta["m_seed"]) != (req.width, req.height, req.seed):
+                raise ValueError("checkpoint of a different request (size or seed)")
+            job.saved_meta = meta
+        self.jobs[jid] = job
         self.waiting.append(jid)
         return jid
+
+    def checkpoint(self, job_id: int, path: str) -> None:
+        """Writes an active job's accumulators and pass state to `path` (.npz,
+        by rename).  The job must have no estimate in flight."""
+        job = self.jobs[job_id]
+        if job.state != "active" or job.pending:
+            raise ValueError(f"job {job_id} is {job.state}{' with an estimate in flight' if job.pending else ''}")
+        bufs = self.backend.save_bufs(job)
+        meta = {"m_width": job.req.width, "m_height": job.req.height, "m_seed": job.req.seed,
+                "m_nbufs": len(bufs), "m_samples": job.samples, "m_n_a": job.n_a, "m_n_b": job.n_b,
+                "m_passes": job.passes, "m_next_spp": job.next_spp, "m_need_spp": job.need_spp,
+                "m_estimate": job.estimate, "m_plain_estimate": job.plain_estimate}
+        tmp = path + ".tmp"
+        with open(tmp, "wb") as f:
+            np.savez(f, **{f"buf{i}": b for i, b in enumerate(bufs)}, **{k: np.array(v) for k, v in meta.items()})
+        os.replace(tmp, path)
 
     def cancel(self, job_id: int) -> None:
         job = self.jobs[job_id]
@@ -618,7 +670,17 @@ class Server:
             if len(self.active) < self.cfg.max_active and self.used + need <= self.cfg.memory_budget:
                 try:
                     job.bufs = self.backend.alloc(job)
-                except Exception as e:  # an allocation failure fails this job only
+                    meta = getattr(job, "saved_meta", None)
+                    if meta is not None:
+                        if len(job.saved_bufs) != len(job.bufs):
+                            raise ValueError("checkpoint buffers do not match the request (denoising on/off)")
+                        self.backend.load_bufs(job, job.saved_bufs)
+                        job.samples, job.n_a, job.n_b = meta["m_samples"], meta["m_n_a"], meta["m_n_b"]
+                        job.passes, job.next_spp, job.need_spp = meta["m_passes"], meta["m_next_spp"], meta["m_need_spp"]
+                        job.estimate, job.plain_estimate = meta["m_estimate"], meta["m_plain_estimate"]
+                        job.saved_bufs = job.saved_meta = None
+                except Exception as e:  # an allocation or restore failure fails this job only
+                    job.bufs = None
                     job.state, job.error, job.finished = "failed", str(e), self.clock()
                     continue
                 self.used += need
