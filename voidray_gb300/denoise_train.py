@@ -57,10 +57,11 @@ def random_camera(rng) -> Camera:
     return Camera.look_at(eye, at, (0.0, 1.0, 0.0), degrees_to_radians(float(rng.uniform(30.0, 60.0))))
 
 
-def render_dataset(views: int, views_per_scene: int = 50, seed: int = 0, size: int = SIZE, log=print):
+def render_dataset(views: int, views_per_scene: int = 50, seed: int = 0, size: int = SIZE, log=print,
+                   target_spp: int = TARGET_SPP):
     """Renders `views` training views; returns a dict of device tensors
     (views x size x size x 4, f32): rad4/alb4/nrm4 (4 spp means), radx/albx/nrmx
-    (extra-spp means), target (1024 spp mean), and the extra spp per view."""
+    (extra-spp means), target (target_spp mean), and the extra spp per view."""
     import torch
 
     n = views
@@ -92,14 +93,14 @@ def render_dataset(views: int, views_per_scene: int = 50, seed: int = 0, size: i
                               albedo_device=data["alb4"][v].data_ptr(), normal_device=data["nrm4"][v].data_ptr())
                 render_device(acc, st, xs, data["radx"][v].data_ptr(), size, size, seed=base + 1, stream=h,
                               albedo_device=data["albx"][v].data_ptr(), normal_device=data["nrmx"][v].data_ptr())
-                render_device(acc, st, TARGET_SPP, data["target"][v].data_ptr(), size, size, seed=base + 2, stream=h)
+                render_device(acc, st, target_spp, data["target"][v].data_ptr(), size, size, seed=base + 2, stream=h)
                 data["rad4"][v] /= IN_SPP
                 data["alb4"][v] /= IN_SPP
                 data["nrm4"][v] /= IN_SPP
                 data["radx"][v] /= xs
                 data["albx"][v] /= xs
                 data["nrmx"][v] /= xs
-                data["target"][v] /= TARGET_SPP
+                data["target"][v] /= target_spp
             v += 1
         stream.synchronize()
         acc.destroy()
@@ -166,7 +167,7 @@ def train(net: Denoiser, data: dict, train_idx: np.ndarray, steps: int, batch: i
 
 
 def evaluate(net: Denoiser, data: dict, idx: np.ndarray) -> dict:
-    """relMSE against the 1024-spp target of the plain inputs and of their
+    """relMSE against the high-spp target of the plain inputs and of their
     denoised versions, per input spp."""
     import torch
 
@@ -207,10 +208,13 @@ def main(argv=None):
     ap.add_argument("--time-budget", type=float, default=0.0, help="seconds of training (0: all steps)")
     ap.add_argument("--relmse-frac", type=float, default=0.5, help="share of steps with the relative-MSE loss")
     ap.add_argument("--p4", type=float, default=0.3, help="share of 4-spp inputs in the batches")
+    ap.add_argument("--size", type=int, default=SIZE, help="view side in pixels")
+    ap.add_argument("--target-spp", type=int, default=TARGET_SPP, help="samples per pixel of the targets")
+    ap.add_argument("--compare", default=None, help="also evaluate these weights (bf16 .npy) on the held-out views")
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
-    data = render_dataset(a.views, a.views_per_scene, a.seed, log=log)
+    data = render_dataset(a.views, a.views_per_scene, a.seed, size=a.size, log=log, target_spp=a.target_spp)
     t_data = time.perf_counter() - t0
     rng = np.random.default_rng(a.seed + 1)
     perm = rng.permutation(a.views)
@@ -221,12 +225,17 @@ def main(argv=None):
     info = train(net, data, tr, a.steps, a.batch, a.crop, a.lr, a.seed, log=log, time_budget=a.time_budget,
                  relmse_frac=a.relmse_frac, p4=a.p4)
     after = evaluate(net, data, val)
+    compared = None
+    if a.compare:
+        other = Denoiser.pretrained(a.compare)
+        compared = evaluate(other, data, val)
+        other.destroy()
     net.save(a.out)
-    report = {"views": a.views, "train_views": int(len(tr)), "val_views": int(nval), "size": SIZE,
-              "input_spp": IN_SPP, "extra_spp": list(EXTRA_SPP), "target_spp": TARGET_SPP,
+    report = {"views": a.views, "train_views": int(len(tr)), "val_views": int(nval), "size": a.size,
+              "input_spp": IN_SPP, "extra_spp": list(EXTRA_SPP), "target_spp": a.target_spp,
               "firefly_clamp": FIREFLY_CLAMP, "data_seconds": t_data, "train": info, "val_untrained": before,
-              "val": after}
-    log(json.dumps({k: report[k] for k in ("val", "data_seconds")}))
+              "val": after, "val_compare": compared, "compare_weights": a.compare}
+    log(json.dumps({k: report[k] for k in ("val", "val_compare", "data_seconds")}))
     if a.report:
         with open(a.report, "w") as f:
             json.dump(report, f, indent=1)
