@@ -93,6 +93,9 @@ class JobState:
     next_spp: int = 0          # adaptive: samples of the job's next pass (0: first pass)
     pending: bool = False      # pipelined: an estimate is in flight
     need_spp: int = 0          # samples the last estimate predicts the job needs (0: assume error ~ 1/n)
+    ready: Any = None          # GPU backend: event after the buffers' fill or restore, until the first pass
+    saved_bufs: Any = None     # submit(resume=...): accumulators restored at admission
+    saved_meta: Optional[dict] = None  # and the pass state that goes with them
 
     @property
     def latency(self) -> Optional[float]:
@@ -420,10 +423,9 @@ class GpuBackend:
         stream = self.streams[k]
         jobs = []
         for job, b, first, n in work:
-            ready = getattr(job, "ready", None)
-            if ready is not None:
+            if job.ready is not None:
                 if k != 0:
-                    stream.wait_event(ready)
+                    stream.wait_event(job.ready)
                 job.ready = None
             # buffers accumulate raw sums: total_samples = 1
             st = replace(job.req.settings, total_samples=1)
@@ -670,7 +672,7 @@ class Server:
             if len(self.active) < self.cfg.max_active and self.used + need <= self.cfg.memory_budget:
                 try:
                     job.bufs = self.backend.alloc(job)
-                    meta = getattr(job, "saved_meta", None)
+                    meta = job.saved_meta
                     if meta is not None:
                         if len(job.saved_bufs) != len(job.bufs):
                             raise ValueError("checkpoint buffers do not match the request (denoising on/off)")
