@@ -41,6 +41,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 
 #include "dn_kernels.h"
 
@@ -755,10 +756,22 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
     }
+    // resident CTAs per SM for this shared-memory size (asked once per size)
+    static std::pair<size_t, int> occ_cache[8] = {};
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_halo, HALO_THREADS, pl.smem) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 1;
+    for (const auto& c : occ_cache)
+        if (c.first == pl.smem) per_sm = c.second;
+    if (!per_sm) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_halo, HALO_THREADS, pl.smem) !=
+                cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        for (auto& c : occ_cache)
+            if (!c.first) {
+                c = {pl.smem, per_sm};
+                break;
+            }
+    }
     const int ncols = ntile <= 32 ? 32 : ntile <= 64 ? 64 : ntile <= 128 ? 128 : 256;
     per_sm = std::min(per_sm, 512 / (2 * ncols));  // the accumulators of co-resident CTAs fit in TMEM
     const int ny = a.cout / ntile;
