@@ -748,6 +748,11 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (pl.smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
         if (e != cudaSuccess) return e;
+        // the whole unified L1 / shared array as shared memory, so that several
+        // CTAs of the smaller plans share an SM (their pipelines are latency-bound)
+        e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
         configured = pl.smem;
     }
     static int sms = 0;
@@ -818,6 +823,9 @@ cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     static size_t configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
