@@ -41,7 +41,6 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
-#include <utility>
 
 #include "dn_kernels.h"
 
@@ -761,21 +760,28 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
     }
-    // resident CTAs per SM for this shared-memory size (asked once per size)
-    static std::pair<size_t, int> occ_cache[8] = {};
-    int per_sm = 0;
-    for (const auto& c : occ_cache)
-        if (c.first == pl.smem) per_sm = c.second;
-    if (!per_sm) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3x3_halo, HALO_THREADS, pl.smem) !=
-                cudaSuccess ||
-            per_sm < 1)
-            per_sm = 1;
-        for (auto& c : occ_cache)
-            if (!c.first) {
-                c = {pl.smem, per_sm};
-                break;
-            }
+    // resident CTAs per SM, from the kernel's registers and static shared memory
+    // and the SM's shared memory (the maximum carveout is requested above);
+    // any grid is correct (CTAs stride over the tiles), this only sizes it
+    static int regs = -1, static_smem = 0, sm_smem = 0, reserved = 0;
+    if (regs < 0) {
+        cudaFuncAttributes fa{};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        regs = cudaFuncGetAttributes(&fa, k_conv3x3_halo) == cudaSuccess ? fa.numRegs : 0;
+        static_smem = (int)fa.sharedSizeBytes;
+        if (cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+            sm_smem = 0;
+        if (cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+            reserved = 0;
+        cudaGetLastError();
+    }
+    int per_sm = 1;
+    if (regs > 0 && sm_smem > 0) {
+        const int by_smem = sm_smem / (int)(pl.smem + (size_t)static_smem + (size_t)reserved);
+        const int regs_per_warp = ((regs + 7) / 8) * 8 * 32;
+        const int by_regs = 65536 / (regs_per_warp * (HALO_THREADS / 32));
+        per_sm = std::max(1, std::min({by_smem, by_regs, 2048 / HALO_THREADS}));
     }
     const int ncols = ntile <= 32 ? 32 : ntile <= 64 ? 64 : ntile <= 128 ? 128 : 256;
     per_sm = std::min(per_sm, 512 / (2 * ncols));  // the accumulators of co-resident CTAs fit in TMEM
