@@ -21,8 +21,8 @@
 // Every mbarrier wait is bounded: a wait that runs out sets an error bit in
 // the caller's status word and the CTA still drains and frees its TMEM.
 //
-// k_conv3x3_halo runs shapes of 64-128 output channels per CTA (the tile
-// kernel above the rest; conv3x3_tc chooses).  Its tile is 16 rows x 8 columns of
+// k_conv3x3_halo runs shapes of up to 128 output channels per CTA (the tile
+// kernel above the wider ones; conv3x3_tc chooses).  Its tile is 16 rows x 8 columns of
 // output pixels (M = 128, one 8-pixel row segment per 8-row core matrix).
 // Per K chunk it loads one 18 x 10 halo of the input (BK/8 TMA boxes of
 // 8 channels x 10 x 18) into the no-swizzle canonical K-major layout
@@ -694,10 +694,10 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
 }
 
 // Variant per shape, from per-layer launch lists of the 1080p forward pass on
-// GB300: the halo kernel is 10-40% faster where a CTA computes 64 or 128
-// output channels; with 16 or 32 its 16-byte TMA rows cannot keep the tensor
-// pipe busy and with 256 the streamed weights dominate, so those shapes run
-// the tile kernel.  VR_DN_TC_VARIANT=tile / halo forces one variant.
+// GB300: with several CTAs per SM the halo kernel is 1.4-2.3x faster than the
+// tile kernel up to 128 output channels per CTA; at 256 the streamed weights
+// dominate and the tile kernel is faster.  VR_DN_TC_VARIANT=tile / halo forces
+// one variant.
 bool use_tile_variant(int ntile) {
     static const int forced = [] {
         const char* e = std::getenv("VR_DN_TC_VARIANT");
@@ -706,7 +706,7 @@ bool use_tile_variant(int ntile) {
         return 0;
     }();
     if (forced) return forced == 1;
-    return !(ntile >= 64 && ntile <= 128);
+    return ntile > 128;
 }
 
 cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
