@@ -643,8 +643,17 @@ bool conv3x3_tc_supported(const ConvArgs& a) {
 
 namespace {
 
-constexpr size_t HALO_SMEM_BUDGET = 200 * 1024;
 constexpr size_t HALO_RESIDENT_MAX = 128 * 1024;
+
+// dynamic shared memory a halo plan may use (VR_DN_HALO_SMEM_KB overrides, for measurements)
+size_t halo_smem_budget() {
+    static const size_t b = [] {
+        const char* e = std::getenv("VR_DN_HALO_SMEM_KB");
+        const long kb = e ? std::strtol(e, nullptr, 10) : 0;
+        return (kb >= 32 && kb <= 200) ? (size_t)kb * 1024 : (size_t)200 * 1024;
+    }();
+    return b;
+}
 
 size_t round1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 
@@ -664,10 +673,10 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
         const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t w = (size_t)(cin / bk) * 9 * b_box;
-        if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= HALO_SMEM_BUDGET) {
+        if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= halo_smem_budget()) {
             p.bk = bk;
             p.resident = 1;
-            p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, (HALO_SMEM_BUDGET - w) / a_stage);
+            p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, (halo_smem_budget() - w) / a_stage);
             p.a_stage = a_stage;
             p.b_box = b_box;
             p.b_off = (size_t)p.stages * a_stage;
@@ -680,10 +689,10 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
         const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t stage = a_stage + 9 * b_box;
-        if (2 * stage > HALO_SMEM_BUDGET) continue;
+        if (2 * stage > halo_smem_budget()) continue;
         p.bk = bk;
         p.resident = 0;
-        p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, HALO_SMEM_BUDGET / stage);
+        p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, halo_smem_budget() / stage);
         p.a_stage = a_stage;
         p.b_box = b_box;
         p.b_off = (size_t)p.stages * a_stage;
@@ -713,7 +722,7 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     const int cin = a.c1 + a.c2;
     const int ntile = ntile_for(a.cout);
     const HaloPlan pl = plan_halo(a.c1, a.c2, ntile);
-    if (!pl.bk) return cudaErrorInvalidValue;
+    if (!pl.bk) return cudaErrorNotSupported;  // no plan within the budget: the caller runs the tile kernel
     CUtensorMap ma1, ma2, mb;
     std::memset(&ma2, 0, sizeof ma2);
     if (!encode_act_halo(&ma1, a.src1, a.n, a.h, a.w, a.c1)) return cudaErrorInvalidValue;
@@ -795,7 +804,10 @@ cudaError_t conv3x3_halo(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
 
 cudaError_t conv3x3_tc(const ConvArgs& a, uint32_t* status, cudaStream_t st) {
     if (!conv3x3_tc_supported(a)) return cudaErrorInvalidValue;
-    if (!use_tile_variant(ntile_for(a.cout))) return conv3x3_halo(a, status, st);
+    if (!use_tile_variant(ntile_for(a.cout))) {
+        const cudaError_t e = conv3x3_halo(a, status, st);
+        if (e != cudaErrorNotSupported) return e;
+    }
     const int cin = a.c1 + a.c2;
     // largest chunk that divides both sources (a chunk never straddles them)
     int bk = 64;
