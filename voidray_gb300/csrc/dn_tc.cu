@@ -645,14 +645,18 @@ namespace {
 
 constexpr size_t HALO_RESIDENT_MAX = 128 * 1024;
 
-// dynamic shared memory a halo plan may use (VR_DN_HALO_SMEM_KB overrides, for measurements)
-size_t halo_smem_budget() {
-    static const size_t b = [] {
+// Dynamic shared memory a halo plan may use.  Up to 64 output channels per
+// CTA a 110 KB plan (two CTAs per SM) beat the 200 KB one (one CTA per SM)
+// by 20-27% per layer at 1080p; with 128 the larger chunks of the 200 KB plan
+// won by 5-10%.  VR_DN_HALO_SMEM_KB overrides both, for measurements.
+size_t halo_smem_budget(int ntile) {
+    static const long forced = [] {
         const char* e = std::getenv("VR_DN_HALO_SMEM_KB");
         const long kb = e ? std::strtol(e, nullptr, 10) : 0;
-        return (kb >= 32 && kb <= 200) ? (size_t)kb * 1024 : (size_t)200 * 1024;
+        return (kb >= 32 && kb <= 200) ? kb : 0L;
     }();
-    return b;
+    if (forced) return (size_t)forced * 1024;
+    return (size_t)(ntile <= 64 ? 110 : 200) * 1024;
 }
 
 size_t round1k(size_t x) { return (x + 1023) & ~size_t(1023); }
@@ -667,16 +671,17 @@ struct HaloPlan {
 // them, else streamed weights with the largest chunk that leaves two stages
 HaloPlan plan_halo(int c1, int c2, int ntile) {
     const int cin = c1 + c2;
+    const size_t budget = halo_smem_budget(ntile);
     HaloPlan p;
     for (int bk = 64; bk >= 16; bk >>= 1) {
         if (c1 % bk || c2 % bk) continue;
         const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t w = (size_t)(cin / bk) * 9 * b_box;
-        if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= halo_smem_budget()) {
+        if (w <= HALO_RESIDENT_MAX && w + 2 * a_stage <= budget) {
             p.bk = bk;
             p.resident = 1;
-            p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, (halo_smem_budget() - w) / a_stage);
+            p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, (budget - w) / a_stage);
             p.a_stage = a_stage;
             p.b_box = b_box;
             p.b_off = (size_t)p.stages * a_stage;
@@ -689,10 +694,10 @@ HaloPlan plan_halo(int c1, int c2, int ntile) {
         const size_t a_stage = round1k((size_t)(bk / 8) * HALO_GROUP_BYTES);
         const size_t b_box = round1k((size_t)ntile * bk * 2);
         const size_t stage = a_stage + 9 * b_box;
-        if (2 * stage > halo_smem_budget()) continue;
+        if (2 * stage > budget) continue;
         p.bk = bk;
         p.resident = 0;
-        p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, halo_smem_budget() / stage);
+        p.stages = (int)std::min<size_t>(HALO_MAX_STAGES, budget / stage);
         p.a_stage = a_stage;
         p.b_box = b_box;
         p.b_off = (size_t)p.stages * a_stage;
