@@ -141,3 +141,37 @@ def test_tuning_cache_keys(tmp_path, monkeypatch):
     assert k1 != T.bucket_key("GB300", 2_000_000, 1920 * 1080, 256, 0)
     T.save_cache({k1: {"wavefront_paths": 1 << 25}})
     assert T.load_cache()[k1]["wavefront_paths"] == 1 << 25
+
+
+def test_descriptor_limits_and_edge_cases(native):
+    """Host validation of the edge cases the scene descriptor can carry: more
+    analytic surfaces than VR_MAX_ANALYTICS, an unknown material kind, empty
+    or ill-formed textures, and a scene whose only mesh has no triangles."""
+    base = vr.Materials.lambertian((0.5, 0.5, 0.5))
+    s = vr.Scene()
+    m = s.add_material(base)
+    for k in range(65):
+        s.add_object(m, s.add_analytic_surface(vr.Surfaces.sphere((k, 0, 0), 0.4)))
+    with pytest.raises(vr.VoidrayError) as e:
+        s.validate()
+    assert e.value.status == 2
+    s = vr.Scene()
+    bad = vr.Materials.lambertian((0.5, 0.5, 0.5))
+    bad.kind = 9
+    s.add_object(s.add_material(bad), s.add_mesh(vr.Mesh(np.eye(3, dtype=np.float32), [0, 1, 2])))
+    with pytest.raises(vr.VoidrayError) as e:
+        s.validate()
+    assert e.value.status == 2
+    for tex in (np.zeros((0, 4, 3), np.float32), np.zeros((4, 4), np.float32)):
+        with pytest.raises(vr.VoidrayError):
+            vr.ImageTexture(tex)
+    s = vr.Scene()
+    t = s.add_texture(vr.ImageTexture(np.ones((2, 2, 3), np.float32)))
+    s.textures[t].sample_type = 7
+    s.add_object(s.add_material(vr.Materials.lambertian_texture_no_normal(t)),
+                 s.add_mesh(vr.Mesh(np.eye(3, dtype=np.float32), [0, 1, 2])))
+    with pytest.raises(vr.VoidrayError):
+        s.validate()   # unknown sampling
+    s = vr.Scene()
+    s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(np.zeros((0, 3), np.float32), np.zeros(0, np.uint32))))
+    assert s.validate().num_triangles == 0

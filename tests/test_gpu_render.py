@@ -252,3 +252,41 @@ def test_renders_converge_at_4096_spp(gpu, oracle):
     # (pixels are not all bit-identical: over 4096 samples a pixel collects the
     # rare counted t ties and last-ulp cases that the 16-spp parity tests allow)
     assert relmse(g, o) < 1e-4
+
+
+def test_zero_samples_add_only_alpha(gpu, oracle):
+    """iterative_render with samples = 0 still visits every pixel: rgb gains
+    +0.0 and alpha gains Color::a() = 1 (iterative.rs:37-50); through
+    vr_render, the AOV variant and a batch job alike."""
+    import torch
+
+    from voidray_gb300.batch import Batch, RenderJob
+
+    scene, st = W.cornell_box()
+    acc = scene.build_acceleration()
+    rng = np.random.default_rng(4)
+    start = rng.uniform(0.0, 2.0, (12, 20, 4)).astype(np.float32)
+    t = vr.CpuRenderTarget(20, 12)
+    t.buffer[...] = start
+    vr.iterative_render(t, acc, st, 0, seed=1)
+    o = start.copy()
+    o, _ = oracle.OracleScene(scene).render(st, 0, 20, 12, seed=1, rgba=o)
+    assert np.array_equal(t.buffer, o)
+    assert np.array_equal(t.buffer[..., :3], start[..., :3]) and np.all(t.buffer[..., 3] == start[..., 3] + 1)
+    # AOV variant and a zero-sample job in a batch
+    bufs = [torch.from_numpy(start.copy()).cuda() for _ in range(3)]
+    vr.render_device(acc, st, 0, bufs[0].data_ptr(), 20, 12, albedo_device=bufs[1].data_ptr(),
+                     normal_device=bufs[2].data_ptr())
+    acc.synchronize()
+    for b in bufs:
+        assert np.array_equal(b.cpu().numpy(), o)
+    img = torch.from_numpy(start.copy()).cuda()
+    other = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda")
+    batch = Batch()
+    stream = torch.cuda.Stream()
+    batch.render([RenderJob(acc, st, 0, img.data_ptr(), 20, 12, 1, 0), RenderJob(acc, st, 2, other.data_ptr(), 8, 8)],
+                 stream.cuda_stream)
+    batch.synchronize(stream.cuda_stream)
+    assert np.array_equal(img.cpu().numpy(), o)
+    assert np.all(other.cpu().numpy()[..., 3] == 1.0)
+    batch.destroy()

@@ -219,3 +219,12 @@ def test_hdri_lookup_at_poles_and_seams(oracle):
         seen.add((x0, y0, ax, ay))
     # the quirks are exercised: top-pole extrapolation and the x0 = W-1, ax = 1 seam
     assert any(ay < 0 for *_, ay in seen) and any(x0 == 15 and ax == 1.0 for x0, _, ax, _ in seen)
+
+
+def test_zero_sample_call_adds_only_alpha(oracle):
+    """iterative.rs:37-50 with samples = 0: rgb += 0, alpha += Color::a() = 1."""
+    scene, st = W.cornell_box()
+    start = np.random.default_rng(2).uniform(0, 1, (6, 5, 4)).astype(np.float32)
+    o, rays = oracle.OracleScene(scene).render(st, 0, 5, 6, rgba=start.copy())
+    assert np.array_equal(o[..., :3], start[..., :3]) and np.all(o[..., 3] == start[..., 3] + 1)
+    assert rays[0] == 0

@@ -661,9 +661,12 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
     if (r != VR_OK) return r;
     if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
     if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
-    if (samples == 0) return VR_OK;
     cudaStream_t cs = pick(s, stream);
     const uint32_t np = w * h;
+    if (samples == 0) {
+        VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(rgba), np, cs));
+        return VR_OK;
+    }
     const uint64_t total = (uint64_t)samples * np;
     // default wavefront: 2^26 paths (about 12 GB of path state with the NEE
     // estimator, 21 GB with the reference estimator at depth 12); deep
@@ -698,9 +701,12 @@ vr_status vr_render_aov_device(vr_scene* s, const vr_render_settings* st, uint32
     if (r != VR_OK) return r;
     if (!rgba || !albedo || !normal) return fail(VR_ERR_INVALID, "rgba, albedo and normal must be set");
     if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
-    if (samples == 0) return VR_OK;
     cudaStream_t cs = pick(s, stream);
     const uint32_t np = w * h;
+    if (samples == 0) {
+        for (float* buf : {rgba, albedo, normal}) VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(buf), np, cs));
+        return VR_OK;
+    }
     const uint64_t total = (uint64_t)samples * np;
     uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
     if (cap > (1ull << 28)) cap = 1ull << 28;
@@ -826,8 +832,19 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
         pixels += (uint64_t)j.width * j.height * (aov ? 3 : 1);
         if (j.settings.estimator == VR_EST_REFERENCE) att_depth = std::max(att_depth, j.settings.max_bounces);
     }
-    if (total == 0) return VR_OK;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    // zero-sample jobs still add (0, 0, 0, 1) to their images, like iterative_render
+    for (uint32_t i = 0; i < count; ++i) {
+        const vr_render_job& j = jobs[i];
+        if (j.samples) continue;
+        const uint32_t np = j.width * j.height;
+        VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(j.rgba_device), np, cs));
+        if (j.albedo_device) {
+            VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(j.albedo_device), np, cs));
+            VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(j.normal_device), np, cs));
+        }
+    }
+    if (total == 0) return VR_OK;
     const uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
     const void* before = b->eng.ps.q_org;
     if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs, want_aov)) != VR_OK) return r;
@@ -1134,8 +1151,11 @@ vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, ui
     if (r != VR_OK) return r;
     if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
     if ((uint64_t)first_sample + samples >= (1ull << 31)) return fail(VR_ERR_INVALID, "sample index out of range");
-    if (samples == 0) return VR_OK;
     const uint32_t np = w * h;
+    if (samples == 0) {
+        VR_CK(vr::launch_empty_pass(reinterpret_cast<float4*>(rgba), np, pick(s, stream)));
+        return VR_OK;
+    }
     const uint64_t total = (uint64_t)samples * np;
     const bool need_att = st->estimator == VR_EST_REFERENCE;
     // fixed layout: pixel sums, counters, wave table, then the per-path arrays

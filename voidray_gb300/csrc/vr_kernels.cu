@@ -904,6 +904,20 @@ __global__ void k_wave_stats(Wave w, PathState ps, uint32_t bounces, unsigned lo
     totals[2] += shd;
 }
 
+// iterative_render with samples = 0 (iterative.rs:37-50): the colour stays
+// BLACK, so rgb gains +0.0 and alpha gains Color::a() = 1, like any call
+__global__ void k_empty_pass(float4* __restrict__ rgba, uint32_t np) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < np; px += stride) {
+        float4 o = rgba[px];
+        o.x = o.x + 0.0f;
+        o.y = o.y + 0.0f;
+        o.z = o.z + 0.0f;
+        o.w = o.w + 1.0f;
+        rgba[px] = o;
+    }
+}
+
 __global__ void k_finalize(const float4* __restrict__ psum, float4* __restrict__ rgba, uint32_t np, float inv_total) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < np; px += stride) {
@@ -1153,6 +1167,12 @@ __global__ void k_env_sample(SceneView s, const float* __restrict__ dirs, uint64
         rgb[3 * i + 1] = c.y;
         rgb[3 * i + 2] = c.z;
     }
+}
+
+cudaError_t launch_empty_pass(float4* rgba, uint32_t np, cudaStream_t st) {
+    if (np == 0) return cudaSuccess;
+    k_empty_pass<<<grid_for(np, 256, 8), 256, 0, st>>>(rgba, np);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_env_sample(const SceneView& s, const float* dirs, uint64_t n, float* rgb, cudaStream_t st) {

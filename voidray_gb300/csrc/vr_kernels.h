@@ -101,6 +101,8 @@ cudaError_t launch_accumulate(const Wave& w, const PathState& ps, uint32_t max_p
 cudaError_t launch_finalize(const float4* psum, float4* rgba, uint32_t np, float inv_total, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, float4* out, uint32_t np, int32_t tonemap, float inv_gamma, float ex,
                            float scale, int32_t transparent, cudaStream_t st);
+// rgba += (0, 0, 0, 1): a render call with zero samples
+cudaError_t launch_empty_pass(float4* rgba, uint32_t np, cudaStream_t st);
 cudaError_t launch_env_sample(const SceneView& s, const float* dirs, uint64_t n, float* rgb, cudaStream_t st);
 cudaError_t launch_relmse(const float4* a, float sa, const float4* r, float sr, uint32_t np, double* out,
                           cudaStream_t st);
