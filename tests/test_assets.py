@@ -284,3 +284,21 @@ def test_files_reach_textures_and_environments(tmp_path):
     assert env.image.shape == (3, 4, 3) and env.image[0, 0].tolist() == [1.0, 2.0, 3.0]
     with pytest.raises(VoidrayError, match="not decoded here"):
         A.load_image_rgb32f(str(tmp_path / "x.jpg"))
+
+
+REF_PNGS = [os.path.join(os.environ.get("VOIDRAY_REFERENCE", "/root/reference"), "assets", f)
+            for f in ("test.png", "uv_test.png")]
+
+
+@pytest.mark.skipif(not all(os.path.exists(p) for p in REF_PNGS), reason="reference assets not present")
+def test_png_reads_the_reference_assets():
+    """The reference's own PNGs (written by another encoder, RGBA 8-bit): every
+    chunk CRC and the zlib checksum verify, the size is the header's, and the
+    values lie on the u8 / 255 grid to_rgb32f produces."""
+    shapes = []
+    for p in REF_PNGS:
+        img = A.load_image_rgb32f(p)
+        shapes.append(img.shape)
+        q = img * np.float32(255)
+        assert np.all(np.abs(q - np.round(q)) < 1e-4) and img.min() >= 0 and img.max() <= 1
+    assert shapes == [(2, 2, 3), (256, 256, 3)]
