@@ -408,3 +408,57 @@ def test_checkpoint_rejects_mismatch_and_in_flight(tmp_path):
     s.checkpoint(jid, str(tmp_path / "a.npz"))
     with pytest.raises(ValueError):
         Server(FakeBackend()).submit(req(seed=4), resume=str(tmp_path / "a.npz"))
+
+
+hypothesis = pytest.importorskip("hypothesis")
+from hypothesis import given, settings, strategies as st  # noqa: E402
+
+
+@settings(max_examples=40, deadline=None)
+@given(seed=st.integers(0, 10_000), n_jobs=st.integers(1, 12), budget_jobs=st.integers(1, 6),
+       mode=st.sampled_from(["plain", "adaptive", "pipelined"]), cancel_every=st.integers(0, 5))
+def test_scheduler_invariants_under_random_load(seed, n_jobs, budget_jobs, mode, cancel_every):
+    """Random arrivals, sizes, targets, memory budgets and cancellations:
+    memory in use never exceeds the budget, every job ends done, cancelled
+    or failed with its memory returned, and a chosen job's result equals
+    its result alone (whatever else ran, unless it was cancelled)."""
+    rng = np.random.default_rng(seed)
+    sizes = [(int(rng.integers(4, 17)), int(rng.integers(4, 17))) for _ in range(n_jobs)]
+    foot = max(2 * w * h * 16 for w, h in sizes)
+    cfg = ServerConfig(memory_budget=budget_jobs * foot, max_active=int(rng.integers(1, 9)), spp_per_pass=8,
+                       min_samples=16, adaptive=mode != "plain", pipelined=mode == "pipelined",
+                       pass_paths=int(rng.integers(1, 5)) * 16 * 16 * 32, first_pass_spp=16)
+
+    def make(k):
+        w, h = sizes[k]
+        return req(seed=1000 + k, w=w, h=h, target=float(rng.choice([5e-4, 1e-3, 3e-3])),
+                   max_samples=int(rng.choice([64, 256, 1024])), scene=f"s{k % 3}")
+
+    reqs = [make(k) for k in range(n_jobs)]
+    s = Server(LaggingBackend(lag=int(rng.integers(0, 3)), noise=0.3), cfg, clock=Clock())
+    ids = []
+    step = 0
+    pending = list(range(n_jobs))
+    while pending or not s.idle():
+        if pending and (step % 2 == 0 or s.idle()):
+            ids.append(s.submit(reqs[pending.pop(0)]))
+        s.step()
+        step += 1
+        assert 0 <= s.used <= cfg.memory_budget
+        if cancel_every and step % (cancel_every + 3) == 0:
+            live = [i for i in ids if s.status(i).state in ("waiting", "active") and i != ids[0]]
+            if live:
+                s.cancel(live[0])
+        assert step < 100_000
+    assert s.used == 0 and not s.resident_scenes
+    assert all(s.status(i).state in ("done", "cancelled", "failed") for i in ids)
+    # the first job (never cancelled) ends as it does alone
+    j0 = s.status(ids[0])
+    alone = Server(LaggingBackend(lag=0, noise=0.3), cfg, clock=Clock())
+    a = alone.submit(reqs[0])
+    while not alone.idle():
+        alone.step()
+    ja = alone.status(a)
+    assert j0.state == ja.state == "done"
+    assert (j0.samples, j0.n_a, j0.n_b) == (ja.samples, ja.n_a, ja.n_b)
+    assert np.array_equal(j0.result, ja.result)

@@ -423,6 +423,10 @@ class GpuBackend:
         stream = self.streams[k]
         jobs = []
         for job, b, first, n in work:
+            # the allocator must not hand these buffers to another job while this
+            # stream still writes them (a job cancelled with its pass in flight)
+            for t in job.bufs:
+                t.record_stream(stream)
             if job.ready is not None:
                 if k != 0:
                     stream.wait_event(job.ready)
@@ -465,6 +469,9 @@ class GpuBackend:
         from . import _native as N
 
         t = self.torch
+        for job in jobs:  # read on this stream: no reuse of the buffers before it is done
+            for b in job.bufs:
+                b.record_stream(stream)
         with t.cuda.stream(stream):
             den = {}
             groups = {}
@@ -577,6 +584,8 @@ class GpuBackend:
         n = job.n_a + job.n_b
         h, w = job.req.height, job.req.width
         es = self.res_stream
+        for b in job.bufs:
+            b.record_stream(es)
         with t.cuda.stream(es):
             p = (job.bufs[0] + job.bufs[1]) / n
             alpha = np.asarray(job.alpha, np.float32)
@@ -769,6 +778,8 @@ class Server:
             self.pending.pop(0)
             block = False
             for job, e in zip(jobs, ests):
+                if job.state != "active":
+                    continue  # cancelled (or failed) while its estimate was in flight
                 job.estimate, job.pending = e, False
                 self._finish_or_plan(job)
 
