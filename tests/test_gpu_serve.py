@@ -212,3 +212,46 @@ def test_gpu_checkpoint_resume_is_bit_identical(gpu, tmp_path):
         be.destroy()
     finally:
         net.destroy()
+
+
+def test_cancellations_in_flight_leave_other_jobs_unchanged(gpu):
+    """Two render streams, pipelined passes, and jobs cancelled while their
+    passes or estimates are in flight (their memory goes back to the
+    allocator): the job that stays ends exactly as it does alone."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig
+
+    scenes = _scenes(vr, W)
+    cfg = ServerConfig(min_samples=16, adaptive=True, pipelined=True, pass_paths=40 * 32 * 24, first_pass_spp=16,
+                       max_inflight=3)
+    acc, st = scenes[1]
+    keep = lambda: JobRequest(acc, st, 40, 32, max_samples=256, target_relmse=5e-3, seed=31)
+
+    def run(with_others):
+        be = GpuBackend(render_streams=2)
+        s = Server(be, cfg)
+        jid = s.submit(keep())
+        others = []
+        if with_others:
+            for k in range(6):
+                a2, s2 = scenes[k % 2]
+                others.append(s.submit(JobRequest(a2, s2, 32 + 8 * k, 24, max_samples=512, target_relmse=1e-5,
+                                                  seed=90 + k)))
+        steps = 0
+        while not s.idle():
+            s.step()
+            steps += 1
+            if with_others and steps % 2 == 0:
+                live = [o for o in others if s.status(o).state in ("waiting", "active")]
+                if live:
+                    s.cancel(live[0])
+        be.finish()
+        j = s.status(jid)
+        out = (j.result, j.samples, j.n_a, j.n_b)
+        be.destroy()
+        return out, [s.status(o).state for o in others]
+
+    (r0, _), (r1, states) = run(False), run(True)
+    assert "cancelled" in states
+    assert r0[1:] == r1[1:] and np.array_equal(r0[0], r1[0])
