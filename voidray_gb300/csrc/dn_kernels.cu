@@ -344,19 +344,47 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const WgradArgs a) {
 }
 
 // ---------------------------------------------------------------- glue ----
-__global__ void k_bias_grad(const bf16* __restrict__ dz, int P, int C, int rows, float* __restrict__ db) {
-    __shared__ float red[256];
-    const int R = blockDim.x / C;
-    const int c = threadIdx.x % C, r = threadIdx.x / C;
+// db[c] += sum over pixels of dz[p][c].  Each thread sums 8 channels (one
+// 16-byte load) of every (256 / (C / 8))-th pixel of the block's rows, four
+// loads in flight; the block reduces per channel in shared memory and adds
+// one float per channel.  C is a multiple of 8 up to 256.
+__global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ dz, int P, int C, int rows,
+                                                    float* __restrict__ db) {
+    __shared__ float red[256 * 8];
+    const int tpp = C >> 3;              // threads per pixel
+    const int slots = blockDim.x / tpp;  // pixels per step
+    const int g = threadIdx.x % tpp, slot = threadIdx.x / tpp;
     const int p0 = blockIdx.x * rows, p1 = min(P, p0 + rows);
-    float s = 0.0f;
-    if (r < R)
-        for (int p = p0 + r; p < p1; p += R) s += __bfloat162float(dz[(size_t)p * C + c]);
-    red[threadIdx.x] = s;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (slot < slots) {
+        const uint4* base = reinterpret_cast<const uint4*>(dz) + g;
+        int p = p0 + slot;
+        for (; p + 3 * slots < p1; p += 4 * slots) {
+            uint4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = __ldg(base + (size_t)(p + u * slots) * tpp);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bf16* h = reinterpret_cast<const bf16*>(&v[u]);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[j] += __bfloat162float(h[j]);
+            }
+        }
+        for (; p < p1; p += slots) {
+            const uint4 v = __ldg(base + (size_t)p * tpp);
+            const bf16* h = reinterpret_cast<const bf16*>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] += __bfloat162float(h[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) red[threadIdx.x * 8 + j] = acc[j];
     __syncthreads();
-    if (r == 0) {
-        for (int k = 1; k < R; ++k) s += red[c + k * C];
-        atomicAdd(&db[c], s);
+    if (threadIdx.x < C) {  // one thread per channel: sum over the pixel slots
+        const int cg = threadIdx.x >> 3, cj = threadIdx.x & 7;
+        float s = 0.0f;
+        for (int k = 0; k < slots; ++k) s += red[(k * tpp + cg) * 8 + cj];
+        atomicAdd(&db[threadIdx.x], s);
     }
 }
 
@@ -659,7 +687,8 @@ cudaError_t conv3x3_wgrad(const WgradArgs& a, cudaStream_t st) {
 }
 
 cudaError_t bias_grad(const bf16* dz, int p, int c, float* db, cudaStream_t st) {
-    if (c <= 0 || c > 256 || (256 % c) != 0) return cudaErrorInvalidValue;
+    if (c <= 0 || c > 256 || (256 % c) != 0 || c % 8 || (reinterpret_cast<uintptr_t>(dz) & 15))
+        return cudaErrorInvalidValue;
     const int rows = 1024;
     k_bias_grad<<<(p + rows - 1) / rows, 256, 0, st>>>(dz, p, c, rows, db);
     return cudaGetLastError();

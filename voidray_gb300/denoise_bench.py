@@ -4,9 +4,10 @@
 
 Times (CUDA events, after warm-up, on a dedicated stream) the forward pass
 (inference: preprocess, 15 convolutions, pools, upsampling, postprocess) on
-the mma.sync and the tcgen05 backends, and one training step (forward on
-mma.sync, backward, Adam).  FLOPs are the network's algorithmic multiply-adds
-(2 * 9 * Cin * Cout per output pixel of every 3x3 convolution, on the padded
+the mma.sync and the tcgen05 backends, and one training step (forward,
+backward, Adam) with forward and backward-data on either backend.  FLOPs are
+the network's algorithmic multiply-adds (2 * 9 * Cin * Cout per output pixel
+of every 3x3 convolution, on the padded
 channel counts the kernels compute) times the padded pixel count; a training
 step counts three times the forward.
 """
@@ -79,14 +80,16 @@ def run(width=1920, height=1080, iters=20, batch=1, train_crop=128, train_batch=
         net.status()
         tf = flops / (ms * 1e-3) / 1e12
         res[name] = {"ms": ms, "tflops": tf, "frac": tf / peak}
-    net.set_backend(Denoiser.MMA_SYNC)
-    # one training step (batch of crops), forward + backward + Adam
+    # one training step (batch of crops), forward + backward + Adam, with forward
+    # and backward-data on each backend (weight gradients on mma.sync in both)
     tr = _inputs(train_crop, train_crop, train_batch, seed=1)
     tgt = tr[0] * 0.9
     step = lambda: net.train_step(*tr, tgt, train_batch, train_crop, train_crop, 0.0, stream=stream.cuda_stream)
-    ms = timed(step, max(5, iters // 2))
-    tflops = 3 * info.flops_per_pixel * train_crop * train_crop * train_batch / (ms * 1e-3) / 1e12
-    res["train_step"] = {"crop": train_crop, "batch": train_batch, "ms": ms, "tflops": tflops, "frac": tflops / peak}
+    for key, backend in (("train_step", Denoiser.TCGEN05), ("train_step_mma_sync", Denoiser.MMA_SYNC)):
+        net.set_backend(backend)
+        ms = timed(step, max(5, iters // 2))
+        tflops = 3 * info.flops_per_pixel * train_crop * train_crop * train_batch / (ms * 1e-3) / 1e12
+        res[key] = {"crop": train_crop, "batch": train_batch, "ms": ms, "tflops": tflops, "frac": tflops / peak}
     net.destroy()
     return res
 

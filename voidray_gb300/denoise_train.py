@@ -211,6 +211,8 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=SIZE, help="view side in pixels")
     ap.add_argument("--target-spp", type=int, default=TARGET_SPP, help="samples per pixel of the targets")
     ap.add_argument("--compare", default=None, help="also evaluate these weights (bf16 .npy) on the held-out views")
+    ap.add_argument("--backend", choices=("mma_sync", "tcgen05"), default="mma_sync",
+                    help="forward and backward-data convolutions (the shipped weights: mma_sync)")
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
@@ -221,6 +223,7 @@ def main(argv=None):
     nval = max(1, int(a.views * a.holdout))
     val, tr = perm[:nval], perm[nval:]
     net = Denoiser.pretrained(a.init) if a.init else Denoiser(seed=a.seed)
+    net.set_backend(Denoiser.TCGEN05 if a.backend == "tcgen05" else Denoiser.MMA_SYNC)
     before = evaluate(net, data, val[:20])
     info = train(net, data, tr, a.steps, a.batch, a.crop, a.lr, a.seed, log=log, time_budget=a.time_budget,
                  relmse_frac=a.relmse_frac, p4=a.p4)
