@@ -96,6 +96,8 @@ WCASES = [  # c1, c2, up1, cout, n, h, w
     (256, 128, 1, 128, 1, 16, 16),
     (64, 32, 1, 32, 2, 16, 8),
     (32, 0, 0, 64, 4, 64, 64),
+    (16, 0, 0, 32, 1, 6, 10),      # not 4 x 8 blocks: the one-tap-per-CTA kernel
+    (96, 0, 0, 32, 2, 32, 48),     # the 96 -> 32 decoder shape
 ]
 
 
@@ -122,6 +124,21 @@ def test_conv3x3_wgrad_matches_fp64(gpu, case):
     torch.cuda.synchronize()
     got = dw.double().cpu().numpy() - 0.25
     assert np.all(np.abs(got - ref) <= 2.0 ** -19 * s + 2.0 ** -24)
+
+
+def test_conv3x3_wgrad_per_tap_kernel_on_every_case(gpu):
+    """Shapes in 4 x 8 blocks run the nine-taps-per-CTA kernel; forcing the
+    one-tap-per-CTA kernel (VR_DN_WGRAD, read once per process) runs every
+    case above through it, in a child process."""
+    import os
+    import subprocess
+    import sys
+
+    env = dict(os.environ, VR_DN_WGRAD="per_tap")
+    r = subprocess.run([sys.executable, "-m", "pytest", os.path.abspath(__file__), "-q", "-p", "no:cacheprovider",
+                        "-k", "test_conv3x3_wgrad_matches_fp64"], env=env, capture_output=True, text=True,
+                       timeout=900, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
 
 
 def batch_arrays(n, h, w, seed):

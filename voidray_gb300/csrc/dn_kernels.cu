@@ -11,6 +11,8 @@
 //   glue             2x2 average pool, skip / upsample backward, bias grad,
 //                    pre/post-processing, L1 loss, Adam, weight cast + flip
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "dn_kernels.h"
 
@@ -651,6 +653,134 @@ cudaError_t launch_wgrad(WgradArgs a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+
+// Weight gradient with all nine taps per CTA: the K loop walks 4 x 8-pixel
+// blocks of the image; per block the CTA stages the 32 pixels' output
+// gradients (A, [pixel][co]) once and one 6 x 10 halo of the input (B,
+// [halo pixel][ci]) once, and each tap's B operand is that halo seen through
+// per-lane ldmatrix row addresses (pixel (r, c) of the block -> halo row
+// (r + dy + 1) * 10 + (c + dx + 1)).  Warps are (BM / 16) x (BN / 16), each
+// owning a 16 (co) x 16 (ci) tile of all nine taps; partial sums over a CTA's
+// range of blocks are added to dw with fp32 atomics.  Needs h % 4 == 0 and
+// w % 8 == 0.
+template <int BM, int BN>
+__global__ void __launch_bounds__(32 * (BM / 16) * (BN / 16)) k_conv3x3_wgrad9(const WgradArgs a) {
+    constexpr int STAGES = 3, CPA = BM / 8, CPB = BN / 8, WN = BN / 16;
+    constexpr int NTHREADS = 32 * (BM / 16) * WN;
+    constexpr int A_ROWS = 32, B_ROWS = 60;
+    constexpr int NT = 2;  // two 8-wide n tiles per warp
+    __shared__ __align__(128) bf16 sA[STAGES][A_ROWS * BM];
+    __shared__ __align__(128) bf16 sB[STAGES][B_ROWS * BN];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp / WN, wn = warp % WN;
+    const int cin = a.c1 + a.c2;
+    const int co0 = blockIdx.x * BM, ci0 = blockIdx.y * BN;
+    const int bx_n = a.w >> 3, by_n = a.h >> 2, per_img = bx_n * by_n;
+    const int nblk = a.n * per_img;
+    const int b0 = blockIdx.z * a.pix_per_split, b1 = min(nblk, b0 + a.pix_per_split);  // in blocks here
+    if (b0 >= b1) return;
+    const int nk = b1 - b0;
+
+    auto load = [&](int stage, int kb) {
+        const int blk = b0 + kb;
+        const int img = blk / per_img, rem = blk - img * per_img;
+        const int y0 = (rem / bx_n) * 4, x0 = (rem % bx_n) * 8;
+        for (int idx = tid; idx < A_ROWS * CPA; idx += NTHREADS) {
+            const int row = idx / CPA, ch = idx % CPA;
+            const int y = y0 + (row >> 3), x = x0 + (row & 7), co = co0 + ch * 8;
+            const bool ok = co < a.cout;
+            const bf16* src = ok ? a.dz + ((size_t)(img * a.h + y) * a.w + x) * a.cout + co : a.dz;
+            cp_async16(smem_u32(&sA[stage][row * BM + ((ch ^ swz<CPA>(row)) << 3)]), src, ok);
+        }
+        for (int idx = tid; idx < B_ROWS * CPB; idx += NTHREADS) {
+            const int row = idx / CPB, ch = idx % CPB;
+            const int yy = y0 - 1 + row / 10, xx = x0 - 1 + row % 10;
+            const bool ok = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
+            const bf16* src = ok ? in_addr(a.src1, a.src2, a.c1, a.c2, a.up1, a.h, a.w, img, yy, xx, ci0 + ch * 8)
+                                 : a.dz;
+            cp_async16(smem_u32(&sB[stage][row * BN + ((ch ^ swz<CPB>(row)) << 3)]), src, ok);
+        }
+    };
+
+    float acc[9][NT][4];
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int j = 0; j < NT; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[t][j][k] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < nk) load(s, s);
+        cp_commit();
+    }
+    const int i4 = lane >> 3;
+    for (int kb = 0; kb < nk; ++kb) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        if (kb + STAGES - 1 < nk) load((kb + STAGES - 1) % STAGES, kb + STAGES - 1);
+        cp_commit();
+        const bf16* tA = sA[kb % STAGES];
+        const bf16* tB = sB[kb % STAGES];
+#pragma unroll
+        for (int kk = 0; kk < 32; kk += 16) {
+            // A: 16 pixels x 16 co (transposed load of the [pixel][co] tile)
+            uint32_t af[4];
+            {
+                const int krow = kk + (lane & 7) + ((i4 >> 1) << 3);
+                const int ch = (wm * 16 + ((i4 & 1) << 3)) >> 3;
+                ldsm_x4_t(smem_u32(tA + krow * BM + ((ch ^ swz<CPA>(krow)) << 3)), af[0], af[1], af[2], af[3]);
+            }
+            // this lane's pixel of the k16 chunk: block row and column
+            const int q = kk + (lane & 7) + ((i4 & 1) << 3);
+            const int qr = q >> 3, qc = q & 7;
+            const int chb = (wn * 16 + ((i4 >> 1) << 3)) >> 3;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                const int hrow = (qr + t / 3) * 10 + (qc + t % 3);
+                uint32_t bfr[NT][2];
+                ldsm_x4_t(smem_u32(tB + hrow * BN + ((chb ^ swz<CPB>(hrow)) << 3)), bfr[0][0], bfr[0][1], bfr[1][0],
+                          bfr[1][1]);
+#pragma unroll
+                for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[t][nt], af, bfr[nt]);
+            }
+        }
+    }
+    cp_wait<0>();
+
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int ci = ci0 + wn * 16 + nt * 8 + 2 * (lane & 3);
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int co = co0 + wm * 16 + (lane >> 2) + 8 * hh;
+                if (co >= a.cout) continue;
+                float* d = a.dw + ((size_t)co * 9 + t) * cin + ci;
+                atomicAdd(d, acc[t][nt][2 * hh]);
+                atomicAdd(d + 1, acc[t][nt][2 * hh + 1]);
+            }
+        }
+}
+
+template <int BM, int BN>
+cudaError_t launch_wgrad9(WgradArgs a, cudaStream_t st) {
+    const int cin = a.c1 + a.c2;
+    const int nblk = a.n * (a.h / 4) * (a.w / 8);
+    const int tiles = ((a.cout + BM - 1) / BM) * (cin / BN);
+    // about two CTAs per SM: long K ranges keep the atomics few
+    int splits = (152 * 2 + tiles - 1) / tiles;
+    if (splits > nblk) splits = nblk;
+    if (splits < 1) splits = 1;
+    const int bps = (nblk + splits - 1) / splits;
+    a.pix_per_split = bps;  // blocks per split
+    splits = (nblk + bps - 1) / bps;
+    dim3 grid((a.cout + BM - 1) / BM, cin / BN, splits);
+    k_conv3x3_wgrad9<BM, BN><<<grid, 32 * (BM / 16) * (BN / 16), 0, st>>>(a);
+    return cudaGetLastError();
+}
 }  // namespace
 
 cudaError_t conv3x3(const ConvArgs& a, cudaStream_t st) {
@@ -676,12 +806,25 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t st) {
     }
 }
 
+// VR_DN_WGRAD=per_tap forces the one-tap-per-CTA kernel (for tests and measurements)
+static bool wgrad_per_tap() {
+    static const bool v = [] {
+        const char* e = std::getenv("VR_DN_WGRAD");
+        return e && std::strcmp(e, "per_tap") == 0;
+    }();
+    return v;
+}
+
 cudaError_t conv3x3_wgrad(const WgradArgs& a, cudaStream_t st) {
     const int cin = a.c1 + a.c2;
     if (a.n <= 0 || a.h <= 0 || a.w <= 0 || cin % 16 || a.c1 % 8 || a.c2 % 8 || a.cout % 16 ||
         (a.up1 && ((a.h | a.w) & 1)))
         return cudaErrorInvalidValue;
     const bool bn32 = cin % 32 == 0;
+    if (a.h % 4 == 0 && a.w % 8 == 0 && !wgrad_per_tap()) {
+        if (a.cout >= 64) return bn32 ? launch_wgrad9<64, 32>(a, st) : launch_wgrad9<64, 16>(a, st);
+        return bn32 ? launch_wgrad9<32, 32>(a, st) : launch_wgrad9<32, 16>(a, st);
+    }
     if (a.cout >= 64) return bn32 ? launch_wgrad<64, 32>(a, st) : launch_wgrad<64, 16>(a, st);
     return bn32 ? launch_wgrad<32, 32>(a, st) : launch_wgrad<32, 16>(a, st);
 }
