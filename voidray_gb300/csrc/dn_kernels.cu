@@ -10,6 +10,7 @@
 //                    atomics into the gradient buffer
 //   glue             2x2 average pool, skip / upsample backward, bias grad,
 //                    pre/post-processing, L1 loss, Adam, weight cast + flip
+#include <algorithm>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -832,7 +833,10 @@ cudaError_t conv3x3_wgrad(const WgradArgs& a, cudaStream_t st) {
 cudaError_t bias_grad(const bf16* dz, int p, int c, float* db, cudaStream_t st) {
     if (c <= 0 || c > 256 || (256 % c) != 0 || c % 8 || (reinterpret_cast<uintptr_t>(dz) & 15))
         return cudaErrorInvalidValue;
-    const int rows = 1024;
+    // about eight blocks per SM, each a multiple of the pixels one step covers
+    const int slots = 256 / (c / 8);
+    const int target = (p + 152 * 8 - 1) / (152 * 8);
+    const int rows = std::max(slots, (target + slots - 1) / slots * slots);
     k_bias_grad<<<(p + rows - 1) / rows, 256, 0, st>>>(dz, p, c, rows, db);
     return cudaGetLastError();
 }
