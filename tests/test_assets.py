@@ -275,7 +275,7 @@ def test_files_reach_textures_and_environments(tmp_path):
     (tmp_path / "t.png").write_bytes(encode_png(rgb, 8, 2))
     (tmp_path / "e.exr").write_bytes(encode_exr({c: np.full((3, 4), i + 1.0, np.float32) for i, c in enumerate("RGB")},
                                                 {c: 2 for c in "RGB"}, 3))
-    (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff")
+    (tmp_path / "x.gif").write_bytes(b"GIF89a\x01\x00\x01\x00")
     t = ImageTexture.from_file(str(tmp_path / "t.png"), SampleType.Nearest)
     assert np.array_equal(t.image, rgb.astype(np.float32) / np.float32(255))
     s = Scene()
@@ -283,7 +283,7 @@ def test_files_reach_textures_and_environments(tmp_path):
     env = Environments.hdri(str(tmp_path / "e.exr"))
     assert env.image.shape == (3, 4, 3) and env.image[0, 0].tolist() == [1.0, 2.0, 3.0]
     with pytest.raises(VoidrayError, match="not decoded here"):
-        A.load_image_rgb32f(str(tmp_path / "x.jpg"))
+        A.load_image_rgb32f(str(tmp_path / "x.gif"))
 
 
 REF_PNGS = [os.path.join(os.environ.get("VOIDRAY_REFERENCE", "/root/reference"), "assets", f)

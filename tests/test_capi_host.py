@@ -24,7 +24,7 @@ def declared():
 def test_exports_every_declared_symbol(native):
     lib = native.lib()
     names = declared()
-    assert len(HEADERS) == 2 and len(names) >= 25
+    assert len(HEADERS) == 3 and len(names) >= 25
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(native.EXPORTED)

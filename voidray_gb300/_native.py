@@ -112,6 +112,11 @@ class vr_stats_job(C.Structure):
                 ("tile_offset", C.c_uint64)]
 
 
+class vr_image_info(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("components", C.c_uint32), ("format", C.c_uint32),
+                ("progressive", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 STATS_TILE = 16
 STATS_MAX_JOBS = 128
 
@@ -132,7 +137,7 @@ STAGES = ["raygen", "extend", "shade", "shadow", "accumulate"]
 INSTR_STAGE_TIMES = 1
 INSTR_WORK = 2
 
-# every function declared in include/voidray_gpu.h: (name, restype, argtypes)
+# every function declared in include/*.h: (name, restype, argtypes)
 P = C.c_void_p
 _SIGS = [
     ("vr_scene_create", C.c_int, [P, P]),
@@ -196,6 +201,9 @@ _SIGS = [
       C.c_int32, P]),
     ("vr_dn_conv3x3_wgrad_device", C.c_int,
      [P, P, C.c_uint32, C.c_int32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P]),
+    # include/voidray_image.h
+    ("vr_image_info_get", C.c_int, [P, C.c_size_t, P]),
+    ("vr_image_decode_rgb8", C.c_int, [P, C.c_size_t, P, C.c_size_t]),
 ]
 EXPORTED = [name for name, _, _ in _SIGS]
 

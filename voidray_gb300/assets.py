@@ -20,14 +20,20 @@ reaches the renderer.
   `HDRIEnvironment::new` (voidray_common/src/environments.rs:42-55) call it
   (image 0.24): row 0 at the top, RGB f32, alpha dropped, grey replicated,
   integer samples divided by their maximum (255 or 65535).  Formats read
-  here: PNG (every colour type and bit depth, Adam7 interlacing) and
-  OpenEXR scanline files with NONE, RLE, ZIPS or ZIP compression and HALF,
-  FLOAT or UINT channels.  JPEG and TIFF decoding and the other EXR
-  compressions are not restated; decode those elsewhere and pass float RGB
-  arrays (`Scene.add_texture`, `Environments.hdri`).
+  here: PNG (every colour type and bit depth, Adam7 interlacing); OpenEXR
+  scanline files with NONE, RLE, ZIPS or ZIP compression and HALF, FLOAT or
+  UINT channels; JPEG (baseline, extended and progressive Huffman DCT, 8-bit;
+  decoded by the native library, `include/voidray_image.h`); TIFF (the first
+  image of the file: strips or tiles, chunky or planar, no / LZW / Deflate /
+  PackBits compression, horizontal and floating-point predictors, grey,
+  palette and RGB(A), 1-32-bit integer and 16/32/64-bit float samples).
+  JPEG-in-TIFF, CMYK and YCbCr TIFF and the other EXR compressions are not
+  restated; decode those elsewhere and pass float RGB arrays
+  (`Scene.add_texture`, `Environments.hdri`).
 """
 from __future__ import annotations
 
+import ctypes
 import os
 import struct
 import zlib
@@ -336,6 +342,266 @@ def decode_exr(data: bytes) -> np.ndarray:
     return np.ascontiguousarray(np.stack([planes["R"], planes["G"], planes["B"]], axis=-1))
 
 
+# ------------------------------------------------------------------- JPEG ---
+_JPEG_MAGIC = b"\xff\xd8\xff"
+
+
+def jpeg_info(data: bytes) -> dict:
+    """Frame-header facts of a JPEG stream (no pixels decoded)."""
+    from . import _native as N
+
+    buf = np.frombuffer(data, np.uint8)
+    info = N.vr_image_info()
+    N.check(N.lib().vr_image_info_get(buf.ctypes.data, buf.size, ctypes.byref(info)))
+    return {"width": info.width, "height": info.height, "components": info.components,
+            "progressive": bool(info.progressive)}
+
+
+def decode_jpeg_rgb8(data: bytes) -> np.ndarray:
+    """Decodes a JPEG stream with the native decoder: uint8 RGB [height, width, 3]."""
+    from . import _native as N
+
+    info = jpeg_info(data)
+    buf = np.frombuffer(data, np.uint8)
+    out = np.empty((info["height"], info["width"], 3), np.uint8)
+    N.check(N.lib().vr_image_decode_rgb8(buf.ctypes.data, buf.size, out.ctypes.data, out.nbytes))
+    return out
+
+
+def decode_jpeg(data: bytes) -> np.ndarray:
+    return decode_jpeg_rgb8(data).astype(np.float32) / np.float32(255.0)
+
+
+# ------------------------------------------------------------------- TIFF ---
+_TIFF_TYPES = {1: "B", 2: "c", 3: "H", 4: "I", 5: "II", 6: "b", 7: "B", 8: "h", 9: "i", 10: "ii", 11: "f",
+               12: "d", 16: "Q", 17: "q", 18: "Q"}
+_TIFF_SIZES = {1: 1, 2: 1, 3: 2, 4: 4, 5: 8, 6: 1, 7: 1, 8: 2, 9: 4, 10: 8, 11: 4, 12: 8, 16: 8, 17: 8, 18: 8}
+
+
+def _tiff_ifd(data: bytes, bo: str):
+    """Tags of the first image file directory: {tag: tuple of values}."""
+    if len(data) < 8:
+        raise VoidrayError(1, "TIFF: truncated header")
+    magic, off = struct.unpack(bo + "HI", data[2:8])
+    if magic == 43:
+        raise VoidrayError(2, "TIFF: BigTIFF is not decoded here")
+    if magic != 42 or off + 2 > len(data):
+        raise VoidrayError(1, "TIFF: bad header")
+    (n,) = struct.unpack(bo + "H", data[off:off + 2])
+    if off + 2 + 12 * n > len(data):
+        raise VoidrayError(1, "TIFF: truncated directory")
+    tags = {}
+    for i in range(n):
+        tag, typ, cnt = struct.unpack(bo + "HHI", data[off + 2 + 12 * i:off + 10 + 12 * i])
+        if typ not in _TIFF_SIZES:
+            continue
+        size = _TIFF_SIZES[typ] * cnt
+        if size <= 4:
+            raw = data[off + 10 + 12 * i:off + 10 + 12 * i + size]
+        else:
+            (voff,) = struct.unpack(bo + "I", data[off + 10 + 12 * i:off + 14 + 12 * i])
+            raw = data[voff:voff + size]
+            if len(raw) != size:
+                raise VoidrayError(1, f"TIFF: tag {tag} points past the end of the file")
+        if typ == 2:
+            tags[tag] = (raw.split(b"\0")[0].decode("latin-1"),)
+            continue
+        fmt = _TIFF_TYPES[typ]
+        vals = struct.unpack(bo + fmt * cnt, raw)
+        if typ in (5, 10):
+            vals = tuple(vals[2 * k] / vals[2 * k + 1] if vals[2 * k + 1] else 0.0 for k in range(cnt))
+        tags[tag] = vals
+    return tags
+
+
+def _tiff_lzw_decode(src: bytes) -> bytes:
+    """TIFF 6.0 LZW: MSB-first codes of 9-12 bits, Clear = 256, EOI = 257, the
+    code width growing one code early (at 511, 1023 and 2047 table entries)."""
+    out = bytearray()
+    table = [bytes((i,)) for i in range(256)] + [b"", b""]
+    total = len(src) * 8
+    padded = src + b"\0\0\0"
+    nbits, pos, prev = 9, 0, b""
+    while pos + nbits <= total:
+        b = pos >> 3
+        word = (padded[b] << 16) | (padded[b + 1] << 8) | padded[b + 2]
+        code = (word >> (24 - (pos & 7) - nbits)) & ((1 << nbits) - 1)
+        pos += nbits
+        if code == 257:
+            break
+        if code == 256:
+            del table[258:]
+            nbits, prev = 9, b""
+            continue
+        if code < len(table) and code < 256 or code >= 258 and code < len(table):
+            entry = table[code]
+            if prev:
+                table.append(prev + entry[:1])
+        elif code == len(table) and prev:
+            entry = prev + prev[:1]
+            table.append(entry)
+        else:
+            raise VoidrayError(1, f"TIFF: corrupt LZW data (code {code} with {len(table)} table entries)")
+        out += entry
+        prev = entry
+        if len(table) >= (1 << nbits) - 1 and nbits < 12:
+            nbits += 1
+    return bytes(out)
+
+
+def _tiff_packbits_decode(src: bytes, size: int) -> bytes:
+    out = bytearray()
+    i, n = 0, len(src)
+    while i < n and len(out) < size:
+        h = src[i]
+        i += 1
+        if h < 128:
+            out += src[i:i + h + 1]
+            i += h + 1
+        elif h > 128:
+            if i >= n:
+                break
+            out += bytes((src[i],)) * (257 - h)
+            i += 1
+    return bytes(out)
+
+
+def _tiff_chunk(raw: bytes, compression: int, size: int) -> bytes:
+    if compression == 1:
+        out = raw
+    elif compression == 5:
+        out = _tiff_lzw_decode(raw)
+    elif compression in (8, 32946):
+        try:
+            out = zlib.decompress(raw)
+        except zlib.error as e:
+            raise VoidrayError(1, f"TIFF: corrupt Deflate data ({e})") from None
+    elif compression == 32773:
+        out = _tiff_packbits_decode(raw, size)
+    else:
+        raise VoidrayError(2, f"TIFF: compression {compression} is not decoded here")
+    if len(out) < size:
+        raise VoidrayError(1, f"TIFF: chunk holds {len(out)} bytes, {size} expected")
+    return out[:size]
+
+
+def _tiff_samples(buf: bytes, rows: int, cols: int, spp: int, bps: int, fmt: int, bo: str,
+                  predictor: int) -> np.ndarray:
+    """One decompressed strip or tile -> samples [rows, cols, spp] (integers or floats)."""
+    row_bytes = (cols * spp * bps + 7) // 8
+    a = np.frombuffer(buf, np.uint8, rows * row_bytes).reshape(rows, row_bytes)
+    if predictor == 3:  # floating-point predictor: byte differences, then byte planes MSB first
+        if fmt != 3 or bps not in (16, 32, 64):
+            raise VoidrayError(1, "TIFF: floating-point predictor on non-float samples")
+        a = np.cumsum(a.reshape(rows, row_bytes), axis=1, dtype=np.uint8)
+        nb = bps // 8
+        planes = a.reshape(rows, nb, cols * spp).transpose(0, 2, 1)
+        return np.ascontiguousarray(planes).view(np.dtype(f">f{nb}")).reshape(rows, cols, spp)
+    if bps < 8:
+        bits = np.unpackbits(a, axis=1)[:, :cols * spp * bps].reshape(rows, cols * spp, bps)
+        weights = (1 << np.arange(bps - 1, -1, -1)).astype(np.uint32)
+        v = (bits.astype(np.uint32) * weights).sum(-1).reshape(rows, cols, spp)
+        if predictor == 2:
+            v = np.cumsum(v, axis=1) % (1 << bps)
+        return v.astype(np.uint32)
+    if bps % 8:
+        raise VoidrayError(2, f"TIFF: {bps}-bit samples are not decoded here")
+    kind = {1: "u", 2: "i", 3: "f"}.get(fmt)
+    if kind is None or (kind == "f" and bps not in (16, 32, 64)) or (kind != "f" and bps > 32):
+        raise VoidrayError(2, f"TIFF: sample format {fmt} with {bps} bits is not decoded here")
+    dt = np.dtype(f"{bo}{kind}{bps // 8}")
+    v = a.view(dt).reshape(rows, cols, spp)
+    if predictor == 2:
+        if kind == "f":
+            raise VoidrayError(1, "TIFF: horizontal predictor on float samples")
+        v = np.cumsum(v, axis=1, dtype=dt.newbyteorder("="))
+    return v
+
+
+def decode_tiff(data: bytes) -> np.ndarray:
+    bo = {b"II": "<", b"MM": ">"}.get(data[:2])
+    if bo is None:
+        raise VoidrayError(1, "TIFF: bad byte-order mark")
+    t = _tiff_ifd(data, bo)
+
+    def one(tag, default=None):
+        v = t.get(tag)
+        if v is None:
+            if default is None:
+                raise VoidrayError(1, f"TIFF: required tag {tag} missing")
+            return default
+        return v[0]
+
+    width, height = int(one(256)), int(one(257))
+    spp = int(one(277, 1))
+    bps_all = t.get(258, (1,) * spp)
+    if len(set(bps_all)) != 1:
+        raise VoidrayError(2, f"TIFF: mixed bit depths {bps_all}")
+    bps = int(bps_all[0])
+    fmt = int(t.get(339, (1,))[0])
+    compression = int(one(259, 1))
+    photometric = int(one(262))
+    planar = int(one(284, 1))
+    predictor = int(one(317, 1))
+    if width <= 0 or height <= 0 or width * height > 1 << 28:
+        raise VoidrayError(2 if width * height > 1 << 28 else 1, f"TIFF: image size {width}x{height}")
+    if photometric not in (0, 1, 2, 3):
+        raise VoidrayError(2, f"TIFF: photometric interpretation {photometric} is not decoded here")
+    if photometric == 2 and spp < 3 or photometric != 2 and spp < 1:
+        raise VoidrayError(1, f"TIFF: {spp} samples per pixel for photometric {photometric}")
+    if predictor not in (1, 2, 3):
+        raise VoidrayError(2, f"TIFF: predictor {predictor}")
+    planes = spp if planar == 2 else 1
+    chunk_spp = 1 if planar == 2 else spp
+    if 322 in t:
+        cw, chh = int(one(322)), int(one(323))
+        offsets, counts = t.get(324), t.get(325)
+        across, down = -(-width // cw), -(-height // chh)
+        layout = [(p, ty * chh, tx * cw, chh, cw) for p in range(planes) for ty in range(down) for tx in range(across)]
+    else:
+        rps = min(int(one(278, height)), height)
+        offsets, counts = t.get(273), t.get(279)
+        per_plane = -(-height // rps)
+        layout = [(p, s * rps, 0, min(rps, height - s * rps), width) for p in range(planes) for s in range(per_plane)]
+    if offsets is None or counts is None or len(offsets) < len(layout) or len(counts) < len(layout):
+        raise VoidrayError(1, "TIFF: chunk offsets or byte counts missing")
+    img = None
+    for k, (p, y0, x0, rows, cols) in enumerate(layout):
+        raw = data[offsets[k]:offsets[k] + counts[k]]
+        if len(raw) != counts[k]:
+            raise VoidrayError(1, "TIFF: chunk points past the end of the file")
+        size = rows * ((cols * chunk_spp * bps + 7) // 8)
+        v = _tiff_samples(_tiff_chunk(raw, compression, size), rows, cols, chunk_spp, bps, fmt, bo, predictor)
+        if img is None:
+            img = np.zeros((height, width, spp), v.dtype.newbyteorder("="))
+        h, w = min(rows, height - y0), min(cols, width - x0)
+        img[y0:y0 + h, x0:x0 + w, p:p + chunk_spp] = v[:h, :w]
+    if photometric == 3:
+        cmap = t.get(320)
+        if cmap is None or len(cmap) != 3 * (1 << bps):
+            raise VoidrayError(1, "TIFF: palette image without a colour map of 3 * 2^bits entries")
+        cm = np.asarray(cmap, np.float32).reshape(3, -1).T / np.float32(65535.0)
+        return np.ascontiguousarray(cm[img[..., 0].astype(np.int64)])
+    if img.dtype.kind == "f":
+        f = img.astype(np.float32)
+        if photometric == 0:
+            f = np.float32(1.0) - f
+    else:
+        if img.dtype.kind == "i":
+            raise VoidrayError(2, "TIFF: signed integer samples are not decoded here")
+        if bps < 8:  # low bit depths expand to 8 bits, as for PNG
+            img = img * (255 // ((1 << bps) - 1))
+            maxv = 255
+        else:
+            maxv = (1 << bps) - 1
+        if photometric == 0:
+            img = maxv - img
+        f = img.astype(np.float32) / np.float32(maxv)
+    if photometric in (0, 1):
+        return np.ascontiguousarray(np.repeat(f[..., :1], 3, axis=-1))
+    return np.ascontiguousarray(f[..., :3])
+
+
 def load_image_rgb32f(path: str) -> np.ndarray:
     """Decodes an image file to float32 RGB [height, width, 3], row 0 at the top."""
     with open(path, "rb") as f:
@@ -344,6 +610,10 @@ def load_image_rgb32f(path: str) -> np.ndarray:
         return decode_png(data)
     if len(data) >= 4 and struct.unpack("<i", data[:4])[0] == _EXR_MAGIC:
         return decode_exr(data)
+    if data[:3] == _JPEG_MAGIC:
+        return decode_jpeg(data)
+    if data[:4] in (b"II*\0", b"MM\0*", b"II+\0", b"MM\0+"):
+        return decode_tiff(data)
     ext = os.path.splitext(path)[1].lower()
     raise VoidrayError(2, f"image format of {os.path.basename(path)!r} ({ext or 'unknown'}) is not "
                           "decoded here: pass float RGB arrays instead")

@@ -20,7 +20,10 @@ BUILD = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libvoidray_gb300.so"
 
-SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "vr_serve.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu"]
+SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "vr_serve.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu",
+           "vr_image.cpp"]
+# host-only translation units: compiled as plain C++ (no device code)
+HOST_ONLY = {"vr_image.cpp"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,6 +39,8 @@ def _flags(src: str) -> list[str]:
               "-I", str(CSRC), "-I", str(PKG.parent / "include")]
     # tuning knobs for sweeps, e.g. VR_NVCC_EXTRA="-DVR_TRACE_MINB=12 -DVR_DYN_FETCH=16" (rebuild with --force)
     common += os.environ.get("VR_NVCC_EXTRA", "").split()
+    if src in HOST_ONLY:
+        return common + ["-x", "c++"]
     if src.endswith(".cu"):
         return ARCH + common + ["-fmad=false", "-Xptxas", "-v" if os.environ.get("VR_PTXAS_VERBOSE") else "-O3"]
     return common + ["-x", "cu"] + ARCH + ["-fmad=false"]

@@ -572,9 +572,15 @@ vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
         *info = vr_scene_info{};
         info->num_triangles = hs.num_prims;
         info->num_nodes = hs.nodes.size() / 4;
-        info->device_bytes = hs.nodes.size() * 16 + hs.tris.size() * 16 + hs.shade.size() * 16 + hs.uvs.size() * 8 +
-                             hs.env_img.size() * 4 +
-                             (hs.tables.marginal.size() + hs.tables.conditional.size() + hs.tables.cell.size()) * 4;
+        // every array vr_scene_create uploads (textures and materials included)
+        info->device_bytes = hs.nodes.size() * sizeof(float4) + hs.tris.size() * sizeof(float4) +
+                             hs.shade.size() * sizeof(float4) + hs.uvs.size() * sizeof(float2) +
+                             hs.materials.size() * sizeof(hs.materials[0]) + hs.analytic.size() * sizeof(float4) +
+                             hs.tex_info.size() * sizeof(int4) + hs.texels.size() * sizeof(float) +
+                             hs.env_img.size() * sizeof(float) +
+                             (hs.has_tables ? (hs.tables.marginal.size() + hs.tables.conditional.size() +
+                                               hs.tables.cell.size()) * sizeof(float)
+                                            : 0);
         info->max_depth = hs.max_depth;
         info->max_leaf = hs.max_leaf;
         info->sah_cost = hs.sah_cost;

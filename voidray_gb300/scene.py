@@ -362,7 +362,7 @@ class Environments:
     @staticmethod
     def hdri(path: str, importance_sample: bool = True) -> Environment:
         """Environments::hdri (environments.rs:14-16, 42-55): decodes the file
-        (EXR or PNG) to RGB f32."""
+        (EXR, PNG, JPEG or TIFF) to RGB f32."""
         from .assets import load_image_rgb32f
 
         return Environments.hdri_image(load_image_rgb32f(path), importance_sample)
@@ -475,7 +475,7 @@ class Scene:
         return self.add_mesh(Mesh.from_file(path))
 
     def add_image_texture(self, path: str, sample_type: "SampleType" = None) -> int:
-        """scene.rs:154-160: decodes the file (PNG or EXR) to RGB f32."""
+        """scene.rs:154-160: decodes the file (PNG, EXR, JPEG or TIFF) to RGB f32."""
         return self.add_texture(ImageTexture.from_file(path, SampleType.Bilinear if sample_type is None
                                                        else sample_type))
 

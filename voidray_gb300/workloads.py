@@ -15,10 +15,13 @@
                        per 64-triangle patch uniformly among Lambertian (albedo
                        U(0.1,0.9)), metal (fuzz U(0,0.5)) and dielectric (1.5);
                        2048x1024 sky-gradient + sun (sigma 0.5 deg, peak 5e4) HDRI.
+  mushroom_scene()     the reference's mushroom demo from its own asset folder
+                       (OBJ meshes, JPEG textures), when that folder is given.
 """
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -351,6 +354,40 @@ def textured_scene(seed: int = 4):
     st = RenderSettings(total_samples=8, max_bounces=6, rr_depth=0, estimator=Estimator.REFERENCE,
                         firefly_clamp=float("inf"))
     return s, st
+
+
+def mushroom_scene(assets_dir: str, hdri_size=(512, 256)):
+    """The reference's mushroom demo (voidray_app/src/examples/mushroom.rs:3-37)
+    built from its asset folder: mushroom.obj and mossy_ground.obj with their
+    albedo JPEGs and normal maps, the depth-of-field camera, ACES with gamma 1
+    and exposure 1, 1000x1000.  Files the folder lacks are replaced: a missing
+    normal-map JPEG by the same material without a normal map
+    (simple.rs:29-34), a missing studio.exr by the synthetic sky.  Returns
+    (scene, Settings, (width, height))."""
+    from .scene import ColorManagementSettings, ImageTexture, SampleType, Settings, Tonemap
+
+    def path(name):
+        return os.path.join(assets_dir, name)
+
+    s = Scene()
+    for stem in ("mushroom", "mossy_ground"):
+        albedo = s.add_image_texture(path(f"{stem}_albedo.jpg"), SampleType.Bilinear)
+        if os.path.exists(path(f"{stem}_normal.jpg")):
+            normal = s.add_texture(ImageTexture.from_file(path(f"{stem}_normal.jpg"), SampleType.Bilinear))
+            mtl = s.add_material(Materials.lambertian_texture(albedo, normal))
+        else:
+            mtl = s.add_material(Materials.lambertian_texture_no_normal(albedo))
+        s.add_object(mtl, s.add_mesh_from_file(path(f"{stem}.obj")))
+    s.camera = Camera(eye=np.array([0.2, 2.8, -10.5], f32), direction=np.array([0.0, -0.2, 1.0], f32),
+                      up=np.array([0.0, 1.0, 0.0], f32), fov=f32(0.17),
+                      dof=(0.17, np.array([0.06, 2.14, 0.18], f32)))
+    if os.path.exists(path("studio.exr")):
+        s.environment = Environments.hdri(path("studio.exr"))
+    else:
+        s.environment = Environments.hdri_image(sky_hdri(*hdri_size))
+    st = Settings()
+    st.color_management = ColorManagementSettings(tonemap=Tonemap.ACES, gamma=1.0, exposure=1.0)
+    return s, st, (1000, 1000)
 
 
 def mix_scene(hdri: bool = False, seed: int = 5):
