@@ -302,3 +302,42 @@ def test_png_reads_the_reference_assets():
         q = img * np.float32(255)
         assert np.all(np.abs(q - np.round(q)) < 1e-4) and img.min() >= 0 and img.max() <= 1
     assert shapes == [(2, 2, 3), (256, 256, 3)]
+
+
+def _fix_png_crcs(b: bytes) -> bytes:
+    """Recomputes every chunk CRC so that a mutation reaches the decoder's logic."""
+    b = bytearray(b)
+    pos = 8
+    while pos + 8 <= len(b):
+        (length,) = struct.unpack(">I", b[pos:pos + 4])
+        if pos + 12 + length > len(b):
+            break
+        b[pos + 8 + length:pos + 12 + length] = struct.pack(">I", zlib.crc32(bytes(b[pos + 4:pos + 8 + length])))
+        pos += 12 + length
+    return bytes(b)
+
+
+def test_corrupt_files_raise_voidray_errors_only():
+    """Mutated PNG / EXR / OBJ inputs either decode or raise VoidrayError with
+    VR_ERR_INVALID or VR_ERR_UNSUPPORTED: no zlib, struct, index or memory
+    errors escape, and no header asks for an unbounded allocation."""
+    rng = np.random.default_rng(9)
+    pngs = [encode_png(rng.integers(0, 256, (7, 9, 3)), 8, 2),
+            encode_png(rng.integers(0, 4, (5, 11, 1)), 2, 0, interlace=True),
+            encode_png(rng.integers(0, 65536, (6, 6, 4)), 16, 6),
+            encode_png(rng.integers(0, 16, (8, 8, 1)), 4, 3, palette=rng.integers(0, 256, (16, 3)))]
+    exrs = [encode_exr({c: rng.normal(0, 1, (6, 5)).astype(np.float32) for c in "RGB"}, {c: 2 for c in "RGB"}, comp)
+            for comp in (0, 1, 2, 3)]
+    obj = b"v 0 0 0\nv 1 0 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 0 1\nvn 0 0 1\nf 1/1/1 2/2/1 3/3/1\nf -1/-1/-1 -2/-2/-1 -3/-3/-1\n"
+    cases = [(pngs, lambda b: A.decode_png(_fix_png_crcs(b)), 8, None),
+             (exrs, A.decode_exr, 8, None),
+             ([obj], lambda b: A.parse_obj(b.decode("latin-1")), 0, list(b"0123456789-/ \nvftn.e"))]
+    for seeds, decode, start, alphabet in cases:
+        for it in range(1200):
+            b = bytearray(seeds[it % len(seeds)])
+            for _ in range(rng.integers(1, 5)):
+                b[int(rng.integers(start, len(b)))] = int(rng.choice(alphabet) if alphabet else rng.integers(0, 256))
+            try:
+                decode(bytes(b))
+            except VoidrayError as e:
+                assert e.status in (1, 2)

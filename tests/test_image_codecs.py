@@ -891,6 +891,22 @@ def test_tiff_errors():
         A.decode_tiff(write_tiff(img, compression=5)[:12] + b"\xff" * 40)
 
 
+def test_tiff_corrupt_files_raise_voidray_errors_only():
+    rng = np.random.default_rng(6)
+    img = rng.integers(0, 256, (20, 24, 3), dtype=np.uint8)
+    seeds = [write_tiff(img, compression=c, predictor=p, rows_per_strip=5) for c in (1, 5, 8, 32773) for p in (1, 2)]
+    seeds.append(write_tiff(rng.integers(0, 65536, (13, 17, 4), dtype=np.uint16), ">", 5, 2, tile=(16, 16), planar=2))
+    seeds.append(write_tiff(rng.normal(0, 1, (9, 10, 3)).astype(np.float32), ">", 8, 3, fmt=3))
+    for it in range(1500):
+        b = bytearray(seeds[it % len(seeds)])
+        for _ in range(rng.integers(1, 6)):
+            b[int(rng.integers(4, len(b)))] = int(rng.integers(0, 256))
+        try:
+            A.decode_tiff(bytes(b))
+        except VoidrayError as e:
+            assert e.status in (1, 2)
+
+
 @pytest.mark.skipif(not (ASSETS / "wood_albedo.tif").exists(), reason="the reference's assets are not here")
 def test_tiff_reference_assets():
     alb = A.load_image_rgb32f(str(ASSETS / "wood_albedo.tif"))

@@ -34,6 +34,7 @@ reaches the renderer.
 from __future__ import annotations
 
 import ctypes
+import functools
 import os
 import struct
 import zlib
@@ -41,6 +42,23 @@ import zlib
 import numpy as np
 
 from ._native import VoidrayError
+
+
+def _corrupt_is_invalid(fmt: str):
+    """Decoders read untrusted bytes: whatever a corrupt file makes the parsing
+    raise (short buffers, bad zlib streams, out-of-range indices, undecodable
+    names) is reported as VR_ERR_INVALID, like the native decoder's errors."""
+    def wrap(fn):
+        @functools.wraps(fn)
+        def inner(*args, **kwargs):
+            try:
+                return fn(*args, **kwargs)
+            except VoidrayError:
+                raise
+            except (zlib.error, struct.error, IndexError, KeyError, ValueError, TypeError, OverflowError) as e:
+                raise VoidrayError(1, f"{fmt}: corrupt data ({type(e).__name__}: {e})") from None
+        return inner
+    return wrap
 
 
 # -------------------------------------------------------------------- OBJ ---
@@ -55,6 +73,7 @@ def _obj_index(tok: str, count: int, what: str, line: int) -> int:
     return j
 
 
+@_corrupt_is_invalid("OBJ")
 def parse_obj(text: str):
     """Returns (positions f32 [V,3], uvs f32 [V,2], normals f32 [V,3],
     indices u32 [F,3]) with the obj-rs TexturedVertex numbering."""
@@ -118,6 +137,9 @@ def load_obj(path: str):
 
 
 # -------------------------------------------------------------------- PNG ---
+# decoders refuse images above this many pixels (the native JPEG decoder's limit too)
+MAX_IMAGE_PIXELS = 1 << 28
+
 _PNG_MAGIC = b"\x89PNG\r\n\x1a\n"
 _ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
 _PNG_CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
@@ -177,6 +199,7 @@ def _png_samples(rows: np.ndarray, width: int, depth: int, channels: int) -> np.
     return (bits.astype(np.uint16) * weights).sum(-1).astype(np.uint16).reshape(h, width, channels)
 
 
+@_corrupt_is_invalid("PNG")
 def decode_png(data: bytes) -> np.ndarray:
     if data[:8] != _PNG_MAGIC:
         raise VoidrayError(1, "PNG: bad signature")
@@ -206,6 +229,10 @@ def decode_png(data: bytes) -> np.ndarray:
         raise VoidrayError(1, f"PNG: unsupported header {ihdr}")
     if ctype == 3 and plte is None:
         raise VoidrayError(1, "PNG: palette image without PLTE")
+    if width == 0 or height == 0:
+        raise VoidrayError(1, "PNG: zero width or height")
+    if width * height > MAX_IMAGE_PIXELS:
+        raise VoidrayError(2, f"PNG: {width}x{height} is above {MAX_IMAGE_PIXELS} pixels")
     ch = _PNG_CHANNELS[ctype]
     raw = zlib.decompress(b"".join(idat))
     bpp = max(1, ch * depth // 8)
@@ -299,6 +326,7 @@ def _exr_unpredict(t: bytes) -> bytes:
     return out.tobytes()
 
 
+@_corrupt_is_invalid("EXR")
 def decode_exr(data: bytes) -> np.ndarray:
     attrs, pos = _exr_header(data)
     for req in ("channels", "compression", "dataWindow"):
@@ -312,6 +340,8 @@ def decode_exr(data: bytes) -> np.ndarray:
     w, h = xmax - xmin + 1, ymax - ymin + 1
     if w <= 0 or h <= 0:
         raise VoidrayError(1, "EXR: empty data window")
+    if w * h > MAX_IMAGE_PIXELS:
+        raise VoidrayError(2, f"EXR: {w}x{h} is above {MAX_IMAGE_PIXELS} pixels")
     lines = _EXR_LINES[comp]
     nchunks = (h + lines - 1) // lines
     offsets = struct.unpack(f"<{nchunks}Q", data[pos:pos + 8 * nchunks])
@@ -518,15 +548,22 @@ def _tiff_samples(buf: bytes, rows: int, cols: int, spp: int, bps: int, fmt: int
     return v
 
 
+@_corrupt_is_invalid("TIFF")
 def decode_tiff(data: bytes) -> np.ndarray:
     bo = {b"II": "<", b"MM": ">"}.get(data[:2])
     if bo is None:
         raise VoidrayError(1, "TIFF: bad byte-order mark")
     t = _tiff_ifd(data, bo)
 
-    def one(tag, default=None):
+    def ints(tag):
         v = t.get(tag)
-        if v is None:
+        if v is not None and not all(isinstance(x, int) and x >= 0 for x in v):
+            raise VoidrayError(1, f"TIFF: tag {tag} holds {v[:4]!r}, not unsigned integers")
+        return v
+
+    def one(tag, default=None):
+        v = ints(tag)
+        if not v:
             if default is None:
                 raise VoidrayError(1, f"TIFF: required tag {tag} missing")
             return default
@@ -534,17 +571,19 @@ def decode_tiff(data: bytes) -> np.ndarray:
 
     width, height = int(one(256)), int(one(257))
     spp = int(one(277, 1))
-    bps_all = t.get(258, (1,) * spp)
+    bps_all = ints(258) or (1,) * spp
     if len(set(bps_all)) != 1:
         raise VoidrayError(2, f"TIFF: mixed bit depths {bps_all}")
     bps = int(bps_all[0])
-    fmt = int(t.get(339, (1,))[0])
+    fmt = int(one(339, 1))
     compression = int(one(259, 1))
     photometric = int(one(262))
     planar = int(one(284, 1))
     predictor = int(one(317, 1))
-    if width <= 0 or height <= 0 or width * height > 1 << 28:
-        raise VoidrayError(2 if width * height > 1 << 28 else 1, f"TIFF: image size {width}x{height}")
+    if width <= 0 or height <= 0 or width * height > MAX_IMAGE_PIXELS:
+        raise VoidrayError(2 if width * height > MAX_IMAGE_PIXELS else 1, f"TIFF: image size {width}x{height}")
+    if not 1 <= spp <= 16:
+        raise VoidrayError(1, f"TIFF: {spp} samples per pixel")
     if photometric not in (0, 1, 2, 3):
         raise VoidrayError(2, f"TIFF: photometric interpretation {photometric} is not decoded here")
     if photometric == 2 and spp < 3 or photometric != 2 and spp < 1:
@@ -555,12 +594,12 @@ def decode_tiff(data: bytes) -> np.ndarray:
     chunk_spp = 1 if planar == 2 else spp
     if 322 in t:
         cw, chh = int(one(322)), int(one(323))
-        offsets, counts = t.get(324), t.get(325)
+        offsets, counts = ints(324), ints(325)
         across, down = -(-width // cw), -(-height // chh)
         layout = [(p, ty * chh, tx * cw, chh, cw) for p in range(planes) for ty in range(down) for tx in range(across)]
     else:
         rps = min(int(one(278, height)), height)
-        offsets, counts = t.get(273), t.get(279)
+        offsets, counts = ints(273), ints(279)
         per_plane = -(-height // rps)
         layout = [(p, s * rps, 0, min(rps, height - s * rps), width) for p in range(planes) for s in range(per_plane)]
     if offsets is None or counts is None or len(offsets) < len(layout) or len(counts) < len(layout):
@@ -577,7 +616,7 @@ def decode_tiff(data: bytes) -> np.ndarray:
         h, w = min(rows, height - y0), min(cols, width - x0)
         img[y0:y0 + h, x0:x0 + w, p:p + chunk_spp] = v[:h, :w]
     if photometric == 3:
-        cmap = t.get(320)
+        cmap = ints(320)
         if cmap is None or len(cmap) != 3 * (1 << bps):
             raise VoidrayError(1, "TIFF: palette image without a colour map of 3 * 2^bits entries")
         cm = np.asarray(cmap, np.float32).reshape(3, -1).T / np.float32(65535.0)

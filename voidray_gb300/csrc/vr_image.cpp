@@ -68,6 +68,8 @@ struct Huffman {
             valptr[len] = k;
             mincode[len] = code;
             for (int i = 0; i < counts[len - 1]; ++i, ++k, ++code) {
+                // checked before the code is used: an over-subscribed table has no valid codes
+                if (code >= (1 << len)) fail(VR_ERR_INVALID, "JPEG: Huffman table over-subscribed");
                 if (len <= kFastBits) {
                     const int shift = kFastBits - len;
                     for (int j = 0; j < (1 << shift); ++j)
@@ -75,7 +77,6 @@ struct Huffman {
                 }
             }
             maxcode[len] = counts[len - 1] ? code - 1 : -1;
-            if (code > (1 << len)) fail(VR_ERR_INVALID, "JPEG: Huffman table over-subscribed");
             code <<= 1;
         }
         maxcode[17] = 0x7fffffff;  // sentinel: lengths above 16 are corrupt data
