@@ -175,3 +175,29 @@ def test_descriptor_limits_and_edge_cases(native):
     s = vr.Scene()
     s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(np.zeros((0, 3), np.float32), np.zeros(0, np.uint32))))
     assert s.validate().num_triangles == 0
+
+
+def test_non_finite_and_extreme_vertices(native):
+    """A NaN or infinite vertex position is rejected by name (the reference's
+    BVH sorts such boxes arbitrarily); finite coordinates up to 3e38, whose
+    extents overflow to infinity inside the SAH binning, still build a BVH
+    that passes the structural checks."""
+    rng = np.random.default_rng(4)
+    base = vr.Materials.lambertian((0.5, 0.5, 0.5))
+    for bad in (np.nan, np.inf, -np.inf):
+        s = vr.Scene()
+        pos = rng.random((30, 3)).astype(np.float32)
+        pos[7, 1] = bad
+        s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(pos, np.arange(30, dtype=np.uint32))))
+        with pytest.raises(vr.VoidrayError, match="non-finite position") as e:
+            s.validate()
+        assert e.value.status == 1
+    s = vr.Scene()
+    pos = rng.uniform(-1, 1, (300, 3)).astype(np.float32)
+    pos[::7] *= np.float32(3e38)
+    pos[1::11] = np.float32(-3e38)
+    pos[2::13] = 0.0
+    s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(pos, np.arange(300, dtype=np.uint32))))
+    for leaf, bins in ((0, 0), (1, 2), (8, 64)):
+        info = s.validate(bvh_max_leaf=leaf, bvh_bins=bins)
+        assert info.num_triangles == 100

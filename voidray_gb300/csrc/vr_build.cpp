@@ -61,6 +61,15 @@ struct Builder {
         return k;
     }
 
+    // Bin of a centroid coordinate; total for every float (an extent that
+    // overflowed to infinity makes the product NaN, which lands in bin 0).
+    int bin_of(float c, float lo, float scale) const {
+        const float f = (c - lo) * scale;
+        if (!(f > 0.0f)) return 0;
+        if (f >= (float)nbins) return nbins - 1;
+        return (int)f;
+    }
+
     int make_leaf(uint32_t b, uint32_t e, const Box& bx) {
         BNode n;
         std::memcpy(n.lo, bx.lo, sizeof n.lo);
@@ -93,8 +102,7 @@ struct Builder {
                 const float scale = (float)nbins / ext;
                 for (int k = 0; k < nbins; ++k) { bb[k] = Box(); bc[k] = 0; }
                 for (uint32_t i = b; i < e; ++i) {
-                    int k = (int)((refs[i].c[a] - cb.lo[a]) * scale);
-                    k = std::min(std::max(k, 0), nbins - 1);
+                    const int k = bin_of(refs[i].c[a], cb.lo[a], scale);
                     bb[k].grow(refs[i].lo, refs[i].hi);
                     bc[k]++;
                 }
@@ -126,9 +134,7 @@ struct Builder {
             const float ext = cb.hi[a] - cb.lo[a];
             const float scale = (float)nbins / ext;
             auto it = std::partition(refs.begin() + b, refs.begin() + e, [&](const PrimRef& r) {
-                int k = (int)((r.c[a] - cb.lo[a]) * scale);
-                k = std::min(std::max(k, 0), nbins - 1);
-                return k <= best_bin;
+                return bin_of(r.c[a], cb.lo[a], scale) <= best_bin;
             });
             mid = (uint32_t)(it - refs.begin());
         } else {
@@ -357,6 +363,11 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             V3 P[3], N[3];
             for (int k = 0; k < 3; ++k) {
                 P[k] = load3(md.positions + 3 * (size_t)ix[k]);
+                if (!std::isfinite(P[k].x) || !std::isfinite(P[k].y) || !std::isfinite(P[k].z)) {
+                    err = "mesh " + std::to_string(m) + ": vertex " + std::to_string(ix[k]) +
+                          " has a non-finite position";
+                    return VR_ERR_INVALID;
+                }
                 N[k] = md.normals ? load3(md.normals + 3 * (size_t)ix[k]) : v3(0.0f, 0.0f, 0.0f);
                 if (any_uv) {
                     hs.uvs[3 * p + k] = md.uvs ? make_float2(md.uvs[2 * (size_t)ix[k]], md.uvs[2 * (size_t)ix[k] + 1])
