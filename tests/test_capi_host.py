@@ -201,3 +201,31 @@ def test_non_finite_and_extreme_vertices(native):
     for leaf, bins in ((0, 0), (1, 2), (8, 64)):
         info = s.validate(bvh_max_leaf=leaf, bvh_bins=bins)
         assert info.num_triangles == 100
+
+
+def test_bvh_build_independent_of_thread_count(tmp_path):
+    """The SAH build runs on several host threads (subtrees, and the bounds /
+    binning passes of large ranges); the tree is the serial depth-first one
+    whatever the thread count.  The SAH cost, summed over every node in flat
+    order, fingerprints the structure."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    code = ("import json, sys; sys.path.insert(0, %r)\n"
+            "from voidray_gb300 import workloads as W\n"
+            "out = []\n"
+            "for n in (70_000, 300_000):\n"
+            "    s = W.soup_scene(n, seed=n)\n"
+            "    for leaf, bins in ((0, 0), (8, 64)):\n"
+            "        i = s.validate(bvh_max_leaf=leaf, bvh_bins=bins)\n"
+            "        out.append([i.num_nodes, i.max_depth, i.max_leaf, i.sah_cost])\n"
+            "print(json.dumps(out))\n") % str(Path(__file__).resolve().parents[1])
+    runs = []
+    for threads in ("1", "3", "8"):
+        env = dict(os.environ, VR_BUILD_THREADS=threads)
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        runs.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert runs[0] == runs[1] == runs[2]

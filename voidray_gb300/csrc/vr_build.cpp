@@ -13,8 +13,10 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <future>
+#include <system_error>
 #include <thread>
 
 #include "vr_host.h"
@@ -46,6 +48,49 @@ struct Box {
 
 constexpr int DEPTH_LIMIT = STACK_SIZE - 2;  // keeps the traversal stack in bounds
 constexpr double C_TRAV = 1.0, C_ISECT = 1.0;
+
+// Threads the BVH build may use: VR_BUILD_THREADS when set (>= 1), else the
+// host's hardware threads.  The tree does not depend on it.
+unsigned build_threads() {
+    static const unsigned n = [] {
+        if (const char* v = std::getenv("VR_BUILD_THREADS")) {
+            const long k = std::strtol(v, nullptr, 10);
+            if (k >= 1) return (unsigned)std::min(k, 1024L);
+        }
+        const unsigned hw = std::thread::hardware_concurrency();
+        return hw ? hw : 1u;
+    }();
+    return n;
+}
+
+// Runs body(chunk, begin, end) over [b, e) cut into `chunks` pieces, the
+// pieces after the first on their own threads.
+template <class F>
+void for_chunks(uint32_t b, uint32_t e, int chunks, F&& body) {
+    std::vector<std::future<void>> tasks;
+    const uint64_t n = e - b;
+    auto edge = [&](int c) { return b + (uint32_t)(n * (uint64_t)c / (uint64_t)chunks); };
+    for (int c = 1; c < chunks; ++c) {
+        try {
+            tasks.push_back(std::async(std::launch::async, [&body, c, lo = edge(c), hi = edge(c + 1)] {
+                body(c, lo, hi);
+            }));
+        } catch (const std::system_error&) {
+            body(c, edge(c), edge(c + 1));
+        }
+    }
+    body(0, edge(0), edge(1));
+    for (auto& t : tasks) t.get();
+}
+
+// Pieces for a pass over n records: one below 2^16, else up to one per
+// hardware thread.  Every parallel pass here either writes disjoint slots or
+// reduces by min / max / integer sums, exact in any order, so no result
+// depends on the number of pieces.
+int chunks_for(uint64_t n) {
+    if (n < (1u << 16)) return 1;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(build_threads(), n >> 15));
+}
 
 struct Builder {
     std::vector<PrimRef>& refs;
@@ -83,29 +128,90 @@ struct Builder {
     // Builds [b, e) and returns its node index.
     int build(uint32_t b, uint32_t e, int depth) {
         max_depth = std::max<uint32_t>(max_depth, (uint32_t)depth);
-        Box bx, cb;
-        for (uint32_t i = b; i < e; ++i) { bx.grow(refs[i].lo, refs[i].hi); cb.growp(refs[i].c); }
+        Box bx;
+        uint32_t mid = 0;
+        if (!split(b, e, depth, bx, mid)) return make_leaf(b, e, bx);
+        BNode node;
+        std::memcpy(node.lo, bx.lo, sizeof node.lo);
+        std::memcpy(node.hi, bx.hi, sizeof node.hi);
+        nodes.push_back(node);
+        const int self = (int)nodes.size() - 1;
+        const int l = build(b, mid, depth + 1);
+        const int r = build(mid, e, depth + 1);
+        nodes[self].left = l;
+        nodes[self].right = r;
+        return self;
+    }
+
+    void bounds(uint32_t b, uint32_t e, Box& bx, Box& cb) const {
+        const int chunks = chunks_for(e - b);
+        std::vector<Box> pb(chunks), pc(chunks);
+        for_chunks(b, e, chunks, [&](int c, uint32_t lo, uint32_t hi) {
+            for (uint32_t i = lo; i < hi; ++i) { pb[c].grow(refs[i].lo, refs[i].hi); pc[c].growp(refs[i].c); }
+        });
+        for (int c = 0; c < chunks; ++c) {
+            bx.grow(pb[c].lo, pb[c].hi);
+            cb.grow(pc[c].lo, pc[c].hi);
+        }
+    }
+
+    // Centroid bins of [b, e) on the three axes (axes with scale 0 skipped):
+    // bins / counts [3][nbins].
+    void bin_centroids(uint32_t b, uint32_t e, const Box& cb, const float scale[3], Box* bins,
+                       uint32_t* counts) const {
+        const int chunks = chunks_for(e - b);
+        const size_t per = 3 * (size_t)nbins;
+        std::vector<Box> pb(chunks * per);
+        std::vector<uint32_t> pn(chunks * per, 0);
+        for_chunks(b, e, chunks, [&](int c, uint32_t lo, uint32_t hi) {
+            Box* bb = &pb[c * per];
+            uint32_t* bn = &pn[c * per];
+            bool on[3];
+            for (int a = 0; a < 3; ++a) on[a] = scale[a] > 0.0f;
+            for (uint32_t i = lo; i < hi; ++i) {  // one pass over the records, all three axes
+                const PrimRef& r = refs[i];
+                for (int a = 0; a < 3; ++a) {
+                    if (!on[a]) continue;
+                    const int k = a * nbins + bin_of(r.c[a], cb.lo[a], scale[a]);
+                    bb[k].grow(r.lo, r.hi);
+                    bn[k]++;
+                }
+            }
+        });
+        for (int c = 0; c < chunks; ++c)
+            for (size_t k = 0; k < per; ++k) {
+                bins[k].grow(pb[c * per + k].lo, pb[c * per + k].hi);
+                counts[k] += pn[c * per + k];
+            }
+    }
+
+    // Bounds of [b, e) into bx; false when [b, e) becomes a leaf, else the
+    // range is partitioned at `mid` by the binned SAH (object median when the
+    // centroids are degenerate or the depth guard applies).
+    bool split(uint32_t b, uint32_t e, int depth, Box& bx, uint32_t& mid) {
+        Box cb;
+        bounds(b, e, bx, cb);
         const uint32_t n = e - b;
-        if (n == 1) return make_leaf(b, e, bx);
+        if (n == 1) return false;
         const bool force_median = depth + ceil_log2((n + max_leaf - 1) / max_leaf) + 1 >= DEPTH_LIMIT;
-        if (force_median && n <= max_leaf) return make_leaf(b, e, bx);
+        if (force_median && n <= max_leaf) return false;
         int best_axis = -1, best_bin = -1;
         double best_cost = INFINITY;
         const double parent_area = bx.area();
         if (!force_median) {
-            std::vector<Box> bb(nbins);
-            std::vector<uint32_t> bc(nbins);
-            std::vector<double> right_area(nbins), right_cnt(nbins);
+            float scale[3];
             for (int a = 0; a < 3; ++a) {
                 const float ext = cb.hi[a] - cb.lo[a];
-                if (!(ext > 0.0f)) continue;
-                const float scale = (float)nbins / ext;
-                for (int k = 0; k < nbins; ++k) { bb[k] = Box(); bc[k] = 0; }
-                for (uint32_t i = b; i < e; ++i) {
-                    const int k = bin_of(refs[i].c[a], cb.lo[a], scale);
-                    bb[k].grow(refs[i].lo, refs[i].hi);
-                    bc[k]++;
-                }
+                scale[a] = ext > 0.0f ? (float)nbins / ext : 0.0f;
+            }
+            std::vector<Box> bins3(3 * (size_t)nbins);
+            std::vector<uint32_t> counts3(3 * (size_t)nbins, 0);
+            bin_centroids(b, e, cb, scale, bins3.data(), counts3.data());
+            std::vector<double> right_area(nbins), right_cnt(nbins);
+            for (int a = 0; a < 3; ++a) {
+                if (!(scale[a] > 0.0f)) continue;
+                const Box* bb = &bins3[(size_t)a * nbins];
+                const uint32_t* bc = &counts3[(size_t)a * nbins];
                 Box acc;
                 uint32_t cnt = 0;
                 for (int k = nbins - 1; k > 0; --k) {
@@ -126,9 +232,8 @@ struct Builder {
                 }
             }
             const double leaf_cost = C_ISECT * n;
-            if (n <= max_leaf && (best_axis < 0 || leaf_cost <= best_cost)) return make_leaf(b, e, bx);
+            if (n <= max_leaf && (best_axis < 0 || leaf_cost <= best_cost)) return false;
         }
-        uint32_t mid;
         if (best_axis >= 0) {
             const int a = best_axis;
             const float ext = cb.hi[a] - cb.lo[a];
@@ -148,18 +253,79 @@ struct Builder {
                              [a](const PrimRef& x, const PrimRef& y) { return x.c[a] < y.c[a]; });
         }
         if (mid == b || mid == e) mid = b + n / 2;
-        BNode node;
-        std::memcpy(node.lo, bx.lo, sizeof node.lo);
-        std::memcpy(node.hi, bx.hi, sizeof node.hi);
-        nodes.push_back(node);
-        const int self = (int)nodes.size() - 1;
-        const int l = build(b, mid, depth + 1);
-        const int r = build(mid, e, depth + 1);
-        nodes[self].left = l;
-        nodes[self].right = r;
-        return self;
+        return true;
     }
 };
+
+// A subtree in preorder (root first), child indices relative to its array.
+struct SubTree {
+    std::vector<BNode> nodes;
+    uint32_t max_depth = 0;
+};
+
+constexpr uint32_t PAR_MIN_PRIMS = 1u << 15;
+
+// Builds [b, e) into `out`.  While the tree is shallower than `spawn_depth`
+// and the range holds at least PAR_MIN_PRIMS primitives, the left subtree is
+// built on another thread; the halves touch disjoint ranges of `refs`, and the
+// result is spliced as [node, left subtree, right subtree], which is exactly
+// the array the serial depth-first build produces.
+void build_subtree(std::vector<PrimRef>& refs, uint32_t max_leaf, int nbins, uint32_t b, uint32_t e, int depth,
+                   int spawn_depth, SubTree& out) {
+    Builder B(refs, max_leaf, nbins);
+    if (depth >= spawn_depth || e - b < PAR_MIN_PRIMS) {
+        B.nodes.reserve((e - b) / 2 + 16);
+        B.build(b, e, depth);
+        out.nodes = std::move(B.nodes);
+        out.max_depth = B.max_depth;
+        return;
+    }
+    Box bx;
+    uint32_t mid = 0;
+    if (!B.split(b, e, depth, bx, mid)) {
+        B.make_leaf(b, e, bx);
+        out.nodes = std::move(B.nodes);
+        out.max_depth = (uint32_t)depth;
+        return;
+    }
+    SubTree left, right;
+    auto build_left = [&] { build_subtree(refs, max_leaf, nbins, b, mid, depth + 1, spawn_depth, left); };
+    std::future<void> task;
+    try {
+        task = std::async(std::launch::async, build_left);
+    } catch (const std::system_error&) {
+        build_left();  // no thread to be had: build it here
+    }
+    build_subtree(refs, max_leaf, nbins, mid, e, depth + 1, spawn_depth, right);
+    if (task.valid()) task.get();  // rethrows what the other thread threw
+    out.nodes.reserve(1 + left.nodes.size() + right.nodes.size());
+    BNode self;
+    std::memcpy(self.lo, bx.lo, sizeof self.lo);
+    std::memcpy(self.hi, bx.hi, sizeof self.hi);
+    self.left = 1;
+    self.right = 1 + (int32_t)left.nodes.size();
+    out.nodes.push_back(self);
+    for (const SubTree* t : {&left, &right}) {
+        const int32_t off = (int32_t)out.nodes.size();
+        for (BNode n : t->nodes) {
+            if (n.left >= 0) {
+                n.left += off;
+                n.right += off;
+            }
+            out.nodes.push_back(n);
+        }
+    }
+    out.max_depth = std::max<uint32_t>((uint32_t)depth, std::max(left.max_depth, right.max_depth));
+}
+
+// Levels of the tree whose subtrees get their own thread: about four
+// subtrees per hardware thread.
+int spawn_depth_for_host() {
+    const unsigned hw = build_threads();
+    int d = 2;
+    while ((1u << (d - 2)) < hw && d < 8) ++d;
+    return hw == 1 ? 0 : d;
+}
 
 inline V3 dir_from_angles(float sin_t, float cos_t, float phi) {
     return v3(-sin_t * std::cos(phi), -cos_t, sin_t * std::sin(phi));
@@ -350,23 +516,34 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     hs.shade.resize(np * 4);
     if (any_uv) hs.uvs.resize(np * 3);
     Box scene_box;
-    uint64_t p = 0;
-    for (uint32_t m = 0; m < d->num_meshes; ++m) {
-        const vr_mesh_desc& md = d->meshes[m];
-        for (uint32_t t = 0; t < md.num_triangles; ++t, ++p) {
+    // prim ids run over the meshes in order; pieces of the id range are
+    // lowered on separate threads, each stopping at its first bad triangle,
+    // and the error of the lowest id is the one reported
+    std::vector<uint64_t> first_prim(d->num_meshes + 1, 0);
+    for (uint32_t m = 0; m < d->num_meshes; ++m) first_prim[m + 1] = first_prim[m] + d->meshes[m].num_triangles;
+    const int lchunks = chunks_for(np);
+    std::vector<Box> chunk_box(lchunks);
+    std::vector<std::string> chunk_err(lchunks);
+    for_chunks(0, (uint32_t)np, lchunks, [&](int c, uint32_t lo, uint32_t hi) {
+        uint32_t m = (uint32_t)(std::upper_bound(first_prim.begin(), first_prim.end(), (uint64_t)lo) -
+                                first_prim.begin()) - 1;
+        for (uint64_t p = lo; p < hi; ++p) {
+            while (p >= first_prim[m + 1]) ++m;
+            const vr_mesh_desc& md = d->meshes[m];
+            const uint64_t t = p - first_prim[m];
             uint32_t ix[3] = {md.indices[3 * t], md.indices[3 * t + 1], md.indices[3 * t + 2]};
             for (int k = 0; k < 3; ++k)
                 if (ix[k] >= md.num_vertices) {
-                    err = "mesh " + std::to_string(m) + ": index out of range";
-                    return VR_ERR_INVALID;
+                    chunk_err[c] = "mesh " + std::to_string(m) + ": index out of range";
+                    return;
                 }
             V3 P[3], N[3];
             for (int k = 0; k < 3; ++k) {
                 P[k] = load3(md.positions + 3 * (size_t)ix[k]);
                 if (!std::isfinite(P[k].x) || !std::isfinite(P[k].y) || !std::isfinite(P[k].z)) {
-                    err = "mesh " + std::to_string(m) + ": vertex " + std::to_string(ix[k]) +
-                          " has a non-finite position";
-                    return VR_ERR_INVALID;
+                    chunk_err[c] = "mesh " + std::to_string(m) + ": vertex " + std::to_string(ix[k]) +
+                                   " has a non-finite position";
+                    return;
                 }
                 N[k] = md.normals ? load3(md.normals + 3 * (size_t)ix[k]) : v3(0.0f, 0.0f, 0.0f);
                 if (any_uv) {
@@ -399,8 +576,15 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
                 r.c[a] = 0.5f * (r.lo[a] + r.hi[a]);
             }
             r.id = pid;
-            scene_box.grow(r.lo, r.hi);
+            chunk_box[c].grow(r.lo, r.hi);
         }
+    });
+    for (int c = 0; c < lchunks; ++c) {
+        if (!chunk_err[c].empty()) {
+            err = chunk_err[c];
+            return VR_ERR_INVALID;
+        }
+        scene_box.grow(chunk_box[c].lo, chunk_box[c].hi);
     }
     // BVH
     uint32_t max_leaf = d->bvh_max_leaf ? d->bvh_max_leaf : 4;
@@ -412,10 +596,11 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     hs.nodes.clear();
     hs.tris.clear();
     if (np > 0) {
-        Builder B(refs, max_leaf, nbins);
-        B.nodes.reserve(np / 2 + 16);
-        int root = B.build(0, (uint32_t)np, 0);
-        hs.max_depth = B.max_depth + 1;
+        SubTree T;
+        build_subtree(refs, max_leaf, nbins, 0, (uint32_t)np, 0, spawn_depth_for_host(), T);
+        std::vector<BNode>& nodes = T.nodes;
+        const int root = 0;
+        hs.max_depth = T.max_depth + 1;
         // conservative padding keeps the f32 slab test from culling a box whose
         // triangle is hit right on its boundary
         float smax = 0.0f;
@@ -423,21 +608,23 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
         const float pad = std::max(smax, 1e-20f) * 1e-6f;
         // triangle order = prim order after partitioning
         hs.tris.resize(np * 3);
-        for (uint64_t i = 0; i < np; ++i)
-            for (int k = 0; k < 3; ++k) hs.tris[3 * i + k] = v0e[3 * (size_t)refs[i].id + k];
+        for_chunks(0, (uint32_t)np, chunks_for(np), [&](int, uint32_t lo, uint32_t hi) {
+            for (uint64_t i = lo; i < hi; ++i)
+                for (int k = 0; k < 3; ++k) hs.tris[3 * i + k] = v0e[3 * (size_t)refs[i].id + k];
+        });
         // flatten inner nodes depth first
         std::vector<int> order;  // builder node -> flat index
-        std::vector<int> flat_of(B.nodes.size(), -1);
+        std::vector<int> flat_of(nodes.size(), -1);
         std::vector<int> stack;
-        auto is_leaf = [&](int n) { return B.nodes[n].left < 0; };
+        auto is_leaf = [&](int n) { return nodes[n].left < 0; };
         int root_inner = root;
         if (is_leaf(root)) {
             // single leaf: an inner root whose both children are that leaf
-            BNode rn = B.nodes[root];
+            BNode rn = nodes[root];
             rn.left = root;
             rn.right = root;
-            B.nodes.push_back(rn);
-            root_inner = (int)B.nodes.size() - 1;
+            nodes.push_back(rn);
+            root_inner = (int)nodes.size() - 1;
             flat_of.push_back(-1);
         }
         stack.push_back(root_inner);
@@ -446,17 +633,16 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             stack.pop_back();
             flat_of[n] = (int)order.size();
             order.push_back(n);
-            const BNode& bn = B.nodes[n];
+            const BNode& bn = nodes[n];
             if (!is_leaf(bn.right) && bn.right != n) stack.push_back(bn.right);
             if (!is_leaf(bn.left) && bn.left != n) stack.push_back(bn.left);
         }
         hs.nodes.resize(order.size() * 4);
-        double sah = 0.0;
-        const double root_area = Box(scene_box).area();
-        for (size_t f = 0; f < order.size(); ++f) {
-            const BNode& bn = B.nodes[order[f]];
-            const BNode& c0 = B.nodes[bn.left];
-            const BNode& c1 = B.nodes[bn.right];
+        for_chunks(0, (uint32_t)order.size(), chunks_for(order.size()), [&](int, uint32_t flo, uint32_t fhi) {
+          for (size_t f = flo; f < fhi; ++f) {
+            const BNode& bn = nodes[order[f]];
+            const BNode& c0 = nodes[bn.left];
+            const BNode& c1 = nodes[bn.right];
             auto lo = [&](const BNode& c, int a) { return c.lo[a] - pad; };
             auto hi = [&](const BNode& c, int a) { return c.hi[a] + pad; };
             hs.nodes[4 * f + 0] = make_float4(lo(c0, 0), hi(c0, 0), lo(c0, 1), hi(c0, 1));
@@ -474,6 +660,15 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
             std::memcpy(&fn0, &n0, 4);
             std::memcpy(&fn1, &n1, 4);
             hs.nodes[4 * f + 3] = make_float4(fr0, fr1, fn0, fn1);
+          }
+        });
+        // SAH cost of the tree, summed in flat order
+        double sah = 0.0;
+        const double root_area = Box(scene_box).area();
+        for (size_t f = 0; f < order.size(); ++f) {
+            const BNode& bn = nodes[order[f]];
+            const BNode& c0 = nodes[bn.left];
+            const BNode& c1 = nodes[bn.right];
             Box nb;
             nb.grow(bn.lo, bn.hi);
             sah += C_TRAV * nb.area() / std::max(root_area, 1e-300);
