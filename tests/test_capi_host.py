@@ -229,3 +229,20 @@ def test_bvh_build_independent_of_thread_count(tmp_path):
         assert r.returncode == 0, r.stderr[-2000:]
         runs.append(json.loads(r.stdout.strip().splitlines()[-1]))
     assert runs[0] == runs[1] == runs[2]
+
+
+def test_first_bad_triangle_is_reported_with_parallel_lowering():
+    """Large meshes are lowered in pieces on several threads; with bad vertices
+    in several pieces the error names the one of the lowest triangle, as a
+    serial pass would."""
+    n = 200_000
+    pos = np.random.default_rng(5).random((3 * n, 3)).astype(np.float32)
+    idx = np.arange(3 * n, dtype=np.uint32)
+    pos[3 * 150_000 + 1, 2] = np.nan   # triangle 150000
+    pos[3 * 90_000 + 2, 0] = np.inf    # triangle 90000: the first bad one
+    pos[3 * 180_000, 1] = np.nan
+    base = vr.Materials.lambertian((0.5, 0.5, 0.5))
+    s = vr.Scene()
+    s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(pos, idx)))
+    with pytest.raises(vr.VoidrayError, match=f"vertex {3 * 90_000 + 2} has a non-finite position"):
+        s.validate()
