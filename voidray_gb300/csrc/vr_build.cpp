@@ -343,36 +343,44 @@ void build_env_tables(HostScene& hs) {
     EnvTables& T = hs.tables;
     T.W = W;
     T.H = H;
+    // Rows are evaluated on several threads; every floating-point sum below
+    // runs in the serial order (cells row-major, rows top to bottom), so the
+    // tables do not depend on the thread count.
+    const int chunks = (uint64_t)W * H >= (1u << 16) ? (int)std::min<unsigned>(build_threads(), H) : 1;
     std::vector<double> lum((size_t)W * H);
-    double lsum = 0.0;
-    for (uint32_t j = 0; j < H; ++j) {
-        float theta = ((float)j + 0.5f) * (PI_F / (float)H);
-        float st = std::sin(theta), ct = std::cos(theta);
-        for (uint32_t i = 0; i < W; ++i) {
-            float phi = ((float)i + 0.5f) * (2.0f * PI_F / (float)W);
-            V3 c = env_eval_host(v, hs.env_img.data(), dir_from_angles(st, ct, phi));
-            float l = 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
-            if (!(l > 0.0f) || !std::isfinite(l)) l = 0.0f;
-            lum[(size_t)j * W + i] = (double)l;
-            lsum += (double)l;
+    for_chunks(0, H, chunks, [&](int, uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0; j < j1; ++j) {
+            float theta = ((float)j + 0.5f) * (PI_F / (float)H);
+            float st = std::sin(theta), ct = std::cos(theta);
+            for (uint32_t i = 0; i < W; ++i) {
+                float phi = ((float)i + 0.5f) * (2.0f * PI_F / (float)W);
+                V3 c = env_eval_host(v, hs.env_img.data(), dir_from_angles(st, ct, phi));
+                float l = 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+                if (!(l > 0.0f) || !std::isfinite(l)) l = 0.0f;
+                lum[(size_t)j * W + i] = (double)l;
+            }
         }
-    }
+    });
+    double lsum = 0.0;
+    for (double l : lum) lsum += l;
     double floor_l = 1e-3 * (lsum / ((double)W * H));
     if (!(floor_l > 0.0)) floor_l = 1.0;
     std::vector<double> w((size_t)W * H), rows(H);
-    double total = 0.0;
-    for (uint32_t j = 0; j < H; ++j) {
-        float theta = ((float)j + 0.5f) * (PI_F / (float)H);
-        double st = (double)std::sin(theta);
-        double rs = 0.0;
-        for (uint32_t i = 0; i < W; ++i) {
-            double x = (lum[(size_t)j * W + i] + floor_l) * st;
-            w[(size_t)j * W + i] = x;
-            rs += x;
+    for_chunks(0, H, chunks, [&](int, uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0; j < j1; ++j) {
+            float theta = ((float)j + 0.5f) * (PI_F / (float)H);
+            double st = (double)std::sin(theta);
+            double rs = 0.0;
+            for (uint32_t i = 0; i < W; ++i) {
+                double x = (lum[(size_t)j * W + i] + floor_l) * st;
+                w[(size_t)j * W + i] = x;
+                rs += x;
+            }
+            rows[j] = rs;
         }
-        rows[j] = rs;
-        total += rs;
-    }
+    });
+    double total = 0.0;
+    for (uint32_t j = 0; j < H; ++j) total += rows[j];
     T.marginal.assign(H + 1, 0.0f);
     T.conditional.assign((size_t)H * (W + 1), 0.0f);
     T.cell.assign((size_t)W * H, 0.0f);
@@ -380,15 +388,19 @@ void build_env_tables(HostScene& hs) {
     for (uint32_t j = 0; j < H; ++j) {
         T.marginal[j] = (float)(acc / total);
         acc += rows[j];
-        double ra = 0.0;
-        float* cr = &T.conditional[(size_t)j * (W + 1)];
-        for (uint32_t i = 0; i < W; ++i) {
-            cr[i] = (float)(ra / rows[j]);
-            ra += w[(size_t)j * W + i];
-            T.cell[(size_t)j * W + i] = (float)(w[(size_t)j * W + i] / total);
-        }
-        cr[W] = 1.0f;
     }
+    for_chunks(0, H, chunks, [&](int, uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0; j < j1; ++j) {
+            double ra = 0.0;
+            float* cr = &T.conditional[(size_t)j * (W + 1)];
+            for (uint32_t i = 0; i < W; ++i) {
+                cr[i] = (float)(ra / rows[j]);
+                ra += w[(size_t)j * W + i];
+                T.cell[(size_t)j * W + i] = (float)(w[(size_t)j * W + i] / total);
+            }
+            cr[W] = 1.0f;
+        }
+    });
     T.marginal[H] = 1.0f;
 }
 
