@@ -22,9 +22,12 @@
 #include <cstdint>
 #include <cstring>
 #include <functional>
+#include <future>
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/voidray_image.h"
@@ -190,7 +193,6 @@ struct Decoder {
     int adobe_transform = -1;
     int eobrun = 0;
     bool header_only = false;
-    bool done = false;
 
     Decoder(const uint8_t* d, size_t n) : data(d), size(n) {}
 
@@ -206,7 +208,7 @@ struct Decoder {
     void run() {
         if (size < 4 || data[0] != 0xFF || data[1] != 0xD8) fail(VR_ERR_INVALID, "not a JPEG stream (no SOI)");
         pos = 2;
-        while (!done) {
+        for (;;) {
             // markers may be preceded by any number of 0xFF fill bytes
             uint8_t b = u8();
             if (b != 0xFF) fail(VR_ERR_INVALID, "JPEG: marker expected");
@@ -634,6 +636,25 @@ void ycc_to_rgb(uint8_t y, uint8_t cb, uint8_t cr, uint8_t* rgb) {
     rgb[2] = clamp_u8(Y + 1.772f * Cb);
 }
 
+// Runs body(begin, end) over [0, n) in pieces on the host's threads (one
+// piece below `grain` items).  The bodies write disjoint outputs.
+template <class F>
+void parallel_for(size_t n, size_t grain, F&& body) {
+    unsigned hw = std::thread::hardware_concurrency();
+    const size_t pieces = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, n / std::max<size_t>(grain, 1)));
+    std::vector<std::future<void>> tasks;
+    for (size_t k = 1; k < pieces; ++k) {
+        const size_t lo = n * k / pieces, hi = n * (k + 1) / pieces;
+        try {
+            tasks.push_back(std::async(std::launch::async, [&body, lo, hi] { body(lo, hi); }));
+        } catch (const std::system_error&) {
+            body(lo, hi);
+        }
+    }
+    body(0, n / pieces);
+    for (auto& t : tasks) t.get();
+}
+
 void decode_pixels(Decoder& d, uint8_t* rgb) {
     static const Idct idct;
     const size_t n = size_t(d.width) * d.height;
@@ -645,9 +666,11 @@ void decode_pixels(Decoder& d, uint8_t* rgb) {
         // only the blocks that cover the component's samples are transformed
         const int bw_used = std::min(c.bw, (c.cw + 7) / 8), bh_used = std::min(c.bh, (c.ch + 7) / 8);
         plane.assign(size_t(pw) * c.bh * 8, 0);
-        for (int by = 0; by < bh_used; ++by)
-            for (int bx = 0; bx < bw_used; ++bx)
-                idct.run(&c.coef[(size_t(by) * c.bw + bx) * 64], c.q, &plane[size_t(by) * 8 * pw + size_t(bx) * 8], pw);
+        parallel_for(size_t(bh_used), 16, [&](size_t by0, size_t by1) {
+            for (size_t by = by0; by < by1; ++by)
+                for (int bx = 0; bx < bw_used; ++bx)
+                    idct.run(&c.coef[(by * c.bw + bx) * 64], c.q, &plane[by * 8 * pw + size_t(bx) * 8], pw);
+        });
         upsample(c, plane, d.hmax, d.vmax, d.width, d.height, full[ci]);
     }
     const size_t nc = d.comps.size();
@@ -659,15 +682,17 @@ void decode_pixels(Decoder& d, uint8_t* rgb) {
         bool is_rgb;
         if (d.adobe) is_rgb = d.adobe_transform == 0;
         else is_rgb = !d.jfif && d.comps[0].id == 'R' && d.comps[1].id == 'G' && d.comps[2].id == 'B';
-        for (size_t i = 0; i < n; ++i) {
-            if (is_rgb) {
-                rgb[3 * i] = full[0][i];
-                rgb[3 * i + 1] = full[1][i];
-                rgb[3 * i + 2] = full[2][i];
-            } else {
-                ycc_to_rgb(full[0][i], full[1][i], full[2][i], rgb + 3 * i);
+        parallel_for(n, 1 << 16, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; ++i) {
+                if (is_rgb) {
+                    rgb[3 * i] = full[0][i];
+                    rgb[3 * i + 1] = full[1][i];
+                    rgb[3 * i + 2] = full[2][i];
+                } else {
+                    ycc_to_rgb(full[0][i], full[1][i], full[2][i], rgb + 3 * i);
+                }
             }
-        }
+        });
         return;
     }
     // four components: Adobe CMYK (transform 0) or YCCK (transform 2), stored
