@@ -246,3 +246,26 @@ def test_first_bad_triangle_is_reported_with_parallel_lowering():
     s.add_object(s.add_material(base), s.add_mesh(vr.Mesh(pos, idx)))
     with pytest.raises(vr.VoidrayError, match=f"vertex {3 * 90_000 + 2} has a non-finite position"):
         s.validate()
+
+
+def test_scene_acceleration_ref_accessors(native):
+    """SceneAcceleration's surface_ref / material_ref / texture_ref / mesh_ref /
+    object_ref (scene.rs:207-225) over the lists copied at build time; host only."""
+    s = vr.Scene()
+    m0 = s.add_material(vr.Materials.lambertian((0.5, 0.5, 0.5)))
+    t0 = s.add_texture(vr.ImageTexture(np.ones((2, 2, 3), np.float32)))
+    m1 = s.add_material(vr.Materials.lambertian_texture_no_normal(t0))
+    mesh = vr.Mesh(np.eye(3, dtype=np.float32), [0, 1, 2])
+    s0 = s.add_mesh(mesh)
+    s1 = s.add_analytic_surface(vr.Surfaces.sphere((0, 0, 0), 1.0))
+    o0 = s.add_object(m0, s0)
+    o1 = s.add_object(m1, s1)
+    acc = vr.SceneAcceleration.__new__(vr.SceneAcceleration)  # no vr_scene_create: the accessors need no device
+    acc._h = None
+    acc._keep_lists(s)
+    s.add_material(vr.Materials.metal((1, 1, 1), 0.1))  # later edits of the scene do not reach the copies
+    assert len(acc._materials) == 2
+    assert acc.surface_ref(s0) is mesh and acc.mesh_ref(0) is mesh
+    assert isinstance(acc.surface_ref(s1), vr.AnalyticSurface)
+    assert acc.material_ref(m1) is s.materials[m1] and acc.texture_ref(t0) is s.textures[t0]
+    assert acc.object_ref(o1).surface == s1 and acc.object_ref(o0).material == m0

@@ -576,7 +576,36 @@ class SceneAcceleration:
         h = C.c_void_p()
         check(lib().vr_scene_create(C.byref(desc), C.byref(h)))
         self._h = h
+        self._keep_lists(scene)
+
+    def _keep_lists(self, scene: Scene) -> None:
+        """Scene::build_acceleration (scene.rs:163-178) keeps copies of the
+        scene's lists; the *_ref accessors read them."""
         self.camera = scene.camera
+        self.environment = scene.environment
+        self._objects = list(scene.objects)
+        self._surfaces = list(scene.surfaces)
+        self._textures = list(scene.textures)
+        self._meshes = list(scene.meshes)
+        self._materials = list(scene.materials)
+
+    # scene.rs:207-225; handles are plain ints
+    def surface_ref(self, surface: int):
+        """The mesh of a mesh surface, or the AnalyticSurface."""
+        s = self._surfaces[surface]
+        return self._meshes[s] if isinstance(s, int) else s
+
+    def material_ref(self, material: int) -> "Material":
+        return self._materials[material]
+
+    def texture_ref(self, texture: int) -> "ImageTexture":
+        return self._textures[texture]
+
+    def mesh_ref(self, mesh: int) -> "Mesh":
+        return self._meshes[mesh]
+
+    def object_ref(self, obj: int) -> "Object":
+        return self._objects[obj]
 
     @property
     def handle(self) -> C.c_void_p:
