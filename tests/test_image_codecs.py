@@ -11,6 +11,7 @@ triangle upsampling, JFIF matrix); a progressive stream must decode to exactly
 the bytes of the sequential stream with the same coefficients.  No GPU.
 """
 import heapq
+import os
 import struct
 import zlib
 from pathlib import Path
@@ -27,7 +28,7 @@ ZZ = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 2
 _U = np.arange(8)
 DCT = np.array([[(np.sqrt(0.5) if u == 0 else 1.0) * 0.5 * np.cos((2 * x + 1) * u * np.pi / 16) for x in _U]
                 for u in _U])  # DCT[u, x]
-ASSETS = Path("/root/reference/assets")
+ASSETS = Path(os.environ.get("VOIDRAY_REFERENCE", "/root/reference")) / "assets"
 
 
 # ------------------------------------------------------------ JPEG encoder ---

@@ -1,4 +1,4 @@
-"""The render-thread driver (renderer.rs one_shot): actions, statistics,
+"""The render thread (renderer.rs one_shot): actions, statistics,
 cancel, and the chunking kept from the reference."""
 import time
 

@@ -217,7 +217,7 @@ def lib() -> C.CDLL:
         path = Path(os.environ.get("VOIDRAY_GB300_LIB", LIB_PATH))
         if not path.exists():
             raise VoidrayError(7, f"native library {path} is missing; build it with "
-                                  "`python -c 'import __graft_entry__ as g; g.build()'`")
+                                  "`python -m voidray_gb300.build`")
         dll = C.CDLL(str(path))
         for name, res, args in _SIGS:
             fn = getattr(dll, name)

@@ -1,5 +1,5 @@
-"""The render-thread driver of voidray_renderer/src/render/renderer.rs on the
-GPU backend.
+"""The render thread of voidray_renderer/src/render/renderer.rs on the GPU
+backend.
 
 `Renderer.execute(RenderAction.RENDER)` starts a one-shot progressive render
 on a background thread (`RenderThread::one_shot`, renderer.rs:35-125): clear
