@@ -79,7 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise RuntimeError(f"nvcc failed for {failed}")
     if force or procs or not LIB.exists():
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"]
+        cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC,-pthread"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         subprocess.run(cmd, check=True)
