@@ -13,6 +13,75 @@ from voidray_gb300 import assets as A
 from voidray_gb300._native import VoidrayError
 from voidray_gb300.scene import Mesh, Scene, ImageTexture, Environments, SampleType
 
+# ------------------------------------------------------- OBJ restatement ---
+def _obj_index(tok: str, count: int, what: str, line: int) -> int:
+    try:
+        i = int(tok)
+    except ValueError:
+        raise VoidrayError(1, f"OBJ line {line}: bad {what} index {tok!r}") from None
+    j = count + i if i < 0 else i - 1
+    if i == 0 or not 0 <= j < count:
+        raise VoidrayError(1, f"OBJ line {line}: {what} index {i} out of range (have {count})")
+    return j
+
+
+def parse_obj_restated(text: str):
+    """The obj-rs TexturedVertex rules written out line by line in Python (the
+    library's parser is native); returns the same four arrays."""
+    pos: list[tuple[float, float, float]] = []
+    tex: list[tuple[float, float]] = []
+    nrm: list[tuple[float, float, float]] = []
+    cache: dict[tuple[int, int, int], int] = {}
+    order: list[tuple[int, int, int]] = []
+    indices: list[int] = []
+    for ln, raw in enumerate(text.splitlines(), 1):
+        line = raw.split("#", 1)[0].split()
+        if not line:
+            continue
+        key, args = line[0], line[1:]
+        try:
+            if key == "v":
+                if len(args) < 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: vertex needs 3 coordinates")
+                pos.append((float(args[0]), float(args[1]), float(args[2])))
+            elif key == "vt":
+                if not args:
+                    raise VoidrayError(1, f"OBJ line {ln}: texture coordinate needs u")
+                tex.append((float(args[0]), float(args[1]) if len(args) > 1 else 0.0))
+            elif key == "vn":
+                if len(args) < 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: normal needs 3 components")
+                nrm.append((float(args[0]), float(args[1]), float(args[2])))
+            elif key == "f":
+                if len(args) != 3:
+                    raise VoidrayError(1, f"OBJ line {ln}: face with {len(args)} corners "
+                                          "(the model must be triangulated)")
+                for corner in args:
+                    parts = corner.split("/")
+                    if len(parts) != 3 or not parts[1] or not parts[2]:
+                        raise VoidrayError(1, f"OBJ line {ln}: face corner {corner!r} lacks texture "
+                                              "or normal indices")
+                    k = (_obj_index(parts[0], len(pos), "position", ln),
+                         _obj_index(parts[2], len(nrm), "normal", ln),
+                         _obj_index(parts[1], len(tex), "texture", ln))
+                    v = cache.get(k)
+                    if v is None:
+                        v = cache[k] = len(order)
+                        order.append(k)
+                    indices.append(v)
+        except ValueError:
+            raise VoidrayError(1, f"OBJ line {ln}: cannot parse {raw.strip()!r}") from None
+    n = len(order)
+    p = np.asarray(pos, np.float64).reshape(-1, 3)
+    t = np.asarray(tex, np.float64).reshape(-1, 2)
+    q = np.asarray(nrm, np.float64).reshape(-1, 3)
+    ix = np.asarray(order, np.int64).reshape(-1, 3)
+    positions = p[ix[:, 0]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
+    normals = q[ix[:, 1]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
+    uvs = t[ix[:, 2]].astype(np.float32) if n else np.zeros((0, 2), np.float32)
+    return positions, uvs, normals, np.asarray(indices, np.uint32).reshape(-1, 3)
+
+
 OBJ = """# comment line
 mtllib x.mtl
 o thing
@@ -341,3 +410,78 @@ def test_corrupt_files_raise_voidray_errors_only():
                 decode(bytes(b))
             except VoidrayError as e:
                 assert e.status in (1, 2)
+
+
+def _random_obj(rng, n_faces, bad=False):
+    """OBJ text with comments, ignored statements, w components, 1- and
+    3-component vt, negative indices, CRLF / CR line ends and shared corners."""
+    lines = ["# generated", "mtllib a.mtl", "o part"]
+    counts = [0, 0, 0]  # v, vt, vn
+    for _ in range(rng.integers(3, 9)):
+        lines.append("v " + " ".join(f"{x:.6g}" for x in rng.normal(0, 3, rng.integers(3, 5))))
+        counts[0] += 1
+    for _ in range(rng.integers(1, 6)):
+        lines.append("vt " + " ".join(f"{x:.5f}" for x in rng.random(rng.integers(1, 4))))
+        counts[1] += 1
+    for _ in range(rng.integers(1, 5)):
+        lines.append("vn " + " ".join(f"{x:.4e}" for x in rng.normal(0, 1, 3)))
+        counts[2] += 1
+    for f in range(n_faces):
+        if rng.random() < 0.15:
+            kind = rng.integers(0, 3)
+            lines.append(["v", "vt", "vn"][kind] + " " + " ".join(f"{x:.3f}" for x in rng.random(3)))
+            counts[kind] += 1
+        corners = []
+        for _ in range(3):
+            ix = []
+            for c in (0, 1, 2):
+                k = int(rng.integers(1, counts[c] + 1))
+                ix.append(str(k - counts[c] - 1) if rng.random() < 0.3 else str(k))
+            corners.append("/".join(ix))
+        line = "f " + " ".join(corners)
+        if rng.random() < 0.1:
+            line += "  # trailing comment"
+        if rng.random() < 0.05:
+            lines.append("s off")
+        lines.append(line)
+    if bad:
+        j = int(rng.integers(3, len(lines)))
+        lines[j] = rng.choice(["f 1/1/1 2/1/1", "f 1//1 2//1 3//1", "v 1 2", "vt", "vn 1 x 2",
+                               f"f 1/1/1 2/1/1 {counts[0] + 7}/1/1", "f 0/1/1 1/1/1 1/1/1", "f a/1/1 1/1/1 1/1/1",
+                               "v 1.5 2..5 3"])
+    sep = rng.choice(["\n", "\r\n", "\r"])
+    return sep.join(lines) + sep
+
+
+def test_native_obj_parser_matches_the_restatement():
+    """The native parser against the Python restatement of the obj-rs rules on
+    random OBJ texts: identical arrays, and the same error message for the
+    same first bad line."""
+    rng = np.random.default_rng(21)
+    for it in range(400):
+        bad = it % 4 == 3
+        text = _random_obj(rng, int(rng.integers(0, 40)), bad)
+        try:
+            want = parse_obj_restated(text)
+        except VoidrayError as e:
+            with pytest.raises(VoidrayError) as got:
+                A.parse_obj(text)
+            assert got.value.status == 1 and str(got.value) == str(e), (str(got.value), str(e))
+            continue
+        got = A.parse_obj(text)
+        for a, b in zip(got, want):
+            assert a.dtype == b.dtype and np.array_equal(a, b)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_ASSET), reason="reference assets not present")
+def test_native_obj_parser_on_the_reference_meshes():
+    folder = os.path.dirname(REF_ASSET)
+    for name in ("mushroom.obj", "mossy_ground.obj", "material_testing_stand.obj"):
+        path = os.path.join(folder, name)
+        if not os.path.exists(path):
+            continue
+        with open(path, "r", encoding="utf-8", errors="replace") as f:
+            want = parse_obj_restated(f.read())
+        got = A.load_obj(path)
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b)

@@ -1,4 +1,4 @@
-"""JPEG (native decoder, include/voidray_image.h) and TIFF (voidray_gb300.assets)
+"""JPEG (native decoder, include/voidray_assets.h) and TIFF (voidray_gb300.assets)
 decoding against independent encoders written here.
 
 The JPEG encoder follows ITU-T T.81: JFIF colour conversion, forward DCT,

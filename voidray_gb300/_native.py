@@ -117,6 +117,12 @@ class vr_image_info(C.Structure):
                 ("progressive", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class vr_obj_mesh(C.Structure):
+    _fields_ = [("positions", C.POINTER(C.c_float)), ("uvs", C.POINTER(C.c_float)),
+                ("normals", C.POINTER(C.c_float)), ("indices", C.POINTER(C.c_uint32)),
+                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32)]
+
+
 STATS_TILE = 16
 STATS_MAX_JOBS = 128
 
@@ -201,9 +207,11 @@ _SIGS = [
       C.c_int32, P]),
     ("vr_dn_conv3x3_wgrad_device", C.c_int,
      [P, P, C.c_uint32, C.c_int32, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P]),
-    # include/voidray_image.h
+    # include/voidray_assets.h
     ("vr_image_info_get", C.c_int, [P, C.c_size_t, P]),
     ("vr_image_decode_rgb8", C.c_int, [P, C.c_size_t, P, C.c_size_t]),
+    ("vr_obj_parse", C.c_int, [P, C.c_size_t, P]),
+    ("vr_obj_free", C.c_int, [P]),
 ]
 EXPORTED = [name for name, _, _ in _SIGS]
 

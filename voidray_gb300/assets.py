@@ -14,7 +14,8 @@ reaches the renderer.
   order of first use; other statements (`o`, `g`, `s`, `usemtl`, `mtllib`,
   `l`, `p`) do not change the mesh.  Numbers are parsed as f64 and rounded
   to f32, which equals a direct decimal-to-f32 conversion for the short
-  decimals OBJ writers emit.
+  decimals OBJ writers emit.  The parsing runs in the native library
+  (`vr_obj_parse`, one pass, hundreds of MB/s).
 - `load_image_rgb32f` follows `image::open(path).to_rgb32f()` as
   `ImageTexture::new` (voidray_renderer/src/core/texture.rs:36-50) and
   `HDRIEnvironment::new` (voidray_common/src/environments.rs:42-55) call it
@@ -23,7 +24,7 @@ reaches the renderer.
   here: PNG (every colour type and bit depth, Adam7 interlacing); OpenEXR
   scanline files with NONE, RLE, ZIPS or ZIP compression and HALF, FLOAT or
   UINT channels; JPEG (baseline, extended and progressive Huffman DCT, 8-bit;
-  decoded by the native library, `include/voidray_image.h`); TIFF (the first
+  decoded by the native library, `include/voidray_assets.h`); TIFF (the first
   image of the file: strips or tiles, chunky or planar, no / LZW / Deflate /
   PackBits compression, horizontal and floating-point predictors, grey,
   palette and RGB(A), 1-32-bit integer and 16/32/64-bit float samples).
@@ -62,77 +63,31 @@ def _corrupt_is_invalid(fmt: str):
 
 
 # -------------------------------------------------------------------- OBJ ---
-def _obj_index(tok: str, count: int, what: str, line: int) -> int:
-    try:
-        i = int(tok)
-    except ValueError:
-        raise VoidrayError(1, f"OBJ line {line}: bad {what} index {tok!r}") from None
-    j = count + i if i < 0 else i - 1
-    if i == 0 or not 0 <= j < count:
-        raise VoidrayError(1, f"OBJ line {line}: {what} index {i} out of range (have {count})")
-    return j
-
-
-@_corrupt_is_invalid("OBJ")
-def parse_obj(text: str):
+def parse_obj(text):
     """Returns (positions f32 [V,3], uvs f32 [V,2], normals f32 [V,3],
-    indices u32 [F,3]) with the obj-rs TexturedVertex numbering."""
-    pos: list[tuple[float, float, float]] = []
-    tex: list[tuple[float, float]] = []
-    nrm: list[tuple[float, float, float]] = []
-    cache: dict[tuple[int, int, int], int] = {}
-    order: list[tuple[int, int, int]] = []
-    indices: list[int] = []
-    for ln, raw in enumerate(text.splitlines(), 1):
-        line = raw.split("#", 1)[0].split()
-        if not line:
-            continue
-        key, args = line[0], line[1:]
-        try:
-            if key == "v":
-                if len(args) < 3:
-                    raise VoidrayError(1, f"OBJ line {ln}: vertex needs 3 coordinates")
-                pos.append((float(args[0]), float(args[1]), float(args[2])))
-            elif key == "vt":
-                if not args:
-                    raise VoidrayError(1, f"OBJ line {ln}: texture coordinate needs u")
-                tex.append((float(args[0]), float(args[1]) if len(args) > 1 else 0.0))
-            elif key == "vn":
-                if len(args) < 3:
-                    raise VoidrayError(1, f"OBJ line {ln}: normal needs 3 components")
-                nrm.append((float(args[0]), float(args[1]), float(args[2])))
-            elif key == "f":
-                if len(args) != 3:
-                    raise VoidrayError(1, f"OBJ line {ln}: face with {len(args)} corners "
-                                          "(the model must be triangulated)")
-                for corner in args:
-                    parts = corner.split("/")
-                    if len(parts) != 3 or not parts[1] or not parts[2]:
-                        raise VoidrayError(1, f"OBJ line {ln}: face corner {corner!r} lacks texture "
-                                              "or normal indices")
-                    k = (_obj_index(parts[0], len(pos), "position", ln),
-                         _obj_index(parts[2], len(nrm), "normal", ln),
-                         _obj_index(parts[1], len(tex), "texture", ln))
-                    v = cache.get(k)
-                    if v is None:
-                        v = cache[k] = len(order)
-                        order.append(k)
-                    indices.append(v)
-        except ValueError:
-            raise VoidrayError(1, f"OBJ line {ln}: cannot parse {raw.strip()!r}") from None
-    n = len(order)
-    p = np.asarray(pos, np.float64).reshape(-1, 3)
-    t = np.asarray(tex, np.float64).reshape(-1, 2)
-    q = np.asarray(nrm, np.float64).reshape(-1, 3)
-    ix = np.asarray(order, np.int64).reshape(-1, 3)
-    positions = p[ix[:, 0]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
-    normals = q[ix[:, 1]].astype(np.float32) if n else np.zeros((0, 3), np.float32)
-    uvs = t[ix[:, 2]].astype(np.float32) if n else np.zeros((0, 2), np.float32)
-    return positions, uvs, normals, np.asarray(indices, np.uint32).reshape(-1, 3)
+    indices u32 [F,3]) with the obj-rs TexturedVertex numbering, parsed by the
+    native library (vr_obj_parse, include/voidray_assets.h)."""
+    from . import _native as N
+
+    data = text.encode("utf-8", "surrogateescape") if isinstance(text, str) else bytes(text)
+    mesh = N.vr_obj_mesh()
+    N.check(N.lib().vr_obj_parse(data, len(data), ctypes.byref(mesh)))
+    try:
+        nv, nt = mesh.num_vertices, mesh.num_triangles
+
+        def take(ptr, count, dtype, width):
+            if count == 0:
+                return np.zeros((0, width), dtype)
+            return np.ctypeslib.as_array(ptr, shape=(count * width,)).copy().reshape(count, width)
+
+        return (take(mesh.positions, nv, np.float32, 3), take(mesh.uvs, nv, np.float32, 2),
+                take(mesh.normals, nv, np.float32, 3), take(mesh.indices, nt, np.uint32, 3))
+    finally:
+        N.lib().vr_obj_free(ctypes.byref(mesh))
 
 
 def load_obj(path: str):
-    with open(path, "r", encoding="utf-8", errors="replace") as f:
+    with open(path, "rb") as f:
         return parse_obj(f.read())
 
 

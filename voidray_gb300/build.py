@@ -21,9 +21,9 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libvoidray_gb300.so"
 
 SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "vr_serve.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu",
-           "vr_image.cpp"]
+           "vr_image.cpp", "vr_obj.cpp"]
 # host-only translation units: compiled as plain C++ (no device code)
-HOST_ONLY = {"vr_image.cpp"}
+HOST_ONLY = {"vr_image.cpp", "vr_obj.cpp"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -30,7 +30,7 @@
 #include <thread>
 #include <vector>
 
-#include "../../include/voidray_image.h"
+#include "../../include/voidray_assets.h"
 
 namespace vr {
 // The C ABI's thread-local error message (vr_capi.cu); returns s.
