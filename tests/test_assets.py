@@ -485,3 +485,12 @@ def test_native_obj_parser_on_the_reference_meshes():
         got = A.load_obj(path)
         for a, b in zip(got, want):
             assert np.array_equal(a, b)
+
+
+def test_obj_errors_quoting_undecodable_bytes():
+    """An error message that quotes bytes of the input which are not UTF-8
+    still reaches Python as a VoidrayError."""
+    with pytest.raises(VoidrayError, match="cannot parse"):
+        A.parse_obj(b"v 0 0 \xff\xfe\n")
+    with pytest.raises(VoidrayError, match="bad position index"):
+        A.parse_obj("v 0 0 0\nvt 0 0\nvn 0 0 1\nf \ud800/1/1 1/1/1 1/1/1\n")

@@ -238,7 +238,7 @@ def lib() -> C.CDLL:
 def check(status: int) -> None:
     if status != VR_OK:
         msg = lib().vr_last_error()
-        raise VoidrayError(status, msg.decode() if msg else "")
+        raise VoidrayError(status, msg.decode("utf-8", "replace") if msg else "")
 
 
 def ptr(a) -> int | None:

@@ -69,7 +69,7 @@ def parse_obj(text):
     native library (vr_obj_parse, include/voidray_assets.h)."""
     from . import _native as N
 
-    data = text.encode("utf-8", "surrogateescape") if isinstance(text, str) else bytes(text)
+    data = text.encode("utf-8", "surrogatepass") if isinstance(text, str) else bytes(text)
     mesh = N.vr_obj_mesh()
     N.check(N.lib().vr_obj_parse(data, len(data), ctypes.byref(mesh)))
     try:
