@@ -67,6 +67,15 @@ vr_status vr_image_info_get(const uint8_t* data, size_t size, vr_image_info* inf
  * (width * height * 3 bytes; `capacity` is the size of `rgb` in bytes). */
 vr_status vr_image_decode_rgb8(const uint8_t* data, size_t size, uint8_t* rgb, size_t capacity);
 
+/* Undoes the PNG scanline filters (None, Sub, Up, Average, Paeth; ISO/IEC
+ * 15948 clause 9) of `rows` scanlines of `stride` bytes, each preceded by its
+ * filter-type byte, read from `data` (`size` bytes, at least rows * (stride +
+ * 1)).  `bpp` is the filters' byte distance: the bytes of one complete pixel,
+ * at least 1.  Writes rows * stride bytes to `out`.  An unknown filter type
+ * returns VR_ERR_INVALID. */
+vr_status vr_png_unfilter(const uint8_t* data, size_t size, uint32_t rows, uint32_t stride, uint32_t bpp,
+                          uint8_t* out);
+
 /* A parsed OBJ mesh; the arrays belong to the library until vr_obj_free. */
 typedef struct vr_obj_mesh {
     float* positions;      /* 3 * num_vertices                                 */

@@ -494,3 +494,65 @@ def test_obj_errors_quoting_undecodable_bytes():
         A.parse_obj(b"v 0 0 \xff\xfe\n")
     with pytest.raises(VoidrayError, match="bad position index"):
         A.parse_obj("v 0 0 0\nvt 0 0\nvn 0 0 1\nf \ud800/1/1 1/1/1 1/1/1\n")
+
+
+def _paeth_restated(a: int, b: int, c: int) -> int:
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def png_unfilter_restated(data: bytes, pos: int, rows: int, stride: int, bpp: int):
+    """The five PNG scanline filters undone byte by byte in Python (the
+    library does it natively); returns (uint8 [rows, stride], new pos)."""
+    out = np.zeros((rows, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    for y in range(rows):
+        ftype = data[pos]
+        line = np.frombuffer(data, np.uint8, stride, pos + 1).astype(np.int32)
+        pos += 1 + stride
+        if ftype == 0:
+            cur = line
+        elif ftype == 2:
+            cur = (line + prev) & 0xFF
+        elif ftype == 1:  # Sub: a running sum per byte lane of the pixel
+            cur = line.copy()
+            for k in range(min(bpp, stride)):
+                cur[k::bpp] = np.cumsum(line[k::bpp]) & 0xFF
+        elif ftype in (3, 4):  # Average and Paeth depend on the byte just decoded
+            lst = line.tolist()
+            up = prev.tolist()
+            for i in range(stride):
+                a = lst[i - bpp] if i >= bpp else 0
+                if ftype == 3:
+                    lst[i] = (lst[i] + ((a + up[i]) >> 1)) & 0xFF
+                else:
+                    lst[i] = (lst[i] + _paeth_restated(a, up[i], up[i - bpp] if i >= bpp else 0)) & 0xFF
+            cur = np.asarray(lst, np.int32)
+        else:
+            raise VoidrayError(1, f"PNG: unknown filter type {ftype}")
+        out[y] = cur
+        prev = cur
+    return out, pos
+
+
+@pytest.mark.parametrize("rows,stride,bpp", [(1, 1, 1), (7, 13, 3), (16, 64, 4), (5, 96, 8), (33, 7, 1), (4, 24, 6)])
+def test_png_unfilter_matches_the_restatement(rows, stride, bpp):
+    """vr_png_unfilter against the byte-by-byte Python restatement on random
+    scanlines with every filter type (and a random mix per row)."""
+    rng = np.random.default_rng(rows * stride + bpp)
+    for types in ([0], [1], [2], [3], [4], [0, 1, 2, 3, 4]):
+        body = rng.integers(0, 256, (rows, stride + 1), dtype=np.uint8)
+        body[:, 0] = rng.choice(types, rows)
+        data = b"xyz" + body.tobytes()
+        got, gpos = A._png_unfilter(data, 3, rows, stride, bpp)
+        want, wpos = png_unfilter_restated(data, 3, rows, stride, bpp)
+        assert gpos == wpos and np.array_equal(got, want)
+    bad = bytearray(data)
+    bad[3 + (stride + 1) * (rows - 1)] = 5
+    with pytest.raises(VoidrayError, match="unknown filter type 5"):
+        A._png_unfilter(bytes(bad), 3, rows, stride, bpp)
+    with pytest.raises(VoidrayError, match="shorter"):
+        A._png_unfilter(data[:-1], 3, rows, stride, bpp)

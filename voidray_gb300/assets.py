@@ -100,45 +100,16 @@ _ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), 
 _PNG_CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
 
 
-def _paeth(a: int, b: int, c: int) -> int:
-    p = a + b - c
-    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
-    if pa <= pb and pa <= pc:
-        return a
-    return b if pb <= pc else c
-
-
 def _png_unfilter(data: bytes, pos: int, rows: int, stride: int, bpp: int):
-    """Undoes the five PNG scanline filters; returns (uint8 [rows, stride], new pos)."""
-    out = np.zeros((rows, stride), np.uint8)
-    prev = np.zeros(stride, np.int32)
-    for y in range(rows):
-        ftype = data[pos]
-        line = np.frombuffer(data, np.uint8, stride, pos + 1).astype(np.int32)
-        pos += 1 + stride
-        if ftype == 0:
-            cur = line
-        elif ftype == 2:
-            cur = (line + prev) & 0xFF
-        elif ftype == 1:  # Sub: a running sum per byte lane of the pixel
-            cur = line.copy()
-            for k in range(min(bpp, stride)):
-                cur[k::bpp] = np.cumsum(line[k::bpp]) & 0xFF
-        elif ftype in (3, 4):  # Average and Paeth depend on the byte just decoded
-            lst = line.tolist()
-            up = prev.tolist()
-            for i in range(stride):
-                a = lst[i - bpp] if i >= bpp else 0
-                if ftype == 3:
-                    lst[i] = (lst[i] + ((a + up[i]) >> 1)) & 0xFF
-                else:
-                    lst[i] = (lst[i] + _paeth(a, up[i], up[i - bpp] if i >= bpp else 0)) & 0xFF
-            cur = np.asarray(lst, np.int32)
-        else:
-            raise VoidrayError(1, f"PNG: unknown filter type {ftype}")
-        out[y] = cur
-        prev = cur
-    return out, pos
+    """Undoes the five PNG scanline filters (native vr_png_unfilter); returns
+    (uint8 [rows, stride], new pos)."""
+    from . import _native as N
+
+    need = rows * (stride + 1)
+    src = np.frombuffer(data, np.uint8, min(need, max(0, len(data) - pos)), pos)
+    out = np.empty((rows, stride), np.uint8)
+    N.check(N.lib().vr_png_unfilter(src.ctypes.data, src.size, rows, stride, bpp, out.ctypes.data))
+    return out, pos + need
 
 
 def _png_samples(rows: np.ndarray, width: int, depth: int, channels: int) -> np.ndarray:

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <future>
@@ -725,6 +726,43 @@ vr_status guarded(const char* what, const std::function<void()>& body) {
 }  // namespace
 
 extern "C" {
+
+vr_status vr_png_unfilter(const uint8_t* data, size_t size, uint32_t rows, uint32_t stride, uint32_t bpp,
+                          uint8_t* out) {
+    if ((!data && size) || (!out && rows && stride) || bpp == 0)
+        return vr::set_error(VR_ERR_INVALID, "vr_png_unfilter: null argument or zero byte distance");
+    if ((uint64_t)rows * ((uint64_t)stride + 1) > size)
+        return vr::set_error(VR_ERR_INVALID, "PNG: image data shorter than its scanlines");
+    const uint8_t* in = data;
+    const uint8_t* up = nullptr;  // previous output row, none above the first
+    for (uint32_t y = 0; y < rows; ++y, in += stride + 1) {
+        const uint8_t type = in[0];
+        const uint8_t* line = in + 1;
+        uint8_t* cur = out + (size_t)y * stride;
+        for (uint32_t i = 0; i < stride; ++i) {
+            const int a = i >= bpp ? cur[i - bpp] : 0;
+            const int b = up ? up[i] : 0;
+            const int c = (up && i >= bpp) ? up[i - bpp] : 0;
+            int pred;
+            switch (type) {
+                case 0: pred = 0; break;
+                case 1: pred = a; break;
+                case 2: pred = b; break;
+                case 3: pred = (a + b) >> 1; break;
+                case 4: {  // Paeth: the neighbour nearest to a + b - c, ties to a then b
+                    const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+                    pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                    break;
+                }
+                default:
+                    return vr::set_error(VR_ERR_INVALID, "PNG: unknown filter type " + std::to_string(type));
+            }
+            cur[i] = (uint8_t)(line[i] + pred);
+        }
+        up = cur;
+    }
+    return VR_OK;
+}
 
 vr_status vr_image_info_get(const uint8_t* data, size_t size, vr_image_info* info) {
     if (!data || !info) return vr::set_error(VR_ERR_INVALID, "vr_image_info_get: null argument");
