@@ -76,6 +76,14 @@ vr_status vr_image_decode_rgb8(const uint8_t* data, size_t size, uint8_t* rgb, s
 vr_status vr_png_unfilter(const uint8_t* data, size_t size, uint32_t rows, uint32_t stride, uint32_t bpp,
                           uint8_t* out);
 
+/* TIFF 6.0 LZW (compression 5): MSB-first codes of 9-12 bits, Clear = 256,
+ * end of information = 257, the code width growing one code early (at 511,
+ * 1023 and 2047 table entries).  Decodes the whole of `src` (to its end of
+ * information or its last whole code), writes the first `capacity` bytes of
+ * the result to `out` and the result's full length to `*length`.  A code
+ * that names no table entry returns VR_ERR_INVALID. */
+vr_status vr_tiff_lzw_decode(const uint8_t* src, size_t size, uint8_t* out, size_t capacity, size_t* length);
+
 /* A parsed OBJ mesh; the arrays belong to the library until vr_obj_free. */
 typedef struct vr_obj_mesh {
     float* positions;      /* 3 * num_vertices                                 */

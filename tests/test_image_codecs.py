@@ -921,3 +921,66 @@ def test_tiff_reference_assets():
     assert np.array_equal(hgt[..., 0], hgt[..., 2])
     # LZW + horizontal predictor decode to whole 8-bit levels
     assert np.array_equal(np.round(alb * 255), alb * np.float32(255.0))
+
+
+def tiff_lzw_decode_restated(src: bytes) -> bytes:
+    """TIFF 6.0 LZW decoded code by code in Python (the library's decoder is
+    native): MSB-first codes of 9-12 bits, Clear = 256, EOI = 257, the code
+    width growing one code early (at 511, 1023 and 2047 table entries)."""
+    out = bytearray()
+    table = [bytes((i,)) for i in range(256)] + [b"", b""]
+    total = len(src) * 8
+    padded = src + b"\0\0\0"
+    nbits, pos, prev = 9, 0, b""
+    while pos + nbits <= total:
+        b = pos >> 3
+        word = (padded[b] << 16) | (padded[b + 1] << 8) | padded[b + 2]
+        code = (word >> (24 - (pos & 7) - nbits)) & ((1 << nbits) - 1)
+        pos += nbits
+        if code == 257:
+            break
+        if code == 256:
+            del table[258:]
+            nbits, prev = 9, b""
+            continue
+        if code < len(table) and code < 256 or code >= 258 and code < len(table):
+            entry = table[code]
+            if prev:
+                table.append(prev + entry[:1])
+        elif code == len(table) and prev:
+            entry = prev + prev[:1]
+            table.append(entry)
+        else:
+            raise VoidrayError(1, f"TIFF: corrupt LZW data (code {code} with {len(table)} table entries)")
+        out += entry
+        prev = entry
+        if len(table) >= (1 << nbits) - 1 and nbits < 12:
+            nbits += 1
+    return bytes(out)
+
+
+def test_native_lzw_matches_the_restatement():
+    """vr_tiff_lzw_decode against the Python restatement: streams from the
+    encoder here (table resets included), truncated streams, and mutated
+    ones, which both decode to the same bytes or both reject."""
+    rng = np.random.default_rng(31)
+    streams = []
+    for n in (1, 100, 5000, 40000):
+        raw = bytes(rng.integers(0, 256, n, dtype=np.uint8)) if n % 2 else bytes(
+            np.cumsum(rng.integers(0, 3, n)).astype(np.uint8))
+        enc = lzw_encode(raw)
+        assert A._tiff_lzw_decode(enc, len(raw)) == raw == tiff_lzw_decode_restated(enc)
+        streams += [enc, enc[:len(enc) // 2]]
+    for it in range(600):
+        b = bytearray(streams[it % len(streams)])
+        for _ in range(rng.integers(0, 4)):
+            b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+        b = bytes(b)
+        try:
+            want = tiff_lzw_decode_restated(b)
+        except VoidrayError:
+            with pytest.raises(VoidrayError, match="corrupt LZW"):
+                A._tiff_lzw_decode(b, 1 << 16)
+            continue
+        assert A._tiff_lzw_decode(b, len(want) + 5) == want
+        assert A._tiff_lzw_decode(b, len(want) // 2) == want[:len(want) // 2]

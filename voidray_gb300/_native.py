@@ -211,6 +211,7 @@ _SIGS = [
     ("vr_image_info_get", C.c_int, [P, C.c_size_t, P]),
     ("vr_image_decode_rgb8", C.c_int, [P, C.c_size_t, P, C.c_size_t]),
     ("vr_png_unfilter", C.c_int, [P, C.c_size_t, C.c_uint32, C.c_uint32, C.c_uint32, P]),
+    ("vr_tiff_lzw_decode", C.c_int, [P, C.c_size_t, P, C.c_size_t, P]),
     ("vr_obj_parse", C.c_int, [P, C.c_size_t, P]),
     ("vr_obj_free", C.c_int, [P]),
 ]

@@ -370,39 +370,18 @@ def _tiff_ifd(data: bytes, bo: str):
     return tags
 
 
-def _tiff_lzw_decode(src: bytes) -> bytes:
-    """TIFF 6.0 LZW: MSB-first codes of 9-12 bits, Clear = 256, EOI = 257, the
-    code width growing one code early (at 511, 1023 and 2047 table entries)."""
-    out = bytearray()
-    table = [bytes((i,)) for i in range(256)] + [b"", b""]
-    total = len(src) * 8
-    padded = src + b"\0\0\0"
-    nbits, pos, prev = 9, 0, b""
-    while pos + nbits <= total:
-        b = pos >> 3
-        word = (padded[b] << 16) | (padded[b + 1] << 8) | padded[b + 2]
-        code = (word >> (24 - (pos & 7) - nbits)) & ((1 << nbits) - 1)
-        pos += nbits
-        if code == 257:
-            break
-        if code == 256:
-            del table[258:]
-            nbits, prev = 9, b""
-            continue
-        if code < len(table) and code < 256 or code >= 258 and code < len(table):
-            entry = table[code]
-            if prev:
-                table.append(prev + entry[:1])
-        elif code == len(table) and prev:
-            entry = prev + prev[:1]
-            table.append(entry)
-        else:
-            raise VoidrayError(1, f"TIFF: corrupt LZW data (code {code} with {len(table)} table entries)")
-        out += entry
-        prev = entry
-        if len(table) >= (1 << nbits) - 1 and nbits < 12:
-            nbits += 1
-    return bytes(out)
+def _tiff_lzw_decode(src: bytes, size: int) -> bytes:
+    """TIFF 6.0 LZW (native vr_tiff_lzw_decode): the first `size` bytes of the
+    decoded stream, fewer when the stream is shorter."""
+    from . import _native as N
+
+    buf = np.frombuffer(src, np.uint8)
+    length = ctypes.c_size_t(0)
+    # the decoded length first, so that a header's claimed size allocates nothing
+    N.check(N.lib().vr_tiff_lzw_decode(buf.ctypes.data, buf.size, None, 0, ctypes.byref(length)))
+    out = np.empty(min(size, length.value), np.uint8)
+    N.check(N.lib().vr_tiff_lzw_decode(buf.ctypes.data, buf.size, out.ctypes.data, out.size, ctypes.byref(length)))
+    return out.tobytes()
 
 
 def _tiff_packbits_decode(src: bytes, size: int) -> bytes:
@@ -426,7 +405,7 @@ def _tiff_chunk(raw: bytes, compression: int, size: int) -> bytes:
     if compression == 1:
         out = raw
     elif compression == 5:
-        out = _tiff_lzw_decode(raw)
+        out = _tiff_lzw_decode(raw, size)
     elif compression in (8, 32946):
         try:
             out = zlib.decompress(raw)

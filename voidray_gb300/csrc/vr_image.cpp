@@ -764,6 +764,78 @@ vr_status vr_png_unfilter(const uint8_t* data, size_t size, uint32_t rows, uint3
     return VR_OK;
 }
 
+vr_status vr_tiff_lzw_decode(const uint8_t* src, size_t size, uint8_t* out, size_t capacity, size_t* length) {
+    if ((!src && size) || (!out && capacity) || !length)
+        return vr::set_error(VR_ERR_INVALID, "vr_tiff_lzw_decode: null argument");
+    // table entries as (prefix code, last byte, first byte, length); codes
+    // below 256 are single bytes, 256 and 257 are the control codes
+    constexpr int kMax = 4096;
+    static thread_local int16_t prefix[kMax];
+    static thread_local uint8_t last[kMax], first[kMax];
+    static thread_local uint16_t len[kMax];
+    for (int c = 0; c < 256; ++c) {
+        prefix[c] = -1;
+        last[c] = first[c] = (uint8_t)c;
+        len[c] = 1;
+    }
+    const uint64_t total = (uint64_t)size * 8;
+    uint64_t pos = 0;
+    int nbits = 9, next = 258, prev = -1;
+    size_t w = 0;
+    auto emit = [&](int code) {
+        const size_t n = len[code];
+        if (w < capacity) {
+            // the entry's bytes from its end back along the prefix chain
+            size_t k = n;
+            for (int c = code; c >= 0; c = prefix[c]) {
+                --k;
+                if (w + k < capacity) out[w + k] = last[c];
+            }
+        }
+        w += n;
+    };
+    while (pos + (uint64_t)nbits <= total) {
+        // nbits (9-12) from the bit position, most significant bit first
+        uint32_t word = 0;
+        const size_t byte = (size_t)(pos >> 3);
+        for (int k = 0; k < 3; ++k) word = (word << 8) | (byte + k < size ? src[byte + k] : 0u);
+        const int code = (int)((word >> (24 - (int)(pos & 7) - nbits)) & ((1u << nbits) - 1));
+        pos += (uint64_t)nbits;
+        if (code == 257) break;
+        if (code == 256) {
+            next = 258;
+            nbits = 9;
+            prev = -1;
+            continue;
+        }
+        if (code < next && (code < 256 || code >= 258)) {
+            if (prev >= 0 && next < kMax) {
+                prefix[next] = (int16_t)prev;
+                last[next] = first[code];
+                first[next] = first[prev];
+                len[next] = (uint16_t)(len[prev] + 1);
+                ++next;
+            }
+            emit(code);
+            prev = code;
+        } else if (code == next && prev >= 0 && next < kMax) {
+            prefix[next] = (int16_t)prev;
+            last[next] = first[prev];
+            first[next] = first[prev];
+            len[next] = (uint16_t)(len[prev] + 1);
+            ++next;
+            emit(code);
+            prev = code;
+        } else {
+            return vr::set_error(VR_ERR_INVALID, "TIFF: corrupt LZW data (code " + std::to_string(code) + " with " +
+                                                     std::to_string(next) + " table entries)");
+        }
+        if (next >= (1 << nbits) - 1 && nbits < 12) ++nbits;
+    }
+    *length = w;
+    return VR_OK;
+}
+
 vr_status vr_image_info_get(const uint8_t* data, size_t size, vr_image_info* info) {
     if (!data || !info) return vr::set_error(VR_ERR_INVALID, "vr_image_info_get: null argument");
     return guarded("vr_image_info_get", [&] {
