@@ -5,7 +5,6 @@
 // resolves its (position, normal, texture) triple to a vertex numbered in
 // order of first use, and the vertex arrays are gathered at the end.
 #include <charconv>
-#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -35,7 +34,7 @@ struct Token {
 
 inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\v' || c == '\f' || c == '\r'; }
 
-// Python-style repr of a token for messages: 'text'.
+// A token quoted for messages: 'text'.
 std::string quoted(const Token& t) { return "'" + t.str() + "'"; }
 
 [[noreturn]] void fail(uint64_t line, const std::string& what) {
