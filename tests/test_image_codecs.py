@@ -529,7 +529,8 @@ def test_jpeg_grey_and_rgb_and_extended_sof(native):
 
 
 @pytest.mark.parametrize("h,w,samp", [(32, 32, ((1, 1), (1, 1), (1, 1))), (45, 70, ((2, 2), (1, 1), (1, 1))),
-                                      (17, 9, ((2, 1), (1, 1), (1, 1)))])
+                                      (17, 9, ((2, 1), (1, 1), (1, 1))),
+                                      (120, 200, ((2, 2), (1, 1), (1, 1)))])  # 26 restart intervals: decoded in parallel
 @pytest.mark.parametrize("restart", [0, 4])
 def test_jpeg_progressive_equals_sequential(native, h, w, samp, restart):
     img = test_image(h, w, seed=w, smooth=False)

@@ -174,7 +174,32 @@ struct Component {
     std::vector<int16_t> coef;  // bw * bh * 64, natural order
     uint16_t q[64] = {};        // latched at the component's first scan
     bool scanned = false;
-    int dc_pred = 0;
+};
+
+// Runs body(begin, end) over [0, n) in pieces on the host's threads (one
+// piece below `grain` items).  The bodies write disjoint outputs.
+template <class F>
+void parallel_for(size_t n, size_t grain, F&& body) {
+    unsigned hw = std::thread::hardware_concurrency();
+    const size_t pieces = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, n / std::max<size_t>(grain, 1)));
+    std::vector<std::future<void>> tasks;
+    for (size_t k = 1; k < pieces; ++k) {
+        const size_t lo = n * k / pieces, hi = n * (k + 1) / pieces;
+        try {
+            tasks.push_back(std::async(std::launch::async, [&body, lo, hi] { body(lo, hi); }));
+        } catch (const std::system_error&) {
+            body(lo, hi);
+        }
+    }
+    body(0, n / pieces);
+    for (auto& t : tasks) t.get();
+}
+
+// Entropy-decoding state that a restart marker resets: the DC predictions of
+// the scan's components and the end-of-band run.
+struct ScanState {
+    int eobrun = 0;
+    int dc_pred[4] = {0, 0, 0, 0};
 };
 
 struct Decoder {
@@ -192,7 +217,6 @@ struct Decoder {
     int restart_interval = 0;
     bool jfif = false, adobe = false;
     int adobe_transform = -1;
-    int eobrun = 0;
     bool header_only = false;
 
     Decoder(const uint8_t* d, size_t n) : data(d), size(n) {}
@@ -366,19 +390,20 @@ struct Decoder {
             const bool need_ac = !progressive || ss > 0;
             if (need_dc && !dc[td[i]].defined) fail(VR_ERR_INVALID, "JPEG: DC Huffman table not defined");
             if (need_ac && !ac[ta[i]].defined) fail(VR_ERR_INVALID, "JPEG: AC Huffman table not defined");
-            c.dc_pred = 0;
         }
         pos = seg_end;
         decode_scan(ns, sc, td, ta, ss, se, ah, al);
     }
 
     // One block of one scan, by scan kind.
-    void block(BitReader& br, Component& c, int16_t* blk, const Huffman& hd, const Huffman& ha, int ss, int se,
-               int ah, int al) {
+    void block(BitReader& br, ScanState& st, int slot, int16_t* blk, const Huffman& hd, const Huffman& ha, int ss,
+               int se, int ah, int al) const {
+        int& dc_pred = st.dc_pred[slot];
+        int& eobrun = st.eobrun;
         if (!progressive) {
             const int t = br.decode(hd);
-            c.dc_pred += br.receive_extend(t);
-            blk[0] = int16_t(c.dc_pred);
+            dc_pred += br.receive_extend(t);
+            blk[0] = int16_t(dc_pred);
             for (int k = 1; k < 64;) {
                 const int rs = br.decode(ha);
                 const int r = rs >> 4, s = rs & 15;
@@ -397,8 +422,8 @@ struct Decoder {
         if (ss == 0) {  // DC scans (G.1.2.1)
             if (ah == 0) {
                 const int t = br.decode(hd);
-                c.dc_pred += br.receive_extend(t);
-                blk[0] = int16_t(c.dc_pred * (1 << al));
+                dc_pred += br.receive_extend(t);
+                blk[0] = int16_t(dc_pred * (1 << al));
             } else if (br.bit()) {
                 blk[0] = int16_t(blk[0] | (1 << al));
             }
@@ -468,19 +493,101 @@ struct Decoder {
         }
     }
 
+    // Decodes units [u0, u1) of a scan (MCUs of an interleaved scan, blocks of
+    // a single-component one) from `br`; restart markers are not handled here.
+    void decode_units(BitReader& br, ScanState& st, long u0, long u1, int ns, Component** sc, const int* td,
+                      const int* ta, int ss, int se, int ah, int al) const {
+        const int ux = (sc[0]->cw + 7) / 8;
+        for (long u = u0; u < u1; ++u) {
+            if (ns == 1) {
+                Component& c = *sc[0];
+                const long by = u / ux, bx = u % ux;
+                block(br, st, 0, c.coef.data() + (size_t(by) * c.bw + bx) * 64, dc[td[0]], ac[ta[0]], ss, se, ah, al);
+            } else {
+                const long my = u / mcux, mx = u % mcux;
+                for (int i = 0; i < ns; ++i) {
+                    Component& c = *sc[i];
+                    for (int v = 0; v < c.v; ++v)
+                        for (int h = 0; h < c.h; ++h) {
+                            const size_t by = size_t(my) * c.v + v, bx = size_t(mx) * c.h + h;
+                            block(br, st, i, c.coef.data() + (by * c.bw + bx) * 64, dc[td[i]], ac[ta[i]], ss, se,
+                                  ah, al);
+                        }
+                }
+            }
+            if (br.overrun) fail(VR_ERR_INVALID, "JPEG: entropy-coded data truncated");
+        }
+    }
+
+    // With many restart intervals the intervals decode on separate threads:
+    // each starts after its RST marker with fresh predictions, and writes its
+    // own blocks.  Returns false, having decoded nothing, when the markers do
+    // not split the scan into the expected intervals (the serial path then
+    // reports what is wrong).
+    bool decode_intervals_parallel(long units, int ns, Component** sc, const int* td, const int* ta, int ss, int se,
+                                   int ah, int al) {
+        const long R = restart_interval;
+        const long intervals = (units + R - 1) / R;
+        std::vector<const uint8_t*> seg{data + pos};
+        const uint8_t* q = data + pos;
+        const uint8_t* end = data + size;
+        while (q + 1 < end) {
+            if (q[0] != 0xFF) {
+                ++q;
+                continue;
+            }
+            const uint8_t m = q[1];
+            if (m == 0x00) {
+                q += 2;
+            } else if (m == 0xFF) {
+                ++q;  // fill byte
+            } else if (m >= 0xD0 && m <= 0xD7) {
+                seg.push_back(q + 2);
+                q += 2;
+            } else {
+                break;  // the marker after the scan
+            }
+        }
+        if (q + 1 >= end || (long)seg.size() < intervals) return false;
+        std::vector<std::string> err(intervals);
+        std::vector<vr_status> code(intervals, VR_OK);
+        parallel_for(size_t(intervals), 4, [&](size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1; ++k) {
+                try {
+                    BitReader br;
+                    br.reset(seg[k], end);
+                    ScanState st;
+                    decode_units(br, st, long(k) * R, std::min(units, long(k + 1) * R), ns, sc, td, ta, ss, se, ah,
+                                 al);
+                    // every byte of the interval consumed: its RST marker is next
+                    br.fill();
+                    if (long(k) + 1 < intervals && !br.at_marker) fail(VR_ERR_INVALID, "JPEG: restart marker missing");
+                } catch (const JpegError& e) {
+                    code[k] = e.status;
+                    err[k] = e.message;
+                }
+            }
+        });
+        for (long k = 0; k < intervals; ++k)
+            if (code[k] != VR_OK) fail(code[k], err[k]);
+        pos = size_t(q - data);
+        return true;
+    }
+
     void decode_scan(int ns, Component** sc, const int* td, const int* ta, int ss, int se, int ah, int al) {
-        BitReader br;
-        br.reset(data + pos, data + size);
-        eobrun = 0;
         long units;  // MCUs of an interleaved scan, blocks of a single-component one
-        int ux = 0;
         if (ns == 1) {
-            ux = (sc[0]->cw + 7) / 8;
-            units = long(ux) * ((sc[0]->ch + 7) / 8);
+            units = long((sc[0]->cw + 7) / 8) * ((sc[0]->ch + 7) / 8);
         } else {
             units = long(mcux) * mcuy;
         }
-        for (long u = 0; u < units; ++u) {
+        if (restart_interval && (units + restart_interval - 1) / restart_interval >= 8 &&
+            decode_intervals_parallel(units, ns, sc, td, ta, ss, se, ah, al))
+            return;
+        BitReader br;
+        br.reset(data + pos, data + size);
+        ScanState st;
+        for (long u = 0; u < units;) {
             if (restart_interval && u > 0 && u % restart_interval == 0) {
                 // byte-align, expect RSTn, reset predictions and the EOB run
                 br.fill();
@@ -489,27 +596,11 @@ struct Decoder {
                 if (!br.at_marker || mp + 1 >= br.end || mp[1] < 0xD0 || mp[1] > 0xD7)
                     fail(VR_ERR_INVALID, "JPEG: restart marker missing");
                 br.reset(mp + 2, data + size);
-                for (int i = 0; i < ns; ++i) sc[i]->dc_pred = 0;
-                eobrun = 0;
+                st = ScanState();
             }
-            if (ns == 1) {
-                Component& c = *sc[0];
-                const long by = u / ux, bx = u % ux;
-                int16_t* blk = c.coef.data() + (size_t(by) * c.bw + bx) * 64;
-                block(br, c, blk, dc[td[0]], ac[ta[0]], ss, se, ah, al);
-            } else {
-                const long my = u / mcux, mx = u % mcux;
-                for (int i = 0; i < ns; ++i) {
-                    Component& c = *sc[i];
-                    for (int v = 0; v < c.v; ++v)
-                        for (int h = 0; h < c.h; ++h) {
-                            const size_t by = size_t(my) * c.v + v, bx = size_t(mx) * c.h + h;
-                            block(br, c, c.coef.data() + (by * c.bw + bx) * 64, dc[td[i]], ac[ta[i]], ss, se, ah,
-                                  al);
-                        }
-                }
-            }
-            if (br.overrun) fail(VR_ERR_INVALID, "JPEG: entropy-coded data truncated");
+            const long u1 = restart_interval ? std::min(units, (u / restart_interval + 1) * restart_interval) : units;
+            decode_units(br, st, u, u1, ns, sc, td, ta, ss, se, ah, al);
+            u = u1;
         }
         // continue at the next marker after the scan's data
         const uint8_t* q = br.p;
@@ -635,25 +726,6 @@ void ycc_to_rgb(uint8_t y, uint8_t cb, uint8_t cr, uint8_t* rgb) {
     rgb[0] = clamp_u8(Y + 1.402f * Cr);
     rgb[1] = clamp_u8(Y - 0.344136f * Cb - 0.714136f * Cr);
     rgb[2] = clamp_u8(Y + 1.772f * Cb);
-}
-
-// Runs body(begin, end) over [0, n) in pieces on the host's threads (one
-// piece below `grain` items).  The bodies write disjoint outputs.
-template <class F>
-void parallel_for(size_t n, size_t grain, F&& body) {
-    unsigned hw = std::thread::hardware_concurrency();
-    const size_t pieces = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, n / std::max<size_t>(grain, 1)));
-    std::vector<std::future<void>> tasks;
-    for (size_t k = 1; k < pieces; ++k) {
-        const size_t lo = n * k / pieces, hi = n * (k + 1) / pieces;
-        try {
-            tasks.push_back(std::async(std::launch::async, [&body, lo, hi] { body(lo, hi); }));
-        } catch (const std::system_error&) {
-            body(lo, hi);
-        }
-    }
-    body(0, n / pieces);
-    for (auto& t : tasks) t.get();
 }
 
 void decode_pixels(Decoder& d, uint8_t* rgb) {
