@@ -441,7 +441,36 @@ void set_camera(SceneView& v, const vr_camera_desc& c) {
     v.c_focal = c.has_dof ? dot(load3(c.focal_point) - eye, dir) : 0.0f;
 }
 
+namespace {
+vr_status build_host_scene_impl(const vr_scene_desc* d, HostScene& hs, std::string& err);
+vr_status validate_host_scene_impl(const HostScene& hs, std::string& err);
+
+// Nothing thrown below (a host allocation failing, a worker thread's
+// exception passed on by its future) crosses the C ABI: it becomes a status.
+template <class F>
+vr_status guarded(std::string& err, F&& body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        err = "host allocation failed while lowering the scene";
+        return VR_ERR_OOM;
+    } catch (const std::exception& e) {
+        err = std::string("scene lowering failed: ") + e.what();
+        return VR_ERR_INVALID;
+    }
+}
+}  // namespace
+
 vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& err) {
+    return guarded(err, [&] { return build_host_scene_impl(d, hs, err); });
+}
+
+vr_status validate_host_scene(const HostScene& hs, std::string& err) {
+    return guarded(err, [&] { return validate_host_scene_impl(hs, err); });
+}
+
+namespace {
+vr_status build_host_scene_impl(const vr_scene_desc* d, HostScene& hs, std::string& err) {
     auto t0 = std::chrono::steady_clock::now();
     if (!d) { err = "null scene descriptor"; return VR_ERR_INVALID; }
     if (d->num_meshes && !d->meshes) { err = "meshes is NULL"; return VR_ERR_INVALID; }
@@ -748,7 +777,7 @@ vr_status build_host_scene(const vr_scene_desc* d, HostScene& hs, std::string& e
     return VR_OK;
 }
 
-vr_status validate_host_scene(const HostScene& hs, std::string& err) {
+vr_status validate_host_scene_impl(const HostScene& hs, std::string& err) {
     const uint64_t np = hs.num_prims;
     if (np == 0) return hs.nodes.empty() ? VR_OK : (err = "nodes without triangles", VR_ERR_INVALID);
     const uint64_t nn = hs.nodes.size() / 4;
@@ -829,5 +858,6 @@ vr_status validate_host_scene(const HostScene& hs, std::string& err) {
         if (seen[p] != 1) { err = "triangle " + std::to_string(p) + " appears " + std::to_string(seen[p]) + " times"; return VR_ERR_INVALID; }
     return VR_OK;
 }
+}  // namespace
 
 }  // namespace vr
