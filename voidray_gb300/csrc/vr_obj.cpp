@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <system_error>
 #include <vector>
@@ -260,6 +261,8 @@ vr_status vr_obj_parse(const char* text, size_t size, vr_obj_mesh* mesh) {
         return vr::set_error(VR_ERR_INVALID, e.message);
     } catch (const std::bad_alloc&) {
         return vr::set_error(VR_ERR_OOM, "vr_obj_parse: host allocation failed");
+    } catch (const std::exception& e) {
+        return vr::set_error(VR_ERR_INVALID, std::string("vr_obj_parse: ") + e.what());
     }
 }
 
