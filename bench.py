@@ -33,7 +33,6 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
-# DRAM bytes per k_extend launch at the default workload (ncu capture summarised in profiles/)
 K_EXTEND_DRAM_BYTES_PER_LAUNCH = 2.374e9
 sys.path.insert(0, str(ROOT))
 

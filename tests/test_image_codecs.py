@@ -28,7 +28,9 @@ ZZ = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 2
 _U = np.arange(8)
 DCT = np.array([[(np.sqrt(0.5) if u == 0 else 1.0) * 0.5 * np.cos((2 * x + 1) * u * np.pi / 16) for x in _U]
                 for u in _U])  # DCT[u, x]
-ASSETS = Path(os.environ.get("VOIDRAY_REFERENCE", "/root/reference")) / "assets"
+# the reference checkout, when the environment names one (VOIDRAY_REFERENCE); otherwise these tests skip
+_REF_ROOT = os.environ.get("VOIDRAY_REFERENCE", "")
+ASSETS = Path(_REF_ROOT) / "assets" if _REF_ROOT else Path("/nonexistent-voidray-assets")
 
 
 # ------------------------------------------------------------ JPEG encoder ---
