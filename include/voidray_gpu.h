@@ -282,19 +282,28 @@ vr_status vr_render_aov_device(vr_scene* scene, const vr_render_settings* settin
                                uint64_t seed, uint32_t first_sample, void* stream);
 
 /* Same render as vr_render_device, for callers that cannot allocate device
- * memory while they render (inside a CUDA stream capture, a real-time frame
- * loop with a fixed memory budget, a host callback).  No counterpart in the
- * reference.  It calls no cudaMalloc/cudaFree: the wavefront scratch (ray
- * queues, path state, per-pixel sums) lives in one device array of
- * VR_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads
- * the library holds until the process exits.  The image must fit in it: 16
- * bytes per pixel plus room for at least 1024 paths (about 4 Mpixels);
- * larger images are rejected with VR_ERR_UNSUPPORTED, and the wavefront is
- * sized to what remains.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
- * share the one array, so calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller.  The scene must
- * have been created beforehand with vr_scene_create. */
+ * memory while they render.  No counterpart in the reference.  Such callers
+ * are, for example, a host application (a game engine, a compositor, a
+ * framework with its own caching allocator) that has already reserved the
+ * GPU's memory for its own pool, so a cudaMalloc from the library would fail
+ * or evict its data; and a real-time frame loop that cannot afford the
+ * device-wide synchronisation that cudaFree implies, nor an allocation that
+ * fails in the middle of a frame.  vr_render_device grows a per-scene scratch
+ * with cudaMalloc when an image or wavefront needs more; this entry point
+ * calls no cudaMalloc, cudaFree or allocating library routine.  Its wavefront
+ * scratch (ray queues, path state, per-pixel sums) lives in one device array
+ * of VR_NOALLOC_SCRATCH_BYTES (64 MiB) inside the library, which every GPU
+ * that loads the library holds until the process exits.  The image must fit
+ * in it: 16 bytes per pixel plus room for at least 1024 paths (about 4
+ * Mpixels, e.g. 2000x2000); larger images are rejected with
+ * VR_ERR_UNSUPPORTED before anything is launched, and the wavefront is sized
+ * to what remains.  The first call on each device looks up the array's
+ * device address with that device current (a one-time set-up); make that
+ * first call before any stream capture.  All calls share the one array and
+ * it keeps the last call's contents (the pixel sums are cleared by every
+ * call), so calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller.  The scene must have been
+ * created beforehand with vr_scene_create, which allocates its own memory. */
 #define VR_NOALLOC_SCRATCH_BYTES (64u << 20)
 vr_status vr_render_device_noalloc(vr_scene* scene, const vr_render_settings* settings,
                                    uint32_t samples, float* rgba_device, uint32_t width,

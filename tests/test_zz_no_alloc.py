@@ -1,14 +1,17 @@
 """vr_render_device_noalloc: the render entry point for callers that cannot
 allocate device memory while they render.
 
-A renderer recording its frame into a CUDA graph (stream capture forbids
-cudaMalloc), a real-time loop that must not stall on allocation, or a host
-callback cannot let the library grow its scratch with cudaMalloc.  This entry
-point takes its scratch from a fixed device array inside the library instead.
-The test renders through the C ABI with both entry points and requires the
-same pixels, on two no-alloc calls in a row (different scenes, sizes and
-estimators, so the second call runs on scratch the first one left behind),
-and checks that an image too large for the fixed array is refused.
+A host application that has reserved the GPU's memory for its own pool (a
+game engine, a compositor, a framework with a caching allocator) cannot let
+the library cudaMalloc more scratch, and a real-time frame loop cannot take
+the device-wide synchronisation of cudaFree or an allocation failure in the
+middle of a frame.  This entry point takes its scratch from a fixed device
+array inside the library instead.  The tests render through the C ABI with
+both entry points and require the same pixels: on two no-alloc calls in a row
+(different scenes, sizes and estimators, so the second call runs on scratch
+the first one left behind), on a render cut into many small wavefronts, and
+on an image close to the size limit; and they check that an image too large
+for the fixed array is refused.
 
 This file is named to be collected last: a failure here leaves every other
 test already run.
@@ -77,7 +80,35 @@ def test_noalloc_rejects_oversize_image(gpu):
     import torch
 
     w = h = 4096  # 16.7 Mpixels x 16 bytes exceeds the fixed scratch; refused before any launch
-    small = torch.zeros(16, dtype=torch.float32, device="cuda")
-    status = vr.lib().vr_render_device_noalloc(acc.handle, C.byref(cst), 1, small.data_ptr(), w, h, 0, 0, None)
+    # a full-size output buffer, so that even a regressed size check would write in bounds
+    out = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    status = vr.lib().vr_render_device_noalloc(acc.handle, C.byref(cst), 1, out.data_ptr(), w, h, 0, 0, None)
+    torch.cuda.synchronize()
     assert status == 2, vr.lib().vr_last_error()
     assert b"no-alloc scratch" in vr.lib().vr_last_error()
+    assert not bool(out.any()), "a refused call wrote to the output"
+    del out
+
+
+def test_noalloc_many_waves_and_near_limit(gpu):
+    """Per-path arrays and queue counters reused across many wavefronts inside
+    the fixed array, and the wavefront sized from what a 4-Mpixel image
+    leaves of it: both bit-identical to vr_render_device."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+
+    scene, st = W.cornell_box(rr_depth=3)
+    acc = scene.build_acceleration()
+    # 64x48 x 4 spp in wavefronts of 1024 paths: 12 waves
+    st.wavefront_paths = 1024
+    ref = _render(vr, acc, st, 4, 64, 48, 11, noalloc=False)
+    got = _render(vr, acc, st, 4, 64, 48, 11, noalloc=True)
+    assert np.array_equal(got, ref)
+    # 2000x2000 at 1 spp: 64 MB of pixel sums leave room for a few thousand
+    # paths per wavefront, so the frame runs as several hundred waves
+    st.wavefront_paths = 0
+    st.max_bounces = 4
+    ref = _render(vr, acc, st, 1, 2000, 2000, 12, noalloc=False)
+    got = _render(vr, acc, st, 1, 2000, 2000, 12, noalloc=True)
+    assert np.array_equal(got, ref)
+    assert np.isfinite(got).all() and got[..., :3].mean() > 0.0

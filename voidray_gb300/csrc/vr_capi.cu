@@ -14,6 +14,8 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -1111,13 +1113,14 @@ vr_status vr_relmse_device(const float* a, float sa, const float* ref, float sr,
 // ---------------------------------------------------------------------------
 // Render without device allocation (no counterpart in the reference).
 //
-// Callers that cannot call cudaMalloc while they render -- a CUDA stream
-// capture in progress, a real-time frame loop with a fixed memory budget, a
-// host callback -- use vr_render_device_noalloc.  Its wavefront scratch (ray
-// queues, path state, per-pixel sums) lives in this file-scope device array
-// of VR_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
-// until the process exits.  The scene itself is still built, and its memory
-// allocated, by vr_scene_create beforehand.
+// Callers that cannot call cudaMalloc while they render -- a host application
+// that has reserved the GPU's memory for its own pool, a real-time frame loop
+// that cannot take cudaFree's device-wide synchronisation or an allocation
+// failure mid-frame -- use vr_render_device_noalloc.  Its wavefront scratch
+// (ray queues, path state, per-pixel sums) lives in this file-scope device
+// array of VR_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library
+// holds until the process exits.  The scene itself is still built, and its
+// memory allocated, by vr_scene_create beforehand.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -1147,12 +1150,8 @@ vr_status noalloc_scratch(void** out) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-}  // namespace
-
-extern "C" {
-
-vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba,
-                                   uint32_t w, uint32_t h, uint64_t seed, uint32_t first_sample, void* stream) {
+vr_status render_device_noalloc(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba,
+                                uint32_t w, uint32_t h, uint64_t seed, uint32_t first_sample, void* stream) {
     vr_status r = validate_render(s, st, w, h);
     if (r != VR_OK) return r;
     if (!rgba) return fail(VR_ERR_INVALID, "rgba is NULL");
@@ -1215,6 +1214,23 @@ vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, ui
     VR_CK(cudaMemsetAsync(psum, 0, (size_t)np * sizeof(float4), cs));
     std::vector<HostJob> jobs{make_job(s->view, st, samples, rgba, w, h, seed, first_sample, psum)};
     return run_waves(jobs, ps, (uint32_t)cap, table, table_entries, s->status, s->totals, nullptr, cs, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+// The planner's host vectors and the error strings may throw; nothing crosses
+// the C ABI as an exception.
+vr_status vr_render_device_noalloc(vr_scene* s, const vr_render_settings* st, uint32_t samples, float* rgba,
+                                   uint32_t w, uint32_t h, uint64_t seed, uint32_t first_sample, void* stream) {
+    try {
+        return render_device_noalloc(s, st, samples, rgba, w, h, seed, first_sample, stream);
+    } catch (const std::bad_alloc&) {
+        return fail(VR_ERR_OOM, "host allocation failed in vr_render_device_noalloc");
+    } catch (const std::exception& e) {
+        return fail(VR_ERR_INVALID, std::string("vr_render_device_noalloc: ") + e.what());
+    }
 }
 
 }  // extern "C"
