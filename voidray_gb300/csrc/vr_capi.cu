@@ -381,6 +381,14 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
                 e.g0 = j.done;
                 e.paths = take;
                 e.base = cap - left;
+                {  // slot order (vr::Job::head): partial row, full rows pixel-major, partial row
+                    const uint64_t np = e.num_pixels;
+                    const uint64_t head = std::min<uint64_t>((np - e.g0 % np) % np, take);
+                    e.head = (uint32_t)head;
+                    e.rows = (uint32_t)((take - head) / np);
+                    e.row0 = (uint32_t)((e.g0 + head) / np);
+                    e.pad_ = 0;
+                }
                 chunk.push_back(e);
                 entry_job.push_back(i);
                 wh.njobs++;
@@ -682,6 +690,7 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
     uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
     if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
+    if (cap > np) cap -= cap % np;  // whole sample rows per wavefront: every slot in pixel-major order
     const uint32_t att_depth = st->estimator == VR_EST_REFERENCE ? st->max_bounces : 0;
     if ((r = s->eng.ensure((uint32_t)cap, att_depth, s->stream)) != VR_OK) return r;
     if (s->psum_cap < np) {
@@ -719,6 +728,7 @@ vr_status vr_render_aov_device(vr_scene* s, const vr_render_settings* st, uint32
     uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
     if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
+    if (cap > np) cap -= cap % np;  // whole sample rows per wavefront
     const uint32_t att_depth = st->estimator == VR_EST_REFERENCE ? st->max_bounces : 0;
     if ((r = s->eng.ensure((uint32_t)cap, att_depth, s->stream, true)) != VR_OK) return r;
     if (s->psum_cap < np) {

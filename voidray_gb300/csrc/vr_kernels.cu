@@ -376,8 +376,34 @@ __device__ bool scatter(const Material& m, V3 ro, V3 rd, const SurfHit& hit, Rng
 // Path slot p of job r is its global sample-major path g = g0 + (p - base):
 // pixel = g % num_pixels, sample = first_sample + g / num_pixels.
 // ----------------------------------------------------------------------------
+// Tiled pixel order: rows of 8x8 tiles, row-major inside a tile (the last
+// tile row and column may be narrower); a bijection of [0, W*H).
+constexpr uint32_t PIX_TILE = 8;
+__device__ __forceinline__ uint32_t tiled_index(uint32_t x, uint32_t y, uint32_t W, uint32_t H) {
+    const uint32_t R = y / PIX_TILE, th = min(PIX_TILE, H - R * PIX_TILE);
+    const uint32_t b = x / PIX_TILE, bw = min(PIX_TILE, W - b * PIX_TILE);
+    return R * PIX_TILE * W + b * PIX_TILE * th + (y - R * PIX_TILE) * bw + (x - b * PIX_TILE);
+}
+__device__ __forceinline__ uint32_t tiled_pixel(uint32_t P, uint32_t W, uint32_t H) {
+    const uint32_t R = P / (PIX_TILE * W), rem = P - R * PIX_TILE * W;
+    const uint32_t th = min(PIX_TILE, H - R * PIX_TILE);
+    const uint32_t b = rem / (PIX_TILE * th), rem2 = rem - b * PIX_TILE * th;
+    const uint32_t bw = min(PIX_TILE, W - b * PIX_TILE);
+    const uint32_t yy = rem2 / bw;
+    return (R * PIX_TILE + yy) * W + b * PIX_TILE + (rem2 - yy * bw);
+}
+
+// (pixel, sample) of the path in slot p (see Job::head for the slot order).
 __device__ __forceinline__ void path_coords(const Job& j, uint32_t p, uint32_t& pixel, uint32_t& sample) {
-    const uint64_t g = j.g0 + (p - j.base);
+    const uint32_t o = p - j.base;
+    if (o >= j.head && o - j.head < j.rows * j.num_pixels) {
+        const uint32_t om = o - j.head;
+        const uint32_t P = om / j.rows;
+        pixel = tiled_pixel(P, j.width, j.height);
+        sample = j.first_sample + j.row0 + (om - P * j.rows);
+        return;
+    }
+    const uint64_t g = j.g0 + o;
     pixel = (uint32_t)(g % j.num_pixels);
     sample = j.first_sample + (uint32_t)(g / j.num_pixels);
 }
@@ -858,14 +884,22 @@ __global__ void k_accumulate(Wave w, PathState ps) {
     const Job& j = ONE ? w.first : w.jobs[blockIdx.y];
     const uint32_t NP = j.num_pixels;
     const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t mid = j.rows * NP;
     for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < NP; px += stride) {
-        // global indices g = s*NP + px inside [g0, g0 + paths)
+        // global indices g = s*NP + px inside [g0, g0 + paths), s in [s_begin, s_end)
         const uint64_t g0 = j.g0, g1 = j.g0 + j.paths;
         const uint64_t s_begin = (g0 > px) ? (g0 - px + NP - 1) / NP : 0;
-        if (s_begin * NP + px >= g1) continue;
+        const uint64_t s_end = (g1 > px) ? (g1 - px + NP - 1) / NP : 0;
+        if (s_begin >= s_end) continue;
+        const uint32_t tp = j.rows ? tiled_index(px % j.width, px / j.width, j.width, j.height) : 0u;
+        // slot of sample row s of this pixel (Job::head)
+        auto slot = [&](uint64_t s) -> uint32_t {
+            const uint32_t o = (uint32_t)(s * NP + px - g0);
+            return j.base + ((o >= j.head && o - j.head < mid) ? j.head + tp * j.rows + (uint32_t)(s - j.row0) : o);
+        };
         float4 acc = j.psum[px];
-        for (uint64_t g = s_begin * NP + px; g < g1; g += NP) {
-            const float4 rr = ps.rad[j.base + (uint32_t)(g - g0)];
+        for (uint64_t s = s_begin; s < s_end; ++s) {
+            const float4 rr = ps.rad[slot(s)];
             acc.x = acc.x + rr.x;
             acc.y = acc.y + rr.y;
             acc.z = acc.z + rr.z;
@@ -873,8 +907,8 @@ __global__ void k_accumulate(Wave w, PathState ps) {
         j.psum[px] = acc;
         if (j.aov_psum) {
             float4 aa = j.aov_psum[px], an = j.aov_psum[NP + px];
-            for (uint64_t g = s_begin * NP + px; g < g1; g += NP) {
-                const uint32_t q = j.base + (uint32_t)(g - g0);
+            for (uint64_t s = s_begin; s < s_end; ++s) {
+                const uint32_t q = slot(s);
                 const float4 a = ps.aov[q], nn = ps.aov[ps.cap + q];
                 aa.x += a.x;
                 aa.y += a.y;

@@ -26,6 +26,14 @@ struct Job {
     uint32_t paths;         // paths of the job in this wave
     uint32_t base;          // first slot of the job's segment in every per-path array
     uint32_t num_pixels, width, height, first_sample;
+    // Slot order of the job's paths in this wave.  Its global paths
+    // [g0, g0 + paths) are `head` paths that finish a partly rendered sample
+    // row, then `rows` full sample rows (row0 = the first of them), then the
+    // start of the next row.  Head and tail keep the global order; the full
+    // rows are stored pixel-major in tiled pixel order (slot head + P * rows + s
+    // holds row row0 + s of tiled pixel P), so that a warp's rays and the
+    // warps fetched after it start from the same few pixels.
+    uint32_t head, rows, row0, pad_;
     float4* psum;           // per-pixel running sums (float4 per pixel)
     float4* aov_psum;       // optional: first-hit albedo sums [0, np), normal sums [np, 2 np)
 };
