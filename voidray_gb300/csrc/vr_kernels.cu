@@ -572,6 +572,12 @@ __device__ __forceinline__ void rad_add(const PathState& ps, uint32_t p, V3 c) {
     ps.rad[p] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
 }
 
+// Direction octant (sign bits of x, y, z).
+__device__ __forceinline__ uint32_t octant(V3 d) {
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+constexpr uint32_t BIN_JOBS = 8;  // jobs per shade block that are appended in (job, octant) runs
+
 // Appends the active lanes with `want` to job r's queue segment: one atomic
 // per group of lanes of the same job; returns this lane's slot in the segment.
 __device__ __forceinline__ uint32_t queue_append(bool want, uint32_t r, uint32_t* counter_of_job, uint32_t lane) {
@@ -792,16 +798,59 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
             const uint32_t gone = __ballot_sync(0xffffffffu, i < n && !cont);
             if (lane == 0 && gone) atomicAdd(retired, (unsigned long long)__popc(gone));
         }
-        // warp-aggregated compaction into the job's next queue segment and shadow segment
+        // Compaction into the job's next queue segment and shadow segment.  The
+        // block appends its rays in runs of equal (job, direction octant): the
+        // block covers a few neighbouring pixels (pixel-major slots), so a
+        // warp of the next traversal gets rays from one small region heading
+        // into one octant, which visit the same nodes in the same order.
+        // Blocks spanning more than BIN_JOBS jobs append per warp instead.
         const uint32_t base_r = (ONE || i >= n) ? 0u : w.jobs[r].base;
-        const uint32_t cs = queue_append(cont, r, &ps.counts[r * JOB_COUNTERS + k + 1], lane);
+        __shared__ uint32_t s_cnt[2][BIN_JOBS * 8];
+        __shared__ uint32_t s_base[2][BIN_JOBS];
+        __shared__ uint32_t s_rlo, s_nj;
+        if (threadIdx.x == 0) {
+            const uint32_t last = min(i0 + blockDim.x, n) - 1u;
+            const uint32_t rlo = ONE ? 0u : find_job(pre, w.njobs, i0);
+            s_rlo = rlo;
+            s_nj = (ONE ? 0u : find_job(pre, w.njobs, last)) - rlo + 1u;
+        }
+        for (uint32_t t = threadIdx.x; t < 2 * BIN_JOBS * 8; t += blockDim.x) (&s_cnt[0][0])[t] = 0u;
+        __syncthreads();
+        uint32_t cs = 0, ss = 0;
+        if (s_nj <= BIN_JOBS) {
+            const uint32_t jl = r - s_rlo;
+            const uint32_t ke = jl * 8 + (cont ? octant(new_d) : 0u);
+            const uint32_t ks = jl * 8 + (want_shadow ? octant(sh_dir) : 0u);
+            if (cont) cs = atomicAdd(&s_cnt[0][ke], 1u);
+            if (want_shadow) ss = atomicAdd(&s_cnt[1][ks], 1u);
+            __syncthreads();
+            const uint32_t nj = s_nj;
+            if (threadIdx.x < 2 * nj) {  // one thread per (queue, job): bin offsets and one global atomic
+                const uint32_t qsel = threadIdx.x / nj, jj = threadIdx.x - qsel * nj;
+                uint32_t* c = &s_cnt[qsel][jj * 8];
+                uint32_t tot = 0;
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t v = c[b];
+                    c[b] = tot;
+                    tot += v;
+                }
+                const uint32_t ctr = (s_rlo + jj) * JOB_COUNTERS + (qsel ? MAX_DEPTH_SLOTS + k : k + 1);
+                s_base[qsel][jj] = tot ? atomicAdd(&ps.counts[ctr], tot) : 0u;
+            }
+            __syncthreads();
+            if (cont) cs += s_base[0][jl] + s_cnt[0][ke];
+            if (want_shadow) ss += s_base[1][jl] + s_cnt[1][ks];
+        } else {
+            cs = queue_append(cont, r, &ps.counts[r * JOB_COUNTERS + k + 1], lane);
+            ss = queue_append(want_shadow, r, &ps.counts[r * JOB_COUNTERS + MAX_DEPTH_SLOTS + k], lane);
+        }
+        __syncthreads();  // s_cnt is cleared again by the next iteration
         if (cont) {
             const uint32_t q = out_half + base_r + cs;
             ps.q_org[q] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
             ps.q_dir[q] = make_float4(new_d.x, new_d.y, new_d.z, INF_F);
             ps.q_path[q] = p;
         }
-        const uint32_t ss = queue_append(want_shadow, r, &ps.counts[r * JOB_COUNTERS + MAX_DEPTH_SLOTS + k], lane);
         if (want_shadow) {
             const uint32_t q = base_r + ss;
             ps.s_org[q] = make_float4(new_o.x, new_o.y, new_o.z, SCENE_TMIN);
