@@ -62,6 +62,15 @@ def parse_args():
     ap.add_argument("--serve-size", type=int, default=256, help="job image side")
     ap.add_argument("--serve-target", type=float, default=1e-3, help="target relMSE")
     ap.add_argument("--serve-streams", type=int, default=2, help="render streams of the served modes")
+    ap.add_argument("--serve-large-jobs", type=int, default=16,
+                    help="requests of the 1920x1080, 2M-triangle serving run (0 = skip)")
+    ap.add_argument("--no-isect", action="store_true", help="skip the intersection microbenchmark")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched workload")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=2, help="timed steps of the batched workload")
+    ap.add_argument("--isect-tris", type=int, default=1_000_000)
+    ap.add_argument("--isect-rays", type=int, default=16_777_216)
+    ap.add_argument("--isect-reps", type=int, default=5, help="timed launches per query kind")
     return ap.parse_args()
 
 
@@ -163,95 +172,291 @@ def cpu_baseline(scene, st, args, budget_s):
             "mrays_per_s": (int(rays[0]) + int(rays[1])) / dt / 1e6}
 
 
-def serving_benchmark(args):
-    """Poisson stream of render jobs drawn like the plain render scene (four
-    resident displaced icospheres of 18k-800k triangles with the sky HDRI),
-    each to a target relative MSE (estimated from the job's two half-buffers
-    without a reference, checked against a 4096-spp reference after the run).
-    plain: the requests rendered one at a time (one active job, the plain
-    single-scene GPU path); served: continuous batching of every admitted job
-    in one launch per pass; served_denoised: the same with AOVs and the
-    learned denoiser, each job returning the plain mean or the denoised blend,
-    whichever is predicted to be better."""
+def timed_on(stream, fn, reps):
+    """Mean ms of `reps` calls of fn() enqueued on `stream`, CUDA events on that stream."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def intersection_benchmark(args, hbm_peak, peak_source):
+    """The intersection microbenchmark: a soup of 1,000,000 triangles (centres
+    uniform in [0,1]^3, vertex offsets N(0, 0.01^2), seed 1) in the SAH BVH and
+    16,777,216 rays (half pinhole rays from z=-1 over 4096x2048, half with
+    origins uniform in the cube and directions uniform on the sphere, tmax
+    inf), closest hit and any hit through vr_intersect_device.  Rays (537 MB)
+    and hits (268 MB) are larger than L2.  The CPU leg runs the oracle's
+    restatement of SceneAcceleration::hit (median BVH, both children visited)
+    on every 16th ray."""
     import numpy as np
     import torch
 
     import voidray_gb300 as vr
+    from voidray_gb300 import _native as N
     from voidray_gb300 import workloads as W
-    from voidray_gb300.denoise import Denoiser
-    from voidray_gb300.scene import Estimator, RenderSettings
-    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig, poisson_arrivals
 
-    size = args.serve_size
-    hdri = vr.Environments.hdri_image(W.sky_hdri(1024, 512))
+    lib = vr.lib()
+    n_tri, n_rays = args.isect_tris, args.isect_rays
+    scene = W.soup_scene(n_tri, seed=1)
+    rays = W.soup_rays(n_rays, seed=1)
+    t0 = time.perf_counter()
+    acc = scene.build_acceleration()
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    dr = torch.from_numpy(rays).cuda()
+    hits = torch.empty((n_rays, 4), dtype=torch.float32, device="cuda")
+    out = {"workload": f"{n_tri} triangle soup (seed 1), {n_rays} rays (half pinhole 4096x2048, half incoherent)",
+           "bvh_build_s": round(build_s, 2), "l2": "rays 537 MB + hits 268 MB per launch, larger than L2"}
+    for name, any_hit in (("closest", 0), ("any", 1)):
+        def launch():
+            N.check(lib.vr_intersect_device(acc.handle, dr.data_ptr(), n_rays, hits.data_ptr(), any_hit, sh))
+        for _ in range(3):
+            launch()
+        ms = timed_on(stream, launch, args.isect_reps)
+        nv, nt = C.c_uint64(), C.c_uint64()
+        N.check(lib.vr_intersect_count_device(acc.handle, dr.data_ptr(), n_rays, any_hit, C.byref(nv), C.byref(nt),
+                                              sh))
+        alg = 48 * n_rays + 64 * nv.value + 48 * nt.value
+        achieved = alg / (ms / 1e3) / 1e9
+        out[name] = {"mrays_per_s": n_rays / (ms / 1e3) / 1e6, "ms_per_launch": ms, "launches": args.isect_reps,
+                     "node_visits_per_ray": nv.value / n_rays, "tri_tests_per_ray": nt.value / n_rays,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                                  "frac": achieved / hbm_peak, "peak_source": peak_source,
+                                  "algorithmic_bytes_per_launch": alg}}
+    torch.cuda.synchronize()
+    g = hits.cpu().numpy()  # any-hit result of the last launch
+    N.check(lib.vr_intersect_device(acc.handle, dr.data_ptr(), n_rays, hits.data_ptr(), 0, sh))
+    torch.cuda.synchronize()  # the launch ran on `stream`, not on torch's current stream
+    closest = hits.cpu().numpy()
+    ids_c, ids_a = closest[:, 0].view(np.uint32), g[:, 0].view(np.uint32)
+    out["hit_fraction"] = float((ids_c != 0xFFFFFFFF).mean())
+    out["any_agrees_with_closest_on_hit_miss"] = bool(np.array_equal(ids_c != 0xFFFFFFFF, ids_a != 0xFFFFFFFF))
+    # end to end through the host-buffer call: rays in and hits out through pinned host memory
+    hrays = torch.from_numpy(rays).pin_memory()
+    hhits = torch.empty((n_rays, 4), dtype=torch.float32).pin_memory()
+    N.check(lib.vr_intersect(acc.handle, hrays.data_ptr(), n_rays, hhits.data_ptr(), 0))
+    t0 = time.perf_counter()
+    for _ in range(args.isect_reps):
+        N.check(lib.vr_intersect(acc.handle, hrays.data_ptr(), n_rays, hhits.data_ptr(), 0))
+    e2e_s = (time.perf_counter() - t0) / args.isect_reps
+    out["e2e_closest"] = {"mrays_per_s": n_rays / e2e_s / 1e6, "call": "vr_intersect (host rays and hits, pinned)",
+                          "h2d_bytes_per_call": n_rays * 32, "d2h_bytes_per_call": n_rays * 16}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        pyoracle.build()
+        osc = pyoracle.OracleScene(scene)
+        sub = np.ascontiguousarray(rays[::16])
+        t0 = time.perf_counter()
+        oh, second = osc.intersect(sub, mode=0, second=True)
+        dt = time.perf_counter() - t0
+        mism = oh[:, 0].view(np.uint32) != ids_c[::16]
+        t1 = oh[:, 1]
+        with np.errstate(invalid="ignore"):
+            tie = np.isfinite(second) & ((second - t1) <= 1e-6 * np.abs(t1))
+        out["cpu_baseline"] = {"mrays_per_s": len(sub) / dt / 1e6, "cores": pyoracle.max_threads(), "kind": "port",
+                               "sample": f"every 16th ray ({len(sub)} rays), closest hit, {dt:.1f} s"}
+        out["parity_on_cpu_sample"] = {"rays": len(sub), "id_mismatches": int(mism.sum()),
+                                       "near_ties": int(tie.sum()), "mismatches_outside_near_ties":
+                                       int((mism & ~tie).sum())}
+    acc.destroy()
+    return out
+
+
+def batch_benchmark(args):
+    """The batched workload: 64 displaced-icosphere scenes (10k-2M triangles,
+    log-uniform; materials per 64-triangle patch; one shared 2048x1024 sky +
+    sun HDRI), each with its own resolution from {256^2, 512^2, 1280x720,
+    1920x1080}, spp log-uniform in 4-256 and depth 8-12, rendered by one
+    vr_batch per pass (all jobs share every wavefront launch), each wavefront's
+    stage sequence replayed as a CUDA graph, launch shapes and wavefront size
+    from the batch autotuner.  A step renders every job's full spp once.
+    Beside it the same jobs rendered one at a time (one single-job render call
+    each, library launch shapes), and every job's batched image compared bit
+    for bit with its image rendered alone."""
+    import numpy as np
+    import torch
+
+    from voidray_gb300 import autotune
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.batch import Batch, RenderJob
+
+    t0 = time.perf_counter()
+    mix = W.batched_job_set(args.batch_jobs, seed=4)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    jobs = []
+    for s, st, spp, w, h, seed in mix:
+        jobs.append((s.build_acceleration(), st, spp, w, h, seed))
+    build_s = time.perf_counter() - t0
+    ntri = [int(a.info().num_triangles) for a, *_ in jobs]
+    samples = sum(spp * w * h for _, _, spp, w, h, _ in jobs)
+    out = {"jobs": len(jobs), "triangles_min_max_sum": [min(ntri), max(ntri), sum(ntri)],
+           "pixels": sum(w * h for _, _, _, w, h, _ in jobs), "samples_per_step": samples,
+           "spp_min_max": [min(j[2] for j in jobs), max(j[2] for j in jobs)],
+           "scene_gen_s": round(gen_s, 1), "bvh_build_s": round(build_s, 1),
+           "device_bytes": int(sum(a.info().device_bytes for a, *_ in jobs))}
+    prev_tuning = autotune.get_tuning()
+    tuning = autotune.tune_batch(jobs)
+    out["tuning"] = tuning
+    stream = torch.cuda.Stream()
+    outs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, _, _, w, h, _ in jobs]
+    first = [torch.zeros_like(o) for o in outs]
+    batch = Batch(int(tuning["max_wave_paths"]))
+    batch.set_graphs(True)
+
+    def step(k, bufs):
+        batch.render([RenderJob(acc, st, spp, o.data_ptr(), w, h, seed, k * spp)
+                      for (acc, st, spp, w, h, seed), o in zip(jobs, bufs)], stream.cuda_stream)
+
+    step(0, first)  # direct launches; pass 0 is also the bit-identity sample
+    for k in range(1, 3):  # graph capture, then replay
+        step(k, outs)
+    ms = timed_on(stream, lambda: [step(3 + k, outs) for k in range(args.batch_steps)], 1) / args.batch_steps
+    batch.synchronize(stream.cuda_stream)
+    caps, reps = batch.graph_stats()
+    out.update({"ms_per_step": ms, "samples_per_s": samples / (ms / 1e3), "steps": args.batch_steps,
+                "graph_captures": caps, "graph_replays": reps})
+    batch.destroy()
+    # the same jobs one at a time (one single-job render call each, library
+    # launch shapes and 2^26-path wavefronts, one shared scratch); pass 0 again
+    # for the comparison
+    autotune.set_tuning({k: v for k, v in autotune.DEFAULT.items() if k != "wavefront_paths"})
+    alone = [torch.zeros_like(o) for o in outs]
+    single = Batch(1 << 26)
+
+    def alone_pass():
+        for (acc, st, spp, w, h, seed), o in zip(jobs, alone):
+            single.render([RenderJob(acc, st, spp, o.data_ptr(), w, h, seed, 0)], stream.cuda_stream)
+
+    ms_alone = timed_on(stream, alone_pass, 1)
+    single.synchronize(stream.cuda_stream)
+    single.destroy()
+    autotune.set_tuning(prev_tuning)
+    same = [bool(torch.equal(a, b)) for a, b in zip(alone, first)]
+    out.update({"alone_ms_per_step": ms_alone, "alone_samples_per_s": samples / (ms_alone / 1e3),
+                "speedup_vs_alone": ms_alone / ms, "jobs_bit_identical_to_alone": int(sum(same))})
+    for acc, *_ in jobs:
+        acc.destroy()
+    return out
+
+
+def serving_scenes(size_label, freqs, seeds, hdri, max_bounces_base=8):
+    """Resident scenes of a serving run: displaced icospheres (materials per
+    64-triangle patch) sharing one HDRI, with the reference's default firefly
+    clamp (3.0): the sun seen through metal / dielectric patches would
+    otherwise keep every job far from the target error."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.scene import Estimator, RenderSettings
+
     pool = []
-    for k, freq in enumerate((30, 60, 120, 200)):
-        s, _ = W.displaced_icosphere_scene(freq=freq, seed=10 + k, hdri_size=None)
+    for k, (freq, seed) in enumerate(zip(freqs, seeds)):
+        s, _ = W.displaced_icosphere_scene(freq=freq, seed=seed, hdri_size=None)
         s.environment = hdri
         acc = s.build_acceleration()
-        # the reference's default firefly clamp (3.0): the sun seen through
-        # metal / dielectric patches would otherwise keep every job far from
-        # the target error
-        st = RenderSettings(total_samples=1, max_bounces=8 + k, rr_depth=3, estimator=Estimator.NEE,
+        st = RenderSettings(total_samples=1, max_bounces=max_bounces_base + k, rr_depth=3, estimator=Estimator.NEE,
                             firefly_clamp=3.0)
         pool.append((acc, st, int(acc.info().device_bytes), s.num_triangles()))
-    # 4096-spp references, one per scene (all jobs of a scene share its camera)
+    return pool
+
+
+def serving_references(pool, w, h, spp=4096):
+    """Per scene: the `spp`-sample reference as the mean of two independent
+    halves A, B (disjoint sample ranges), and the reference's own noise term
+    mean(Var(ref) / (ref^2 + 1e-2)) with Var(ref) = (A - B)^2 / 4 per pixel
+    and channel; a job's error against the true image is its measured error
+    minus this term (the job and the reference are independent)."""
+    import numpy as np
+
+    import voidray_gb300 as vr
+    from voidray_gb300.scene import RenderSettings
+
     refs = {}
     for acc, st, *_ in pool:
-        t = vr.CpuRenderTarget(size, size)
-        vr.iterative_render(t, acc, RenderSettings(**{**st.__dict__, "total_samples": 4096}), 4096, seed=99)
-        refs[id(acc)] = t.buffer[..., :3].astype(np.float64)
+        halves = []
+        for first in (0, spp // 2):
+            t = vr.CpuRenderTarget(w, h)
+            vr.iterative_render(t, acc, RenderSettings(**{**st.__dict__, "total_samples": spp // 2}), spp // 2,
+                                seed=99, first_sample=first)
+            halves.append(t.buffer[..., :3].astype(np.float64))
+        ref = 0.5 * (halves[0] + halves[1])
+        noise = float(np.mean((halves[0] - halves[1]) ** 2 / 4.0 / (ref * ref + 1e-2)))
+        refs[id(acc)] = (ref, noise)
+    return refs
 
-    def relmse(x, r):
-        return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
+def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_passes, warm_jobs, max_samples):
+    """One Poisson request stream (seeded) served by every mode:
+    plain_<n>: the plain single-scene GPU path, one job at a time, n spp per
+    pass (plain_adaptive: one job at a time with predictive pass sizes, the
+    job's predicted remaining samples in one pass); served: continuous
+    batching of every admitted job in one launch per pass; served_denoised:
+    the same with AOVs and the learned denoiser, each job returning the plain
+    mean or the denoised blend, whichever is predicted to be better.  The
+    best plain mode (lowest p50) is the denominator of the ratios."""
+    import numpy as np
+    import torch
+
+    from voidray_gb300.serve import GpuBackend, JobRequest, Server, ServerConfig, poisson_arrivals
 
     rng = np.random.default_rng(5)
-    arrivals = poisson_arrivals(args.serve_rate, args.serve_jobs, seed=5)
+    arrivals = poisson_arrivals(rate, n_jobs, seed=5)
     picks = [int(rng.integers(0, len(pool))) for _ in arrivals]
-    net = Denoiser.pretrained()
-    net.set_backend(Denoiser.TCGEN05)   # inference on the tcgen05 convolution
-    out = {"jobs": args.serve_jobs, "rate_per_s": args.serve_rate, "image": f"{size}x{size}",
-           "target_relmse": args.serve_target, "scenes_triangles": [p[3] for p in pool],
+    out = {"jobs": n_jobs, "rate_per_s": rate, "image": f"{w}x{h}", "target_relmse": target,
+           "scenes_triangles": [p[3] for p in pool],
            "error_estimate": "half-buffer variance of the mean / (m^2 + 1e-2); denoised: reference-free "
                              "prediction of the blend's error from the halves",
-           "reference": "4096 spp per scene", "denoiser": "U-Net 32/64/128/256, bf16, shipped weights",
-           "warmup": "6 untimed jobs per mode on the same backend before the timed arrivals"}
-    spp_pass = 32
-    # plain: the progressive single-scene loop, one job at a time, 32 spp per
-    # pass, stopping on the same half-buffer estimate.  served: continuous
-    # batching with predictive per-job pass sizes (16M-path passes, jobs take
-    # them in admission order).  served_denoised: the same plus AOVs and the
-    # denoiser blend.
-    plain_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=1, spp_per_pass=spp_pass, min_samples=64)
+           "reference": "4096 spp per scene (two independent 2048-spp halves); true_relmse = measured relMSE "
+                        "against it minus its own noise term",
+           "reference_noise_relmse": [refs[id(p[0])][1] for p in pool],
+           "denoiser": "U-Net 32/64/128/256, bf16, shipped weights",
+           "warmup": f"{warm_jobs} untimed jobs per mode on the same backend before the timed arrivals"}
+    modes = []
+    for n in plain_passes:
+        if n == "adaptive":
+            modes.append(("plain_adaptive", ServerConfig(memory_budget=150 * 10**9, max_active=1, adaptive=True,
+                                                         pass_paths=1 << 26, first_pass_spp=64, min_samples=64,
+                                                         overshoot=1.15), False))
+        else:
+            modes.append((f"plain_{n}", ServerConfig(memory_budget=150 * 10**9, max_active=1, spp_per_pass=n,
+                                                     min_samples=64), False))
     # the denoised path starts with a larger first pass: its blend estimate
     # needs a less noisy input, and its per-job sample counts are smaller
-    served_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
-                              pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15, max_inflight=3)
-    served_dn_cfg = ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
-                                 pass_paths=1 << 24, first_pass_spp=128, min_samples=64, overshoot=1.2,
-                                 max_inflight=3)
+    modes.append(("served", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
+                                         pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15,
+                                         max_inflight=3), False))
+    modes.append(("served_denoised", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True,
+                                                  pipelined=True, pass_paths=1 << 24, first_pass_spp=128,
+                                                  min_samples=64, overshoot=1.2, max_inflight=3), True))
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
-                            "max_inflight": 3, "render_streams": args.serve_streams,
+                            "max_inflight": 3, "render_streams": streams,
                             "first_pass_spp": {"served": 64, "served_denoised": 128},
                             "overshoot": {"served": 1.15, "served_denoised": 1.2}}
-    modes = (("plain", plain_cfg, False), ("served", served_cfg, False), ("served_denoised", served_dn_cfg, True))
     for name, cfg, dn in modes:
-        active = cfg.max_active
-        backend = GpuBackend(denoiser=net if dn else None, render_streams=args.serve_streams if cfg.pipelined else 1)
+        backend = GpuBackend(denoiser=net if dn else None, render_streams=streams if cfg.pipelined else 1)
         # untimed warm-up on the same backend: graph shapes, denoiser
         # workspaces and lazily loaded kernels, for every mode alike
         warm = Server(backend, cfg)
-        warm.run([(0.0, JobRequest(pool[k % len(pool)][0], pool[k % len(pool)][1], size, size, max_samples=256,
-                                   target_relmse=args.serve_target, seed=500 + k, scene_bytes=pool[k % len(pool)][2],
-                                   denoise=dn)) for k in range(6)])
+        warm.run([(0.0, JobRequest(pool[k % len(pool)][0], pool[k % len(pool)][1], w, h, max_samples=256,
+                                   target_relmse=target, seed=500 + k, scene_bytes=pool[k % len(pool)][2],
+                                   denoise=dn)) for k in range(warm_jobs)])
         backend.time = {k: 0.0 for k in backend.time}
         backend.denoise_calls = 0
         requests = []
         for i, t in enumerate(arrivals):
             acc, st, nbytes, _ = pool[picks[i]]
-            requests.append((float(t), JobRequest(acc, st, size, size, max_samples=2048,
-                                                  target_relmse=args.serve_target, seed=1000 + i,
-                                                  scene_bytes=nbytes, denoise=dn)))
+            requests.append((float(t), JobRequest(acc, st, w, h, max_samples=max_samples, target_relmse=target,
+                                                  seed=1000 + i, scene_bytes=nbytes, denoise=dn)))
         srv = Server(backend, cfg)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -260,27 +465,66 @@ def serving_benchmark(args):
         lat = srv.latencies()
         jobs = list(srv.jobs.values())
         samples = sum(j.samples * j.req.width * j.req.height for j in jobs)
-        errs = [relmse(j.result.astype(np.float64), refs[id(j.req.scene)]) for j in jobs]
+        errs = []
+        for j in jobs:
+            ref, noise = refs[id(j.req.scene)]
+            x = j.result.astype(np.float64)
+            errs.append(float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2))) - noise)
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "jobs_per_s": len(lat) / wall, "samples_per_s": samples / wall, "wall_s": wall,
-                     "passes": srv.passes, "max_active": active,
+                     "passes": srv.passes, "max_active": cfg.max_active,
                      "mean_spp": float(np.mean([j.samples for j in jobs])),
                      "true_relmse_p50": float(np.median(errs)), "true_relmse_p99": float(np.percentile(errs, 99)),
-                     "true_relmse_max": float(np.max(errs))}
+                     "true_relmse_max": float(np.max(errs)),
+                     "jobs_meeting_target": int(sum(e <= target for e in errs))}
         out[name]["host_phase_s"] = dict(backend.time)
         if dn:
             out[name]["denoised_jobs"] = int(sum(np.any(np.asarray(j.alpha) > 0) for j in jobs))
             out[name]["mean_alpha"] = float(np.mean([np.mean(j.alpha) for j in jobs]))
             out[name]["denoiser_calls"] = backend.denoise_calls
         backend.destroy()
-    out["p50_speedup_served"] = out["plain"]["p50_s"] / out["served"]["p50_s"]
-    out["p50_speedup_served_denoised"] = out["plain"]["p50_s"] / out["served_denoised"]["p50_s"]
-    out["throughput_ratio_served"] = out["served"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
-    out["throughput_ratio_served_denoised"] = out["served_denoised"]["jobs_per_s"] / out["plain"]["jobs_per_s"]
-    out["equal_time"] = denoiser_equal_time(pool, refs, net, size)
-    net.destroy()
+    plains = [m for m, _, _ in modes if m.startswith("plain")]
+    best = min(plains, key=lambda m: out[m]["p50_s"])
+    out["plain_best"] = best
+    for m in ("served", "served_denoised"):
+        out[f"p50_speedup_{m}"] = out[best]["p50_s"] / out[m]["p50_s"]
+        out[f"throughput_ratio_{m}"] = out[m]["jobs_per_s"] / out[best]["jobs_per_s"]
+    return out
+
+
+def serving_benchmark(args):
+    """The serving workload at two job sizes.  `small`: 48 requests of 256x256
+    on four resident displaced icospheres of 18k-800k triangles (a size at
+    which one job alone leaves most of the GPU idle); `config5`: requests drawn
+    like the plain-render scene -- 1920x1080 images of 2M-triangle displaced
+    icospheres (four seeds) -- at the same 200 jobs/s Poisson rate.  Every job
+    renders to a target relMSE of 1e-3 against its scene's 4096-spp reference,
+    its own error estimated from its two half-buffers without a reference."""
+    import voidray_gb300 as vr
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.denoise import Denoiser
+
+    net = Denoiser.pretrained()
+    net.set_backend(Denoiser.TCGEN05)   # inference on the tcgen05 convolution
+    out = {}
+    hdri_small = vr.Environments.hdri_image(W.sky_hdri(1024, 512))
+    pool = serving_scenes("small", (30, 60, 120, 200), (10, 11, 12, 13), hdri_small)
+    size = args.serve_size
+    refs = serving_references(pool, size, size)
+    out["small"] = serving_run(pool, refs, net, size, size, args.serve_jobs, args.serve_rate, args.serve_target,
+                               args.serve_streams, (32, 128, 512, "adaptive"), 6, 2048)
+    out["small"]["equal_time"] = denoiser_equal_time(pool, {k: v[0] for k, v in refs.items()}, net, size)
     for acc, *_ in pool:
         acc.destroy()
+    if args.serve_large_jobs:
+        hdri = vr.Environments.hdri_image(W.sky_hdri(2048, 1024), importance_sample=True)
+        pool = serving_scenes("config5", (316, 316, 316, 316), (2, 21, 22, 23), hdri)
+        refs = serving_references(pool, 1920, 1080)
+        out["config5"] = serving_run(pool, refs, net, 1920, 1080, args.serve_large_jobs, args.serve_rate,
+                                     args.serve_target, args.serve_streams, (32, 128, "adaptive"), 2, 2048)
+        for acc, *_ in pool:
+            acc.destroy()
+    net.destroy()
     return out
 
 
@@ -540,6 +784,13 @@ def main():
     finite = bool(np.isfinite(out_img).all())
 
     acc.destroy()
+    isect = None
+    if rank == 0 and world == 1 and not args.no_isect:
+        isect = intersection_benchmark(args, hbm_peak, "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
+                                       else "fallback")
+    batched = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        batched = batch_benchmark(args)
     serve = None
     if rank == 0 and world == 1 and not args.no_serve:
         serve = serving_benchmark(args)
@@ -570,7 +821,7 @@ def main():
             "mrays_per_s": (ext_rays + shd_rays) / (ms / 1e3) / 1e6,
             "rays": {"extend": int(ext_rays), "shadow": int(shd_rays)},
             "stages": stage, "gpu_launches": gpu_launches, "clocks": clk, "e2e": e2e, "roofline": roofline,
-            "cpu_baseline": cpu, "image_finite": finite, "serving": serve, "denoiser": dnb,
+            "cpu_baseline": cpu, "image_finite": finite, "intersection": isect, "batched": batched, "serving": serve, "denoiser": dnb,
         }
         print(json.dumps(line), flush=True)
     acc.destroy()

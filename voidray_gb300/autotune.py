@@ -139,3 +139,80 @@ def tune(acc, settings, width: int, height: int, spp: int, *, use_cache: bool = 
         save_cache(cache)
     set_tuning(best)
     return dict(best, cached=False, key=key)
+
+
+BATCH_WAVEFRONTS = (1 << 24, 1 << 25, 1 << 26)
+
+
+def tune_batch(jobs, *, scale: int = 8, use_cache: bool = True, log=None) -> dict:
+    """Best launch shapes for a many-job batch: the batch's wavefront size
+    (vr_batch_create's max_wave_paths) and the shade / raygen launch shapes,
+    by the same coordinate descent as tune(), each configuration timed with
+    CUDA events on the caller's own jobs with their sample counts divided by
+    `scale` (at least 1), graphs on, after two warm-up passes (direct, then
+    capture).  `jobs`: [(acc, settings, spp, width, height, seed)].  Cached per
+    (GPU, job count, triangle / pixel / sample buckets).  Returns {knobs...,
+    "max_wave_paths", "ms", "trials", "cached"} and leaves the launch shapes set."""
+    import torch
+
+    from .batch import Batch, RenderJob
+
+    gpu = torch.cuda.get_device_name()
+    lg = lambda x: int(math.log2(max(1, x)))
+    tris = sum(int(a.info().num_triangles) for a, *_ in jobs)
+    pix = sum(w * h for _, _, _, w, h, _ in jobs)
+    smp = sum(spp * w * h for _, _, spp, w, h, _ in jobs)
+    key = f"{gpu}|batch{len(jobs)}|tri2^{lg(tris)}|px2^{lg(pix)}|smp2^{lg(smp)}"
+    cache = load_cache() if use_cache else {}
+    if key in cache:
+        best = dict(cache[key], cached=True, key=key)
+        set_tuning(best)
+        return best
+    outs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, _, _, w, h, _ in jobs]
+    stream = torch.cuda.Stream()
+    trials = 0
+
+    def run(cfg) -> float:
+        nonlocal trials
+        set_tuning(cfg)
+        b = Batch(int(cfg["max_wave_paths"]))
+        b.set_graphs(True)
+        try:
+            def one(p):
+                b.render([RenderJob(acc, st, max(1, spp // scale), o.data_ptr(), w, h, seed, p * max(1, spp // scale))
+                          for (acc, st, spp, w, h, seed), o in zip(jobs, outs)], stream.cuda_stream)
+            one(0)
+            one(1)
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            one(2)
+            one(3)
+            e1.record(stream)
+            e1.synchronize()
+            b.synchronize(stream.cuda_stream)
+            ms = e0.elapsed_time(e1) / 2
+        finally:
+            b.destroy()
+        trials += 1
+        if log:
+            log(f"[autotune batch] {cfg} {ms:.2f} ms")
+        return ms
+
+    cfg = dict(DEFAULT)
+    cfg.pop("wavefront_paths")
+    cfg["max_wave_paths"] = 1 << 26
+    best_ms = None
+    t0 = time.perf_counter()
+    for knob, values in (("max_wave_paths", BATCH_WAVEFRONTS), ("shade_block", BLOCKS),
+                         ("shade_blocks_per_sm", PER_SM), ("raygen_block", BLOCKS)):
+        results = {v: run(dict(cfg, **{knob: v})) for v in values}
+        v_best = min(results, key=results.get)
+        cfg[knob] = v_best
+        best_ms = results[v_best]
+    best = dict(cfg, ms=best_ms, trials=trials, seconds=time.perf_counter() - t0, sample_scale=scale)
+    if use_cache:
+        cache[key] = best
+        save_cache(cache)
+    set_tuning(best)
+    return dict(best, cached=False, key=key)

@@ -2,9 +2,10 @@
 
 Each translation unit is compiled by nvcc in parallel, then linked into
 ``voidray_gb300/_lib/libvoidray_gb300.so`` with the CUDA runtime linked
-statically.  Device code is compiled with ``-fmad=false`` and host code with
-``-ffp-contract=off`` so that every f32 operation on the reference-estimator
-path rounds separately, as the reference computes it.
+statically.  The tracer's device code is compiled with ``-fmad=false`` and
+host code with ``-ffp-contract=off`` so that every f32 operation on the
+reference-estimator path rounds separately, as the reference computes it; the
+denoiser's kernels keep FMA contraction.
 """
 from __future__ import annotations
 
@@ -22,6 +23,8 @@ LIB = LIBDIR / "libvoidray_gb300.so"
 
 SOURCES = ["vr_build.cpp", "vr_kernels.cu", "vr_capi.cu", "vr_serve.cu", "dn_kernels.cu", "dn_unet.cu", "dn_tc.cu",
            "vr_image.cpp", "vr_obj.cpp"]
+# the denoiser's translation units (compiled with FMA contraction)
+DENOISER = {"dn_kernels.cu", "dn_unet.cu", "dn_tc.cu"}
 # host-only translation units: compiled as plain C++ (no device code)
 HOST_ONLY = {"vr_image.cpp", "vr_obj.cpp"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -42,7 +45,10 @@ def _flags(src: str) -> list[str]:
     if src in HOST_ONLY:
         return common + ["-x", "c++"]
     if src.endswith(".cu"):
-        return ARCH + common + ["-fmad=false", "-Xptxas", "-v" if os.environ.get("VR_PTXAS_VERBOSE") else "-O3"]
+        # the tracer reproduces the reference's f32 rounding operation by
+        # operation; the denoiser's kernels have no such contract and keep FMA
+        fmad = [] if src in DENOISER else ["-fmad=false"]
+        return ARCH + common + fmad + ["-Xptxas", "-v" if os.environ.get("VR_PTXAS_VERBOSE") else "-O3"]
     return common + ["-x", "cu"] + ARCH + ["-fmad=false"]
 
 

@@ -211,7 +211,7 @@ struct GraphCache {
     bool first_sight(const GraphKey& k) {
         for (const GraphKey& s : seen)
             if (std::memcmp(&s, &k, sizeof k) == 0) return false;
-        if (seen.size() >= 64) seen.erase(seen.begin());
+        if (seen.size() >= 1024) seen.erase(seen.begin());
         seen.push_back(k);
         return true;
     }
@@ -224,7 +224,7 @@ struct GraphCache {
         return nullptr;
     }
     void insert(const GraphKey& k, cudaGraphExec_t x) {
-        if (entries.size() >= 16) {
+        if (entries.size() >= 256) {
             size_t lru = 0;
             for (size_t i = 1; i < entries.size(); ++i)
                 if (entries[i].used < entries[lru].used) lru = i;
@@ -376,7 +376,12 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
             for (size_t i = 0; i < jobs.size() && left > 0 && wh.njobs < vr::MAX_JOBS; ++i) {
                 HostJob& j = jobs[i];
                 if (j.done >= j.total) continue;
-                const uint32_t take = (uint32_t)std::min<uint64_t>(left, j.total - j.done);
+                uint32_t take = (uint32_t)std::min<uint64_t>(left, j.total - j.done);
+                // a job that does not finish in this wave takes whole sample rows
+                // when it can (pixel-major slot order), leaving the rest of the
+                // wave to the jobs after it
+                if (take < j.total - j.done && take >= j.tmpl.num_pixels)
+                    take -= (take + (uint32_t)(j.done % j.tmpl.num_pixels)) % j.tmpl.num_pixels;
                 vr::Job e = j.tmpl;
                 e.g0 = j.done;
                 e.paths = take;
@@ -863,7 +868,9 @@ vr_status vr_batch_render(vr_batch* b, const vr_render_job* jobs, uint32_t count
         }
     }
     if (total == 0) return VR_OK;
-    const uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
+    uint64_t cap = std::min<uint64_t>(b->max_wave_paths, total);
+    if (count == 1 && cap > (uint64_t)jobs[0].width * jobs[0].height)  // one job: whole sample rows per wave
+        cap -= cap % ((uint64_t)jobs[0].width * jobs[0].height);
     const void* before = b->eng.ps.q_org;
     if ((r = b->eng.ensure((uint32_t)cap, att_depth, cs, want_aov)) != VR_OK) return r;
     if (b->eng.ps.q_org != before) b->graphs.clear();  // graphs bake in the old scratch pointers

@@ -444,3 +444,29 @@ def mixed_job_set(count: int = 16, seed: int = 4, tri_range=(10_000, 200_000), s
         st.firefly_clamp = float(rng.choice([3.0, float("inf")]))
         out.append((s, st, spp, w, h, int(rng.integers(0, 1 << 30))))
     return out
+
+
+def batched_job_set(count: int = 64, seed: int = 4, tri_range=(10_000, 2_000_000), spp_range=(4, 256),
+                    depth_range=(8, 12), hdri_size=(2048, 1024)):
+    """The batched workload at full size: `count` displaced-icosphere scenes
+    (materials per 64-triangle patch, NEE estimator, clamp off) with triangle
+    counts log-uniform in `tri_range`, resolution drawn from {256^2, 512^2,
+    1280x720, 1920x1080}, spp log-uniform in `spp_range`, depth uniform in
+    `depth_range`, all sharing one importance-sampled sky + sun HDRI.  Every
+    draw is seeded.  Returns [(scene, settings, spp, width, height, seed)]."""
+    rng = np.random.default_rng(seed)
+    sizes = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+    env = Environments.hdri_image(sky_hdri(*hdri_size), importance_sample=True)
+    lo, hi = np.log(tri_range[0]), np.log(tri_range[1])
+    out = []
+    for k in range(count):
+        tris = float(np.exp(rng.uniform(lo, hi)))
+        freq = max(2, int(round(math.sqrt(tris / 20.0))))
+        s, st = displaced_icosphere_scene(freq=freq, seed=200 + k, hdri_size=None)
+        s.environment = env
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        spp = int(round(np.exp(rng.uniform(np.log(spp_range[0]), np.log(spp_range[1])))))
+        st.max_bounces = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        st.total_samples = spp
+        out.append((s, st, spp, w, h, int(rng.integers(0, 1 << 30))))
+    return out
