@@ -33,7 +33,12 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
-K_EXTEND_DRAM_BYTES_PER_LAUNCH = 2.374e9
+# DRAM and L2 bytes per closest-hit ray of k_extend on the default scene,
+# from an ncu capture of all twelve k_extend launches of one 960x540 x 32 spp
+# frame of it (the same 2M-triangle scene and HDRI, 34.4M extend rays); the
+# bench scales them to its own launches by the extend rays per launch
+K_EXTEND_DRAM_BYTES_PER_RAY = 165.6
+K_EXTEND_L2_BYTES_PER_RAY = 1102.3
 sys.path.insert(0, str(ROOT))
 
 CLOCK_FIELDS = ["uuid", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
@@ -395,7 +400,8 @@ def serving_references(pool, w, h, spp=4096):
     return refs
 
 
-def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_passes, warm_jobs, max_samples):
+def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_passes, warm_jobs, max_samples,
+                dn_first_pass=96, only=None):
     """One Poisson request stream (seeded) served by every mode:
     plain_<n>: the plain single-scene GPU path, one job at a time, n spp per
     pass (plain_adaptive: one job at a time with predictive pass sizes, the
@@ -430,17 +436,22 @@ def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_pass
         else:
             modes.append((f"plain_{n}", ServerConfig(memory_budget=150 * 10**9, max_active=1, spp_per_pass=n,
                                                      min_samples=64), False))
-    # the denoised path starts with a larger first pass: its blend estimate
-    # needs a less noisy input, and its per-job sample counts are smaller
     modes.append(("served", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
                                          pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15,
                                          max_inflight=3), False))
+    # the denoised path starts with a larger first pass: its blend estimate
+    # needs a less noisy input (a smaller first pass makes the prediction
+    # noisier and more conservative: 32 spp first passes ended at 134 spp per
+    # 1080p job on average, 96 spp ones at 98)
     modes.append(("served_denoised", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True,
-                                                  pipelined=True, pass_paths=1 << 24, first_pass_spp=128,
-                                                  min_samples=64, overshoot=1.2, max_inflight=3), True))
+                                                  pipelined=True, pass_paths=1 << 24, first_pass_spp=dn_first_pass,
+                                                  min_samples=min(64, dn_first_pass), overshoot=1.2,
+                                                  max_inflight=3), True))
+    if only is not None:
+        modes = [m for m in modes if m[0] in only]
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
                             "max_inflight": 3, "render_streams": streams,
-                            "first_pass_spp": {"served": 64, "served_denoised": 128},
+                            "first_pass_spp": {"served": 64, "served_denoised": dn_first_pass},
                             "overshoot": {"served": 1.15, "served_denoised": 1.2}}
     for name, cfg, dn in modes:
         backend = GpuBackend(denoiser=net if dn else None, render_streams=streams if cfg.pipelined else 1)
@@ -484,9 +495,11 @@ def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_pass
             out[name]["denoiser_calls"] = backend.denoise_calls
         backend.destroy()
     plains = [m for m, _, _ in modes if m.startswith("plain")]
+    if not plains:
+        return out
     best = min(plains, key=lambda m: out[m]["p50_s"])
     out["plain_best"] = best
-    for m in ("served", "served_denoised"):
+    for m in [x for x in ("served", "served_denoised") if x in out]:
         out[f"p50_speedup_{m}"] = out[best]["p50_s"] / out[m]["p50_s"]
         out[f"throughput_ratio_{m}"] = out[m]["jobs_per_s"] / out[best]["jobs_per_s"]
     return out
@@ -512,7 +525,7 @@ def serving_benchmark(args):
     size = args.serve_size
     refs = serving_references(pool, size, size)
     out["small"] = serving_run(pool, refs, net, size, size, args.serve_jobs, args.serve_rate, args.serve_target,
-                               args.serve_streams, (32, 128, 512, "adaptive"), 6, 2048)
+                               args.serve_streams, (32, 128, 512, "adaptive"), 6, 2048, dn_first_pass=96)
     out["small"]["equal_time"] = denoiser_equal_time(pool, {k: v[0] for k, v in refs.items()}, net, size)
     for acc, *_ in pool:
         acc.destroy()
@@ -521,7 +534,8 @@ def serving_benchmark(args):
         pool = serving_scenes("config5", (316, 316, 316, 316), (2, 21, 22, 23), hdri)
         refs = serving_references(pool, 1920, 1080)
         out["config5"] = serving_run(pool, refs, net, 1920, 1080, args.serve_large_jobs, args.serve_rate,
-                                     args.serve_target, args.serve_streams, (32, 128, "adaptive"), 2, 2048)
+                                     args.serve_target, args.serve_streams, (32, 128, "adaptive"), 2, 2048,
+                                     dn_first_pass=96)
         for acc, *_ in pool:
             acc.destroy()
     net.destroy()
@@ -732,7 +746,7 @@ def main():
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    default_workload = (args.width, args.height, args.spp, args.freq) == (1920, 1080, 256, 316)
+    default_scene = args.freq == 316
     if not args.no_work_count:
         N.check(lib.vr_scene_instrument(acc.handle, N.INSTR_WORK))
         c0 = acc.stats()
@@ -750,11 +764,15 @@ def main():
         achieved = alg_bytes / (ext_ms_per_frame / 1e3) / 1e9
         roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit BVH2 traversal)", "achieved": achieved,
                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                    # ncu dram__bytes_read.sum + dram__bytes_write.sum per k_extend launch, mean over the 12
-                    # depths of one full-size wavefront of this workload (a constant from that capture:
-                    # profiles/k_extend_k_shadow_1920x1080_256spp_dram_traffic.md); only valid at the
-                    # default workload
-                    "traffic": K_EXTEND_DRAM_BYTES_PER_LAUNCH if default_workload else None,
+                    # dram__bytes_read.sum + dram__bytes_write.sum per k_extend launch: bytes per extend
+                    # ray measured on a smaller frame of the same scene, times this run's extend rays per
+                    # launch (the scene's figure; null for another scene)
+                    "traffic": K_EXTEND_DRAM_BYTES_PER_RAY * rays1 / max(ext_launches_per_frame, 1)
+                    if default_scene else None,
+                    "traffic_source": "ncu dram bytes per extend ray (960x540 x 32 spp frame of the same scene) "
+                                      "x extend rays per launch",
+                    "l2_gbs": K_EXTEND_L2_BYTES_PER_RAY * rays1 / (ext_ms_per_frame / 1e3) / 1e9
+                    if default_scene else None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
                     "algorithmic_bytes_per_launch": alg_bytes / max(ext_launches_per_frame, 1),
                     "avg_launch_ms": ext_ms_per_frame / max(ext_launches_per_frame, 1),
