@@ -401,7 +401,7 @@ def serving_references(pool, w, h, spp=4096):
 
 
 def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_passes, warm_jobs, max_samples,
-                dn_first_pass=96, only=None):
+                dn_first_pass=96, only=None, dn_overshoot=1.2):
     """One Poisson request stream (seeded) served by every mode:
     plain_<n>: the plain single-scene GPU path, one job at a time, n spp per
     pass (plain_adaptive: one job at a time with predictive pass sizes, the
@@ -445,14 +445,14 @@ def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_pass
     # 1080p job on average, 96 spp ones at 98)
     modes.append(("served_denoised", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True,
                                                   pipelined=True, pass_paths=1 << 24, first_pass_spp=dn_first_pass,
-                                                  min_samples=min(64, dn_first_pass), overshoot=1.2,
+                                                  min_samples=min(64, dn_first_pass), overshoot=dn_overshoot,
                                                   max_inflight=3), True))
     if only is not None:
         modes = [m for m in modes if m[0] in only]
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
                             "max_inflight": 3, "render_streams": streams,
                             "first_pass_spp": {"served": 64, "served_denoised": dn_first_pass},
-                            "overshoot": {"served": 1.15, "served_denoised": 1.2}}
+                            "overshoot": {"served": 1.15, "served_denoised": dn_overshoot}}
     for name, cfg, dn in modes:
         backend = GpuBackend(denoiser=net if dn else None, render_streams=streams if cfg.pipelined else 1)
         # untimed warm-up on the same backend: graph shapes, denoiser

@@ -402,6 +402,31 @@ void build_env_tables(HostScene& hs) {
         }
     });
     T.marginal[H] = 1.0f;
+    // Guide tables: guide[k] = the index the device's search returns for
+    // u = k / M (the largest i < n with cdf[i] <= u; the CDFs are
+    // non-decreasing, so that index is non-decreasing in u).  For u in
+    // [k/M, (k+1)/M) the search then only needs [guide[k], guide[k+1]].
+    auto pow2_at_least = [](uint32_t x, uint32_t lo, uint32_t hi) {
+        uint32_t m = lo;
+        while (m < x && m < hi) m <<= 1;
+        return m;
+    };
+    auto guide = [](const float* cdf, uint32_t n, uint32_t m, uint32_t* g) {
+        for (uint32_t k = 0; k <= m; ++k) {
+            const float u = (float)k / (float)m;  // exact: m is a power of two
+            const uint32_t c = (uint32_t)(std::upper_bound(cdf, cdf + n, u) - cdf);
+            g[k] = c > 0 ? c - 1 : 0;
+        }
+    };
+    T.gm = pow2_at_least(H, 16, 4096);
+    T.gc = pow2_at_least(W / 4, 16, 1024);
+    T.guide_marginal.assign(T.gm + 1, 0);
+    guide(T.marginal.data(), H, T.gm, T.guide_marginal.data());
+    T.guide_conditional.assign((size_t)H * (T.gc + 1), 0);
+    for_chunks(0, H, chunks, [&](int, uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0; j < j1; ++j)
+            guide(&T.conditional[(size_t)j * (W + 1)], W, T.gc, &T.guide_conditional[(size_t)j * (T.gc + 1)]);
+    });
 }
 
 }  // namespace

@@ -552,6 +552,10 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
         if ((st = upload(s, hs.tables.marginal, &s->view.env_marg)) != VR_OK) return cleanup(st);
         if ((st = upload(s, hs.tables.conditional, &s->view.env_cond)) != VR_OK) return cleanup(st);
         if ((st = upload(s, hs.tables.cell, &s->view.env_cell)) != VR_OK) return cleanup(st);
+        if ((st = upload(s, hs.tables.guide_marginal, &s->view.env_gmarg)) != VR_OK) return cleanup(st);
+        if ((st = upload(s, hs.tables.guide_conditional, &s->view.env_gcond)) != VR_OK) return cleanup(st);
+        s->view.env_gm = hs.tables.gm;
+        s->view.env_gc = hs.tables.gc;
     }
     void* p = nullptr;
     if (cudaMalloc(&p, 64) != cudaSuccess) return cleanup(fail(VR_ERR_OOM, "status alloc"));

@@ -74,6 +74,9 @@ struct SceneView {
     const float* env_cell;   // H*W
     int32_t env_is;
     float env_density_scale; // W*H/(2 pi^2) as f32
+    const uint32_t* env_gmarg;  // guide of the marginal search, env_gm + 1 entries
+    const uint32_t* env_gcond;  // guides of the conditional rows, H * (env_gc + 1)
+    uint32_t env_gm, env_gc;    // powers of two
     // camera acceleration (camera.rs:38-53)
     float c_origin[3], c_dir[3], c_right[3], c_up[3];
     float c_d;

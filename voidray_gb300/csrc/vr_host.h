@@ -20,6 +20,11 @@ struct EnvTables {
     std::vector<float> marginal;     // H+1
     std::vector<float> conditional;  // H*(W+1)
     std::vector<float> cell;         // H*W, probability of each cell
+    // guide tables of the inverse-CDF search: for u in [k/M, (k+1)/M) the
+    // searched index lies in [guide[k], guide[k+1]] (M a power of two)
+    uint32_t gm = 0, gc = 0;                // M of the marginal / of every conditional row
+    std::vector<uint32_t> guide_marginal;   // gm + 1
+    std::vector<uint32_t> guide_conditional;  // H * (gc + 1)
 };
 
 // Everything vr_scene_create uploads, laid out as the kernels read it.

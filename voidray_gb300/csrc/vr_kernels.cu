@@ -100,8 +100,16 @@ __device__ V3 env_eval(const SceneView& s, V3 dir) {
     return lerp3(lerp3(env_px(img, (y0 * W + x0) % len), env_px(img, (y0 * W + x0 + 1) % len), ax),
                  lerp3(env_px(img, ((y0 + 1) * W + x0) % len), env_px(img, ((y0 + 1) * W + x0 + 1) % len), ax), ay);
 }
-__device__ __forceinline__ uint32_t cdf_find(const float* cdf, uint32_t n, float u) {
-    uint32_t lo = 0, hi = n;
+// Largest i < n with cdf[i] <= u (cdf[0] = 0 <= u): a binary search of the
+// non-decreasing CDF, started from the guide table's bracket.  u in [0, 1)
+// and m a power of two make k / m <= u < (k + 1) / m exact, and the result
+// for u lies between the results for k / m and (k + 1) / m, which the guide
+// holds; so the search returns exactly what a search of all of [0, n) does.
+__device__ __forceinline__ uint32_t cdf_find(const float* cdf, uint32_t n, const uint32_t* guide, uint32_t m,
+                                             float u) {
+    uint32_t k = (uint32_t)(u * (float)m);
+    if (k >= m) k = m - 1;
+    uint32_t lo = __ldg(guide + k), hi = min(__ldg(guide + k + 1) + 1u, n);
     while (hi - lo > 1) {
         uint32_t mid = (lo + hi) >> 1;
         if (__ldg(cdf + mid) <= u) lo = mid; else hi = mid;
@@ -115,8 +123,9 @@ __device__ __forceinline__ float cell_density(const SceneView& s, uint32_t j, ui
     return __ldg(s.env_cell + (size_t)j * s.env_w + i) * s.env_density_scale / st;
 }
 __device__ bool env_sample(const SceneView& s, float u1, float u2, float u3, float u4, V3* dir, float* pdf) {
-    uint32_t j = cdf_find(s.env_marg, s.env_h, u1);
-    uint32_t i = cdf_find(s.env_cond + (size_t)j * (s.env_w + 1), s.env_w, u2);
+    uint32_t j = cdf_find(s.env_marg, s.env_h, s.env_gmarg, s.env_gm, u1);
+    uint32_t i = cdf_find(s.env_cond + (size_t)j * (s.env_w + 1), s.env_w, s.env_gcond + (size_t)j * (s.env_gc + 1),
+                          s.env_gc, u2);
     float theta = ((float)j + u3) * (PI_F / (float)s.env_h);
     float phi = ((float)i + u4) * (2.0f * PI_F / (float)s.env_w);
     float st = sinf(theta), ct = cosf(theta);
@@ -596,7 +605,7 @@ __device__ __forceinline__ uint32_t queue_append(bool want, uint32_t r, uint32_t
 }
 
 template <bool ONE>
-__global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
+__global__ void __launch_bounds__(256, 3) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;
     if (ONE) {
@@ -611,14 +620,34 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
     const uint32_t out_half = (k & 1) ? 0 : ps.cap;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
+    // the jobs this block's entries belong to (a contiguous range: job
+    // segments are concatenated); up to BIN_JOBS of them are copied to shared
+    // memory, so that every thread reads its job there instead of from the
+    // job table in global memory
+    __shared__ uint32_t s_rlo, s_nj;
+    __shared__ Job s_jobs[ONE ? 1 : BIN_JOBS];
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         const uint32_t i = i0 + threadIdx.x;
+        if (threadIdx.x == 0) {
+            const uint32_t last = min(i0 + blockDim.x, n) - 1u;
+            const uint32_t rlo = ONE ? 0u : find_job(pre, w.njobs, i0);
+            s_rlo = rlo;
+            s_nj = (ONE ? 0u : find_job(pre, w.njobs, last)) - rlo + 1u;
+        }
+        __syncthreads();
+        if (!ONE && s_nj <= BIN_JOBS) {
+            const uint32_t words = s_nj * (uint32_t)(sizeof(Job) / 4);
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(w.jobs + s_rlo);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(s_jobs);
+            for (uint32_t t = threadIdx.x; t < words; t += blockDim.x) dst[t] = src[t];
+            __syncthreads();
+        }
         bool cont = false, want_shadow = false;
         V3 new_o, new_d, sh_dir, sh_c;
         uint32_t p = 0, r = 0;
         if (i < n) {
             r = ONE ? 0u : find_job(pre, w.njobs, i);
-            const Job& j = ONE ? w.first : w.jobs[r];
+            const Job& j = ONE ? w.first : (s_nj <= BIN_JOBS ? s_jobs[r - s_rlo] : w.jobs[r]);
             const SceneView& s = j.view;
             const RenderParams& rp = j.rp;
             const float fc = rp.firefly_clamp;
@@ -807,13 +836,6 @@ __global__ void __launch_bounds__(256) k_shade(Wave w, PathState ps, uint32_t k,
         const uint32_t base_r = (ONE || i >= n) ? 0u : w.jobs[r].base;
         __shared__ uint32_t s_cnt[2][BIN_JOBS * 8];
         __shared__ uint32_t s_base[2][BIN_JOBS];
-        __shared__ uint32_t s_rlo, s_nj;
-        if (threadIdx.x == 0) {
-            const uint32_t last = min(i0 + blockDim.x, n) - 1u;
-            const uint32_t rlo = ONE ? 0u : find_job(pre, w.njobs, i0);
-            s_rlo = rlo;
-            s_nj = (ONE ? 0u : find_job(pre, w.njobs, last)) - rlo + 1u;
-        }
         for (uint32_t t = threadIdx.x; t < 2 * BIN_JOBS * 8; t += blockDim.x) (&s_cnt[0][0])[t] = 0u;
         __syncthreads();
         uint32_t cs = 0, ss = 0;

@@ -39,6 +39,7 @@ struct Job {
 };
 
 constexpr uint32_t MAX_JOBS = 256;                       // jobs per wavefront
+static_assert(sizeof(Job) % 4 == 0, "jobs are copied to shared memory as 32-bit words");
 constexpr uint32_t JOB_COUNTERS = 2 * MAX_DEPTH_SLOTS;   // [k] queue size, [M + k] shadow queue size
 
 // A wavefront: jobs[0..njobs) in device memory, their segments packed from slot 0.
