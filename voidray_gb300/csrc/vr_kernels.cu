@@ -449,6 +449,20 @@ __device__ __forceinline__ uint32_t find_job(const uint32_t* pre, uint32_t njobs
     return lo;
 }
 
+// A wave of at most STAGED_JOBS jobs has its job table copied to shared
+// memory by every block of a kernel that reads it per ray or path (the copy
+// is uniform across the block); larger waves read the table in global memory.
+constexpr uint32_t STAGED_JOBS = 8;
+__device__ __forceinline__ const Job* stage_jobs(const Wave& w, Job* sj) {
+    if (w.njobs > STAGED_JOBS) return w.jobs;
+    const uint32_t words = w.njobs * (uint32_t)(sizeof(Job) / 4);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(w.jobs);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(sj);
+    for (uint32_t t = threadIdx.x; t < words; t += blockDim.x) dst[t] = src[t];
+    __syncthreads();
+    return sj;
+}
+
 // Clears the wave's counters and fetch cursors; depth-0 queue size = paths.
 __global__ void k_wave_begin(Wave w, PathState ps) {
     const uint32_t n = w.njobs * JOB_COUNTERS;
@@ -464,15 +478,18 @@ __global__ void k_wave_begin(Wave w, PathState ps) {
 template <bool ONE>
 __global__ void k_raygen(Wave w, PathState ps) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
+    __shared__ Job sj[ONE ? 1 : STAGED_JOBS];
+    const Job* jobs = w.jobs;
     if (!ONE) {
         if (threadIdx.x == 0)
             for (uint32_t r = 0; r <= w.njobs; ++r) pre[r] = (r < w.njobs) ? w.jobs[r].base : w.total_paths;
         __syncthreads();
+        jobs = stage_jobs(w, sj);
     }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.total_paths; p += stride) {
         const uint32_t r = ONE ? 0u : find_job(pre, w.njobs, p);
-        const Job& j = ONE ? w.first : w.jobs[r];
+        const Job& j = ONE ? w.first : jobs[r];
         const SceneView& s = j.view;
         uint32_t pixel, sample;
         path_coords(j, p, pixel, sample);
@@ -557,8 +574,10 @@ __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_extend(Wave w, PathState
         job_prefix(ps.counts, k, w.njobs, pre);
         n = pre[w.njobs];
     }
+    __shared__ Job sj[ONE ? 1 : STAGED_JOBS];
+    const Job* jobs = ONE ? w.jobs : stage_jobs(w, sj);
     const uint32_t half = (k & 1) ? ps.cap : 0;
-    ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, w.jobs, pre, w.njobs, w.first.view.nodes,
+    ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, jobs, pre, w.njobs, w.first.view.nodes,
                      w.first.view.tris};
     persistent_trace<false, COUNT>(n, &ps.cursors[k], io, status, work);
 }
@@ -936,8 +955,10 @@ __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(Wave w, PathState
         job_prefix(ps.counts, MAX_DEPTH_SLOTS + k, w.njobs, pre);
         n = pre[w.njobs];
     }
+    __shared__ Job sj[ONE ? 1 : STAGED_JOBS];
+    const Job* jobs = ONE ? w.jobs : stage_jobs(w, sj);
     ShadowIo<ONE> io{ps,
-                     w.jobs,
+                     jobs,
                      pre,
                      w.njobs,
                      w.first.view.nodes,
