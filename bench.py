@@ -37,8 +37,10 @@ ROOT = Path(__file__).resolve().parent
 # from an ncu capture of all twelve k_extend launches of one 960x540 x 32 spp
 # frame of it (the same 2M-triangle scene and HDRI, 34.4M extend rays); the
 # bench scales them to its own launches by the extend rays per launch
-K_EXTEND_DRAM_BYTES_PER_RAY = 165.6
-K_EXTEND_L2_BYTES_PER_RAY = 1102.3
+# bytes a 4-wide node visit reads: six float4 of child boxes and one of child codes
+NODE_BYTES = 112
+K_EXTEND_DRAM_BYTES_PER_RAY = 149.9
+K_EXTEND_L2_BYTES_PER_RAY = 1005.1
 sys.path.insert(0, str(ROOT))
 
 CLOCK_FIELDS = ["uuid", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
@@ -229,7 +231,7 @@ def intersection_benchmark(args, hbm_peak, peak_source):
         nv, nt = C.c_uint64(), C.c_uint64()
         N.check(lib.vr_intersect_count_device(acc.handle, dr.data_ptr(), n_rays, any_hit, C.byref(nv), C.byref(nt),
                                               sh))
-        alg = 48 * n_rays + 64 * nv.value + 48 * nt.value
+        alg = 48 * n_rays + NODE_BYTES * nv.value + 48 * nt.value
         achieved = alg / (ms / 1e3) / 1e9
         out[name] = {"mrays_per_s": n_rays / (ms / 1e3) / 1e6, "ms_per_launch": ms, "launches": args.isect_reps,
                      "node_visits_per_ray": nv.value / n_rays, "tri_tests_per_ray": nt.value / n_rays,
@@ -757,12 +759,12 @@ def main():
         c1 = acc.stats()
         rays1 = c1.extend_rays - c0.extend_rays
         # algorithmic bytes of the extend (closest-hit) stage for one frame:
-        # 32 B ray in + 16 B hit out per ray, 64 B per inner-node visit, 48 B per triangle test
-        alg_bytes = 48 * rays1 + 64 * wk.extend_node_visits + 48 * wk.extend_tri_tests
+        # 32 B ray in + 16 B hit out per ray, 112 B per 4-wide node visit, 48 B per triangle test
+        alg_bytes = 48 * rays1 + NODE_BYTES * wk.extend_node_visits + 48 * wk.extend_tri_tests
         ext_ms_per_frame = ins.stage_ms[1] / args.steps
         ext_launches_per_frame = ins.stage_launches[1] / args.steps
         achieved = alg_bytes / (ext_ms_per_frame / 1e3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit BVH2 traversal)", "achieved": achieved,
+        roofline = {"bound": "hbm", "kernel": "k_extend (closest-hit 4-wide BVH traversal)", "achieved": achieved,
                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                     # dram__bytes_read.sum + dram__bytes_write.sum per k_extend launch: bytes per extend
                     # ray measured on a smaller frame of the same scene, times this run's extend rays per

@@ -11,6 +11,7 @@
 // differently).  Compiled with -ffp-contract=off: face normals and edge
 // vectors round exactly as the reference computes them.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -46,7 +47,8 @@ struct Box {
     }
 };
 
-constexpr int DEPTH_LIMIT = STACK_SIZE - 2;  // keeps the traversal stack in bounds
+constexpr int DEPTH_LIMIT = 62;  // keeps the BVH2 traversal stack (64 entries) in bounds
+constexpr int WIDE_STACK = 96;   // entries of the 4-wide traversal's stack
 constexpr double C_TRAV = 1.0, C_ISECT = 1.0;
 
 // Threads the BVH build may use: VR_BUILD_THREADS when set (>= 1), else the
@@ -467,6 +469,96 @@ void set_camera(SceneView& v, const vr_camera_desc& c) {
 }
 
 namespace {
+// 4-wide nodes collapsed from the flattened BVH2: a wide node holds the
+// children of a BVH2 node, and repeatedly the children of its inner child
+// with the largest surface area in place of that child, until it has four
+// (or only leaves are left).  Layout (8 x float4): for children 0/1 and
+// 2/3 the BVH2 pair layout (x lo/hi, y lo/hi per child, then both z
+// ranges), then the four child codes (>= 0 wide node, < 0 leaf code as in
+// the BVH2, 0x7fffffff an empty slot), then zeros.  Wide nodes are in
+// depth-first preorder.
+void collapse_wide(HostScene& hs) {
+    hs.wide.clear();
+    hs.wide_depth = 0;
+    const size_t nb2 = hs.nodes.size() / 4;
+    if (nb2 == 0) return;
+    auto code = [&](size_t p, int s) {
+        int32_t c;
+        const float f = s ? hs.nodes[4 * p + 3].y : hs.nodes[4 * p + 3].x;
+        std::memcpy(&c, &f, 4);
+        return c;
+    };
+    auto box = [&](size_t p, int s, float* lo, float* hi) {
+        const float4 a = hs.nodes[4 * p + s], z = hs.nodes[4 * p + 2];
+        lo[0] = a.x; hi[0] = a.y; lo[1] = a.z; hi[1] = a.w;
+        lo[2] = s ? z.z : z.x; hi[2] = s ? z.w : z.y;
+    };
+    auto area = [&](size_t p, int s) {
+        float lo[3], hi[3];
+        box(p, s, lo, hi);
+        const double dx = (double)hi[0] - lo[0], dy = (double)hi[1] - lo[1], dz = (double)hi[2] - lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    };
+    struct Entry {
+        uint32_t p;
+        int s;
+    };
+    std::vector<std::array<Entry, 4>> sets;
+    std::vector<uint8_t> counts;
+    std::vector<int32_t> wide_of(nb2, -1);
+    std::vector<std::pair<uint32_t, uint32_t>> stack{{0u, 1u}};  // (BVH2 node, depth)
+    while (!stack.empty()) {
+        const auto [f, depth] = stack.back();
+        stack.pop_back();
+        hs.wide_depth = std::max(hs.wide_depth, depth);
+        wide_of[f] = (int32_t)sets.size();
+        std::array<Entry, 4> e{};
+        int n = 2;
+        e[0] = {f, 0};
+        e[1] = {f, 1};
+        while (n < 4) {
+            int best = -1;
+            double ba = -1.0;
+            for (int k = 0; k < n; ++k)
+                if (code(e[k].p, e[k].s) >= 0 && area(e[k].p, e[k].s) > ba) {
+                    ba = area(e[k].p, e[k].s);
+                    best = k;
+                }
+            if (best < 0) break;
+            const uint32_t g = (uint32_t)code(e[best].p, e[best].s);
+            for (int k = n; k > best + 1; --k) e[k] = e[k - 1];
+            e[best] = {g, 0};
+            e[best + 1] = {g, 1};
+            ++n;
+        }
+        sets.push_back(e);
+        counts.push_back((uint8_t)n);
+        for (int k = n - 1; k >= 0; --k)
+            if (code(e[k].p, e[k].s) >= 0) stack.push_back({(uint32_t)code(e[k].p, e[k].s), depth + 1});
+    }
+    hs.wide.assign(sets.size() * 8, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (size_t w = 0; w < sets.size(); ++w) {
+        float lo[4][3] = {}, hi[4][3] = {};
+        int32_t c[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        for (int k = 0; k < counts[w]; ++k) {
+            const Entry& en = sets[w][k];
+            box(en.p, en.s, lo[k], hi[k]);
+            const int32_t cc = code(en.p, en.s);
+            c[k] = cc >= 0 ? wide_of[cc] : cc;
+        }
+        float4* o = &hs.wide[8 * w];
+        for (int pr = 0; pr < 2; ++pr) {
+            const int a = 2 * pr, b = 2 * pr + 1;
+            o[3 * pr + 0] = make_float4(lo[a][0], hi[a][0], lo[a][1], hi[a][1]);
+            o[3 * pr + 1] = make_float4(lo[b][0], hi[b][0], lo[b][1], hi[b][1]);
+            o[3 * pr + 2] = make_float4(lo[a][2], hi[a][2], lo[b][2], hi[b][2]);
+        }
+        float fc[4];
+        std::memcpy(fc, c, sizeof fc);
+        o[6] = make_float4(fc[0], fc[1], fc[2], fc[3]);
+    }
+}
+
 vr_status build_host_scene_impl(const vr_scene_desc* d, HostScene& hs, std::string& err);
 vr_status validate_host_scene_impl(const HostScene& hs, std::string& err);
 
@@ -747,6 +839,7 @@ vr_status build_host_scene_impl(const vr_scene_desc* d, HostScene& hs, std::stri
             }
         }
         hs.sah_cost = sah;
+        collapse_wide(hs);
     }
     // environment
     SceneView& v = hs.view;
@@ -826,7 +919,7 @@ vr_status validate_host_scene_impl(const HostScene& hs, std::string& err) {
         stack.pop_back();
         if (it.node < 0 || (uint64_t)it.node >= nn) { err = "child index out of range"; return VR_ERR_INVALID; }
         if (visited[it.node]++) { err = "node reached twice"; return VR_ERR_INVALID; }
-        if (it.depth >= (uint32_t)STACK_SIZE) { err = "tree deeper than the traversal stack"; return VR_ERR_INVALID; }
+        if (it.depth >= (uint32_t)(DEPTH_LIMIT + 2)) { err = "tree deeper than the traversal stack"; return VR_ERR_INVALID; }
         const float4* n = &hs.nodes[4 * (size_t)it.node];
         float clo[2][3] = {{n[0].x, n[0].z, n[2].x}, {n[1].x, n[1].z, n[2].z}};
         float chi[2][3] = {{n[0].y, n[0].w, n[2].y}, {n[1].y, n[1].w, n[2].w}};
@@ -881,6 +974,64 @@ vr_status validate_host_scene_impl(const HostScene& hs, std::string& err) {
         if (!visited[i]) { err = "unreachable node"; return VR_ERR_INVALID; }
     for (uint64_t p = 0; p < np; ++p)
         if (seen[p] != 1) { err = "triangle " + std::to_string(p) + " appears " + std::to_string(seen[p]) + " times"; return VR_ERR_INVALID; }
+    // the 4-wide nodes: a tree over every triangle once (the single-leaf
+    // scene's duplicated leaf aside), child codes in range, every leaf's
+    // triangles inside its box, stack use within the wide traversal's stack
+    const uint64_t nw = hs.wide.size() / 8;
+    if (hs.wide.size() % 8 || (nn > 0 && nw == 0)) { err = "wide node array size"; return VR_ERR_INVALID; }
+    if (nw) {
+        if (3ull * hs.wide_depth + 1 > (uint64_t)WIDE_STACK) { err = "wide tree deeper than the traversal stack"; return VR_ERR_INVALID; }
+        std::vector<uint8_t> wvis(nw, 0);
+        std::vector<uint32_t> wseen(np, 0);
+        std::vector<uint32_t> wst{0};
+        while (!wst.empty()) {
+            const uint32_t w = wst.back();
+            wst.pop_back();
+            if (wvis[w]) { err = "wide node reached twice"; return VR_ERR_INVALID; }
+            wvis[w] = 1;
+            const float4* o = &hs.wide[8 * (size_t)w];
+            int32_t cd[4];
+            std::memcpy(cd, &o[6], sizeof cd);
+            for (int c = 0; c < 4; ++c) {
+                if (cd[c] == 0x7fffffff) continue;
+                const float4 xy = o[3 * (c >> 1) + (c & 1)], z = o[3 * (c >> 1) + 2];
+                const float lo[3] = {xy.x, xy.z, (c & 1) ? z.z : z.x}, hi[3] = {xy.y, xy.w, (c & 1) ? z.w : z.y};
+                if (cd[c] >= 0) {
+                    if ((uint64_t)cd[c] >= nw) { err = "wide child index out of range"; return VR_ERR_INVALID; }
+                    wst.push_back((uint32_t)cd[c]);
+                    continue;
+                }
+                const uint32_t code = ~(uint32_t)cd[c];
+                const uint32_t first = code >> 4, count = (code & 15u) + 1u;
+                if ((uint64_t)first + count > np) { err = "wide leaf range out of bounds"; return VR_ERR_INVALID; }
+                for (uint32_t k = 0; k < count; ++k) {
+                    const float4* t = &hs.tris[3 * ((size_t)first + k)];
+                    uint32_t pid;
+                    std::memcpy(&pid, &t[0].w, 4);
+                    if (pid >= np) { err = "prim id out of range"; return VR_ERR_INVALID; }
+                    wseen[pid]++;
+                    const float vx[3][3] = {{t[0].x, t[0].y, t[0].z},
+                                            {t[0].x + t[1].x, t[0].y + t[1].y, t[0].z + t[1].z},
+                                            {t[0].x + t[2].x, t[0].y + t[2].y, t[0].z + t[2].z}};
+                    for (int q = 0; q < 3; ++q)
+                        for (int a = 0; a < 3; ++a) {
+                            const float slack = 4e-6f * std::max(1.0f, std::fabs(vx[q][a]));
+                            if (vx[q][a] < lo[a] - slack || vx[q][a] > hi[a] + slack) {
+                                err = "triangle outside its wide leaf box";
+                                return VR_ERR_INVALID;
+                            }
+                        }
+                }
+            }
+        }
+        for (uint64_t i = 0; i < nw; ++i)
+            if (!wvis[i]) { err = "unreachable wide node"; return VR_ERR_INVALID; }
+        for (uint64_t p = 0; p < np; ++p)
+            if (wseen[p] != 1 && !(np <= 16 && wseen[p] == 2)) {
+                err = "triangle " + std::to_string(p) + " appears " + std::to_string(wseen[p]) + " times in the wide tree";
+                return VR_ERR_INVALID;
+            }
+    }
     return VR_OK;
 }
 }  // namespace

@@ -539,7 +539,7 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(fail(VR_ERR_CUDA, "stream creation failed"));
     s->view = hs.view;
-    if ((st = upload(s, hs.nodes, &s->view.nodes)) != VR_OK) return cleanup(st);
+    if ((st = upload(s, hs.wide, &s->view.nodes)) != VR_OK) return cleanup(st);  // the 4-wide tree
     if ((st = upload(s, hs.tris, &s->view.tris)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.shade, &s->view.shade)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.uvs, &s->view.uvs)) != VR_OK) return cleanup(st);
@@ -570,7 +570,7 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if (cudaMemset(s->status, 0, 64) != cudaSuccess || cudaMemset(s->totals, 0, 64) != cudaSuccess)
         return cleanup(fail(VR_ERR_CUDA, "memset"));
     s->info.num_triangles = hs.num_prims;
-    s->info.num_nodes = hs.nodes.size() / 4;
+    s->info.num_nodes = hs.wide.size() / 8;
     s->info.device_bytes = s->scene_bytes;
     s->info.max_depth = hs.max_depth;
     s->info.max_leaf = hs.max_leaf;
@@ -590,9 +590,9 @@ vr_status vr_scene_validate(const vr_scene_desc* desc, vr_scene_info* info) {
     if (info) {
         *info = vr_scene_info{};
         info->num_triangles = hs.num_prims;
-        info->num_nodes = hs.nodes.size() / 4;
+        info->num_nodes = hs.wide.size() / 8;
         // every array vr_scene_create uploads (textures and materials included)
-        info->device_bytes = hs.nodes.size() * sizeof(float4) + hs.tris.size() * sizeof(float4) +
+        info->device_bytes = hs.wide.size() * sizeof(float4) + hs.tris.size() * sizeof(float4) +
                              hs.shade.size() * sizeof(float4) + hs.uvs.size() * sizeof(float2) +
                              hs.materials.size() * sizeof(hs.materials[0]) + hs.analytic.size() * sizeof(float4) +
                              hs.tex_info.size() * sizeof(int4) + hs.texels.size() * sizeof(float) +

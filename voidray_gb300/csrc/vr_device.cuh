@@ -16,7 +16,7 @@ constexpr float PI_F = 3.14159265358979323846f;
 constexpr float INF_F = __builtin_huge_valf();
 constexpr float SCENE_TMIN = 0.00001f;  // SceneAcceleration::hit (scene.rs:183)
 constexpr int REJECT_TRIES = 64;        // bound on the reference's rejection loops
-constexpr int STACK_SIZE = 64;          // traversal stack; the builder keeps depth below it
+constexpr int STACK_SIZE = 96;          // traversal stack entries (the builder keeps 3 x wide depth + 1 below it)
 constexpr uint32_t MISS = 0xFFFFFFFFu;
 
 // device status word bits
@@ -35,13 +35,8 @@ struct Material {  // same layout as vr_material
     float mix_factor;
 };
 
-// Flattened BVH2: node = 4 x float4 (64 bytes)
-//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   n3 = (c0 ref, c1 ref, c0 count, c1 count) as int; count > 0: leaf with
-//        `count` triangles from index `ref`; count == 0: inner node `ref`;
-//        ref < 0: empty child.
+// BVH: 4-wide nodes of 8 x float4 (128 bytes; layout in vr_traverse.cuh),
+// node 0 the root; leaves are ranges of at most 16 triangles.
 // Triangle = 3 x float4 (48 bytes) in leaf order: (v0, prim id bits),
 // (v1 - v0, 0), (v2 - v0, 0); the edges are the f32 differences the
 // reference computes in Triangle::hit (mesh.rs:150-151).

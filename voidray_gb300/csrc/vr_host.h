@@ -29,7 +29,9 @@ struct EnvTables {
 
 // Everything vr_scene_create uploads, laid out as the kernels read it.
 struct HostScene {
-    std::vector<float4> nodes;  // 4 per BVH2 node
+    std::vector<float4> nodes;  // 4 per BVH2 node (the SAH build; collapsed into `wide`, not uploaded)
+    std::vector<float4> wide;   // 8 per 4-wide node: the tree the kernels traverse
+    uint32_t wide_depth = 0;
     std::vector<float4> tris;   // 3 per triangle, leaf order
     std::vector<float4> shade;  // 4 per prim, global id order
     std::vector<float2> uvs;    // 3 per prim, empty if no mesh has uvs

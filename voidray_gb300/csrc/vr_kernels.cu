@@ -575,11 +575,17 @@ __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_extend(Wave w, PathState
         n = pre[w.njobs];
     }
     __shared__ Job sj[ONE ? 1 : STAGED_JOBS];
-    const Job* jobs = ONE ? w.jobs : stage_jobs(w, sj);
     const uint32_t half = (k & 1) ? ps.cap : 0;
-    ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, jobs, pre, w.njobs, w.first.view.nodes,
-                     w.first.view.tris};
-    persistent_trace<false, COUNT>(n, &ps.cursors[k], io, status, work);
+    if (!ONE && w.njobs <= STAGED_JOBS) {  // a separate inlined copy that reads the jobs from shared memory
+        stage_jobs(w, sj);
+        ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, sj, pre, w.njobs, w.first.view.nodes,
+                         w.first.view.tris};
+        persistent_trace<false, COUNT>(n, &ps.cursors[k], io, status, work);
+    } else {
+        ExtendIo<ONE> io{ps.q_org + half, ps.q_dir + half, ps.hits, w.jobs, pre, w.njobs, w.first.view.nodes,
+                         w.first.view.tris};
+        persistent_trace<false, COUNT>(n, &ps.cursors[k], io, status, work);
+    }
 }
 
 // Reference estimator: the path's radiance is the recursion of
@@ -623,8 +629,191 @@ __device__ __forceinline__ uint32_t queue_append(bool want, uint32_t r, uint32_t
     return slot;
 }
 
+// One live path at depth k: the hit's material (or the environment on a miss),
+// next event estimation, the scatter and Russian roulette; returns the
+// continuation and shadow rays to append.  `j` is the path's job, read from
+// the kernel parameters, shared memory or the job table (the caller picks, so
+// that each inlined copy loads from one known address space).
+__device__ __forceinline__ void shade_path(const Job& j, const PathState& ps, uint32_t k, uint32_t in_half,
+                                           uint32_t local, unsigned long long* retired, bool& cont,
+                                           bool& want_shadow, V3& new_o, V3& new_d, V3& sh_dir, V3& sh_c,
+                                           uint32_t& p) {
+        const SceneView& s = j.view;
+        const RenderParams& rp = j.rp;
+        const float fc = rp.firefly_clamp;
+        const bool nee_mode = rp.estimator == 1;
+        const bool last = (k + 1 >= rp.max_bounces);
+        const uint32_t q = in_half + j.base + local;
+        p = ps.q_path[q];
+        const float4 ro4 = ps.q_org[q], rd4 = ps.q_dir[q];
+        const V3 ro = xyz(ro4), rd = xyz(rd4);
+        float4 hh = ps.hits[q - in_half];
+        uint32_t prim = __float_as_uint(hh.x);
+        if (s.num_analytic) {  // SceneAcceleration::hit keeps the nearest surface, analytic ones included
+            float tb = prim == MISS ? INF_F : hh.y;
+            uint32_t pb = prim;
+            analytic_closest(s.analytic, s.num_analytic, s.num_tris, ro, rd, ro4.w, rd4.w, tb, pb);
+            if (pb != prim) {
+                prim = pb;
+                hh = make_float4(__uint_as_float(pb), tb, 0.0f, 0.0f);
+            }
+        }
+        uint32_t pixel, sample;
+        path_coords(j, p, pixel, sample);
+        Rng rng;
+        rng.inc = pcg_inc(sample, pixel);
+        rng.state = ps.rng[p];
+        const float4 thr4 = ps.thr[p];
+        V3 T = xyz(thr4);
+        float prev_pdf = thr4.w;
+        if (prim == MISS) {
+            const V3 le = env_eval(s, rd);
+            if (k == 0 && j.aov_psum) {  // first-hit AOVs of a miss: environment (clamped), no normal
+                ps.aov[p] = make_float4(fminf(le.x, 1.0f), fminf(le.y, 1.0f), fminf(le.z, 1.0f), 0.0f);
+                ps.aov[ps.cap + p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            if (nee_mode) {
+                float wgt = 1.0f;
+                if (prev_pdf >= 0.0f && s.env_is) {
+                    float pl = env_pdf(s, rd);
+                    float a = prev_pdf * prev_pdf, b = pl * pl;
+                    wgt = a / (a + b);
+                }
+                rad_add(ps, p, clampc(vmul(T, le) * wgt, fc));
+            } else {
+                unwind(ps, p, k, le, fc);
+            }
+        } else {
+            const float t = hh.y;
+            const V3 point = ro + rd * t;
+            Material m;
+            V3 normal;
+            float uvx = 0.0f, uvy = 0.0f;  // HitRecord::uv
+            if (prim < s.num_tris) {
+                // shading record and normal (mesh.rs:176-188, ray.rs:34-49)
+                const float4* sh = s.shade + 4 * (size_t)prim;
+                const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3);
+                m = s.materials[__float_as_uint(s0.w)];
+                const float u = hh.z, v = hh.w;
+                const float wb = 1.0f - u - v;
+                normal = u * xyz(s1) + v * xyz(s2) + wb * xyz(s0);
+                const V3 fnm = xyz(s3);
+                const float ang = acosf(dot(normal, fnm) / (sqrtf(mag2(normal)) * sqrtf(mag2(fnm))));
+                if (ang > 30.0f * PI_F / 180.0f) normal = fnm;
+                if (s.uvs && s.num_textures) {  // u v1.uv + v v2.uv + (1 - u - v) v0.uv (mesh.rs:177)
+                    const float2 t0 = __ldg(s.uvs + 3 * (size_t)prim), t1 = __ldg(s.uvs + 3 * (size_t)prim + 1),
+                                 t2 = __ldg(s.uvs + 3 * (size_t)prim + 2);
+                    uvx = u * t1.x + v * t2.x + wb * t0.x;
+                    uvy = u * t1.y + v * t2.y + wb * t0.y;
+                }
+            } else {
+                // analytic surface: sphere normal (p - c) / r, uv 0; ground plane +y, uv (x, z)
+                // (surfaces.rs:74-75, 98-102)
+                const float4 a0 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris));
+                const float4 a1 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris) + 1);
+                m = s.materials[__float_as_uint(a1.y)];
+                const bool sphere = __float_as_uint(a1.x) == A_SPHERE;
+                normal = sphere ? (point - v3(a0.x, a0.y, a0.z)) / a0.w : v3(0.0f, 1.0f, 0.0f);
+                if (!sphere) {
+                    uvx = point.x;
+                    uvy = point.z;
+                }
+            }
+            resolve_mix(s, m, rng);
+            SurfHit hit;
+            hit.point = point;
+            hit.t = t;
+            hit.front = dot(rd, normal) < 0.0f;
+            hit.normal = hit.front ? normal : -normal;
+            hit.snormal = hit.normal;
+            if (m.albedo_tex >= 0) {  // ColorType::Texture: the albedo is the texture at the hit's uv
+                const V3 c = tex_sample(s, m.albedo_tex, uvx, uvy);
+                m.color[0] = c.x;
+                m.color[1] = c.y;
+                m.color[2] = c.z;
+            }
+            if (m.normal_tex >= 0) hit.snormal = tex_sample(s, m.normal_tex, uvx, uvy);
+            if (k == 0 && j.aov_psum) {  // first-hit AOVs: surface colour (1 for glass), shading normal
+                const V3 al = (m.kind == M_DIEL) ? v3(1.0f, 1.0f, 1.0f)
+                                                 : v3(fminf(m.color[0], 1.0f), fminf(m.color[1], 1.0f),
+                                                      fminf(m.color[2], 1.0f));
+                ps.aov[p] = make_float4(al.x, al.y, al.z, 0.0f);
+                ps.aov[ps.cap + p] = make_float4(hit.normal.x, hit.normal.y, hit.normal.z, 0.0f);
+            }
+            if (rp.render_mode != 1) {
+                const V3 nn = normalize(hit.normal);
+                const V3 c = (0.5f * nn) + v3(1.0f, 1.0f, 1.0f) * 0.5f;
+                if (nee_mode) rad_add(ps, p, clampc(vmul(T, c), fc));
+                else unwind(ps, p, k, clampc(c, fc), fc);
+            } else {
+                // next event estimation at Lambertian vertices whose scatter is
+                // cosine-distributed around the shading normal (not with a normal map)
+                const bool lamb = (m.kind == M_LAMB) && m.normal_tex < 0 &&
+                                  !(hit.normal.x == 0.0f && hit.normal.y == 0.0f && hit.normal.z == 0.0f);
+                if (nee_mode && lamb && s.env_is) {
+                    const float u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform(), u4 = rng.uniform();
+                    V3 dl;
+                    float pl;
+                    if (env_sample(s, u1, u2, u3, u4, &dl, &pl)) {
+                        const float cosl = dot(hit.normal, dl);
+                        if (cosl > 0.0f) {
+                            const float pb = cosl / PI_F;
+                            const float a = pl * pl, b = pb * pb;
+                            const float wgt = a / (a + b);
+                            const float fscale = cosl / PI_F * wgt / pl;
+                            sh_c = vmul(vmul(T, load3(m.color)), env_eval(s, dl)) * fscale;
+                            sh_dir = dl;
+                            want_shadow = true;
+                        }
+                    }
+                }
+                V3 att, nd;
+                if (!scatter(m, ro, rd, hit, rng, &att, &nd)) {
+                    // instrumented runs count the metal paths absorbed by the bounded rejection loop
+                    if (retired && m.kind == M_METAL) atomicAdd(retired + 1, 1ull);
+                    if (nee_mode) rad_add(ps, p, clampc(vmul(T, att), fc));
+                    else unwind(ps, p, k, clampc(att, fc), fc);
+                } else {
+                    V3 tn = vmul(T, att);
+                    if (nee_mode) prev_pdf = lamb ? dot(hit.normal, nd) / PI_F : -1.0f;
+                    bool alive = true;
+                    if (rp.rr_depth != 0 && k >= rp.rr_depth) {
+                        const float qq = fminf(max3(tn), 0.95f);
+                        const float ur = rng.uniform();
+                        if (!(ur < qq)) {
+                            alive = false;
+                        } else {
+                            att = att / qq;
+                            tn = tn / qq;
+                        }
+                    }
+                    if (!nee_mode) {
+                        if (!alive || last) {
+                            // continuation not traced: it contributes BLACK
+                            const V3 lk = clampc(vmul(att, v3(0.0f, 0.0f, 0.0f)), fc);
+                            unwind(ps, p, k, lk, fc);
+                        } else {
+                            float* a = ps.att + (size_t)k * 3 * ps.cap;
+                            a[p] = att.x;
+                            a[ps.cap + p] = att.y;
+                            a[2 * ps.cap + p] = att.z;
+                        }
+                    }
+                    if (alive && !last) {
+                        cont = true;
+                        new_o = hit.point;
+                        new_d = nd;
+                        ps.thr[p] = make_float4(tn.x, tn.y, tn.z, prev_pdf);
+                    }
+                }
+                if (want_shadow) new_o = hit.point;
+            }
+        }
+        ps.rng[p] = rng.state;
+}
+
 template <bool ONE>
-__global__ void __launch_bounds__(256, 3) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
+__global__ void __launch_bounds__(256, ONE ? 3 : 2) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;
     if (ONE) {
@@ -666,179 +855,15 @@ __global__ void __launch_bounds__(256, 3) k_shade(Wave w, PathState ps, uint32_t
         uint32_t p = 0, r = 0;
         if (i < n) {
             r = ONE ? 0u : find_job(pre, w.njobs, i);
-            const Job& j = ONE ? w.first : (s_nj <= BIN_JOBS ? s_jobs[r - s_rlo] : w.jobs[r]);
-            const SceneView& s = j.view;
-            const RenderParams& rp = j.rp;
-            const float fc = rp.firefly_clamp;
-            const bool nee_mode = rp.estimator == 1;
-            const bool last = (k + 1 >= rp.max_bounces);
-            const uint32_t q = in_half + j.base + (i - pre[r]);
-            p = ps.q_path[q];
-            const float4 ro4 = ps.q_org[q], rd4 = ps.q_dir[q];
-            const V3 ro = xyz(ro4), rd = xyz(rd4);
-            float4 hh = ps.hits[q - in_half];
-            uint32_t prim = __float_as_uint(hh.x);
-            if (s.num_analytic) {  // SceneAcceleration::hit keeps the nearest surface, analytic ones included
-                float tb = prim == MISS ? INF_F : hh.y;
-                uint32_t pb = prim;
-                analytic_closest(s.analytic, s.num_analytic, s.num_tris, ro, rd, ro4.w, rd4.w, tb, pb);
-                if (pb != prim) {
-                    prim = pb;
-                    hh = make_float4(__uint_as_float(pb), tb, 0.0f, 0.0f);
-                }
-            }
-            uint32_t pixel, sample;
-            path_coords(j, p, pixel, sample);
-            Rng rng;
-            rng.inc = pcg_inc(sample, pixel);
-            rng.state = ps.rng[p];
-            const float4 thr4 = ps.thr[p];
-            V3 T = xyz(thr4);
-            float prev_pdf = thr4.w;
-            if (prim == MISS) {
-                const V3 le = env_eval(s, rd);
-                if (k == 0 && j.aov_psum) {  // first-hit AOVs of a miss: environment (clamped), no normal
-                    ps.aov[p] = make_float4(fminf(le.x, 1.0f), fminf(le.y, 1.0f), fminf(le.z, 1.0f), 0.0f);
-                    ps.aov[ps.cap + p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                }
-                if (nee_mode) {
-                    float wgt = 1.0f;
-                    if (prev_pdf >= 0.0f && s.env_is) {
-                        float pl = env_pdf(s, rd);
-                        float a = prev_pdf * prev_pdf, b = pl * pl;
-                        wgt = a / (a + b);
-                    }
-                    rad_add(ps, p, clampc(vmul(T, le) * wgt, fc));
-                } else {
-                    unwind(ps, p, k, le, fc);
-                }
-            } else {
-                const float t = hh.y;
-                const V3 point = ro + rd * t;
-                Material m;
-                V3 normal;
-                float uvx = 0.0f, uvy = 0.0f;  // HitRecord::uv
-                if (prim < s.num_tris) {
-                    // shading record and normal (mesh.rs:176-188, ray.rs:34-49)
-                    const float4* sh = s.shade + 4 * (size_t)prim;
-                    const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3);
-                    m = s.materials[__float_as_uint(s0.w)];
-                    const float u = hh.z, v = hh.w;
-                    const float wb = 1.0f - u - v;
-                    normal = u * xyz(s1) + v * xyz(s2) + wb * xyz(s0);
-                    const V3 fnm = xyz(s3);
-                    const float ang = acosf(dot(normal, fnm) / (sqrtf(mag2(normal)) * sqrtf(mag2(fnm))));
-                    if (ang > 30.0f * PI_F / 180.0f) normal = fnm;
-                    if (s.uvs && s.num_textures) {  // u v1.uv + v v2.uv + (1 - u - v) v0.uv (mesh.rs:177)
-                        const float2 t0 = __ldg(s.uvs + 3 * (size_t)prim), t1 = __ldg(s.uvs + 3 * (size_t)prim + 1),
-                                     t2 = __ldg(s.uvs + 3 * (size_t)prim + 2);
-                        uvx = u * t1.x + v * t2.x + wb * t0.x;
-                        uvy = u * t1.y + v * t2.y + wb * t0.y;
-                    }
-                } else {
-                    // analytic surface: sphere normal (p - c) / r, uv 0; ground plane +y, uv (x, z)
-                    // (surfaces.rs:74-75, 98-102)
-                    const float4 a0 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris));
-                    const float4 a1 = __ldg(s.analytic + 2 * (size_t)(prim - s.num_tris) + 1);
-                    m = s.materials[__float_as_uint(a1.y)];
-                    const bool sphere = __float_as_uint(a1.x) == A_SPHERE;
-                    normal = sphere ? (point - v3(a0.x, a0.y, a0.z)) / a0.w : v3(0.0f, 1.0f, 0.0f);
-                    if (!sphere) {
-                        uvx = point.x;
-                        uvy = point.z;
-                    }
-                }
-                resolve_mix(s, m, rng);
-                SurfHit hit;
-                hit.point = point;
-                hit.t = t;
-                hit.front = dot(rd, normal) < 0.0f;
-                hit.normal = hit.front ? normal : -normal;
-                hit.snormal = hit.normal;
-                if (m.albedo_tex >= 0) {  // ColorType::Texture: the albedo is the texture at the hit's uv
-                    const V3 c = tex_sample(s, m.albedo_tex, uvx, uvy);
-                    m.color[0] = c.x;
-                    m.color[1] = c.y;
-                    m.color[2] = c.z;
-                }
-                if (m.normal_tex >= 0) hit.snormal = tex_sample(s, m.normal_tex, uvx, uvy);
-                if (k == 0 && j.aov_psum) {  // first-hit AOVs: surface colour (1 for glass), shading normal
-                    const V3 al = (m.kind == M_DIEL) ? v3(1.0f, 1.0f, 1.0f)
-                                                     : v3(fminf(m.color[0], 1.0f), fminf(m.color[1], 1.0f),
-                                                          fminf(m.color[2], 1.0f));
-                    ps.aov[p] = make_float4(al.x, al.y, al.z, 0.0f);
-                    ps.aov[ps.cap + p] = make_float4(hit.normal.x, hit.normal.y, hit.normal.z, 0.0f);
-                }
-                if (rp.render_mode != 1) {
-                    const V3 nn = normalize(hit.normal);
-                    const V3 c = (0.5f * nn) + v3(1.0f, 1.0f, 1.0f) * 0.5f;
-                    if (nee_mode) rad_add(ps, p, clampc(vmul(T, c), fc));
-                    else unwind(ps, p, k, clampc(c, fc), fc);
-                } else {
-                    // next event estimation at Lambertian vertices whose scatter is
-                    // cosine-distributed around the shading normal (not with a normal map)
-                    const bool lamb = (m.kind == M_LAMB) && m.normal_tex < 0 &&
-                                      !(hit.normal.x == 0.0f && hit.normal.y == 0.0f && hit.normal.z == 0.0f);
-                    if (nee_mode && lamb && s.env_is) {
-                        const float u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform(), u4 = rng.uniform();
-                        V3 dl;
-                        float pl;
-                        if (env_sample(s, u1, u2, u3, u4, &dl, &pl)) {
-                            const float cosl = dot(hit.normal, dl);
-                            if (cosl > 0.0f) {
-                                const float pb = cosl / PI_F;
-                                const float a = pl * pl, b = pb * pb;
-                                const float wgt = a / (a + b);
-                                const float fscale = cosl / PI_F * wgt / pl;
-                                sh_c = vmul(vmul(T, load3(m.color)), env_eval(s, dl)) * fscale;
-                                sh_dir = dl;
-                                want_shadow = true;
-                            }
-                        }
-                    }
-                    V3 att, nd;
-                    if (!scatter(m, ro, rd, hit, rng, &att, &nd)) {
-                        // instrumented runs count the metal paths absorbed by the bounded rejection loop
-                        if (retired && m.kind == M_METAL) atomicAdd(retired + 1, 1ull);
-                        if (nee_mode) rad_add(ps, p, clampc(vmul(T, att), fc));
-                        else unwind(ps, p, k, clampc(att, fc), fc);
-                    } else {
-                        V3 tn = vmul(T, att);
-                        if (nee_mode) prev_pdf = lamb ? dot(hit.normal, nd) / PI_F : -1.0f;
-                        bool alive = true;
-                        if (rp.rr_depth != 0 && k >= rp.rr_depth) {
-                            const float qq = fminf(max3(tn), 0.95f);
-                            const float ur = rng.uniform();
-                            if (!(ur < qq)) {
-                                alive = false;
-                            } else {
-                                att = att / qq;
-                                tn = tn / qq;
-                            }
-                        }
-                        if (!nee_mode) {
-                            if (!alive || last) {
-                                // continuation not traced: it contributes BLACK
-                                const V3 lk = clampc(vmul(att, v3(0.0f, 0.0f, 0.0f)), fc);
-                                unwind(ps, p, k, lk, fc);
-                            } else {
-                                float* a = ps.att + (size_t)k * 3 * ps.cap;
-                                a[p] = att.x;
-                                a[ps.cap + p] = att.y;
-                                a[2 * ps.cap + p] = att.z;
-                            }
-                        }
-                        if (alive && !last) {
-                            cont = true;
-                            new_o = hit.point;
-                            new_d = nd;
-                            ps.thr[p] = make_float4(tn.x, tn.y, tn.z, prev_pdf);
-                        }
-                    }
-                    if (want_shadow) new_o = hit.point;
-                }
-            }
-            ps.rng[p] = rng.state;
+            const uint32_t local = i - pre[r];
+            if (ONE)
+                shade_path(w.first, ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d, sh_dir, sh_c, p);
+            else if (s_nj <= BIN_JOBS)
+                shade_path(s_jobs[r - s_rlo], ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d,
+                           sh_dir, sh_c, p);
+            else
+                shade_path(w.jobs[r], ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d, sh_dir,
+                           sh_c, p);
         }
         // queue conservation (instrumented runs): every path that does not
         // continue is retired here, exactly once
@@ -956,17 +981,22 @@ __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(Wave w, PathState
         n = pre[w.njobs];
     }
     __shared__ Job sj[ONE ? 1 : STAGED_JOBS];
-    const Job* jobs = ONE ? w.jobs : stage_jobs(w, sj);
-    ShadowIo<ONE> io{ps,
-                     jobs,
-                     pre,
-                     w.njobs,
-                     w.first.view.nodes,
-                     w.first.view.tris,
-                     w.first.rp.firefly_clamp,
-                     w.first.view.analytic,
-                     w.first.view.num_analytic};
-    persistent_trace<true, COUNT>(n, &ps.cursors[MAX_DEPTH_SLOTS + k], io, status, work);
+    const bool staged = !ONE && w.njobs <= STAGED_JOBS;
+    if (staged) stage_jobs(w, sj);
+    auto run = [&](const Job* jobs) {
+        ShadowIo<ONE> io{ps,
+                         jobs,
+                         pre,
+                         w.njobs,
+                         w.first.view.nodes,
+                         w.first.view.tris,
+                         w.first.rp.firefly_clamp,
+                         w.first.view.analytic,
+                         w.first.view.num_analytic};
+        persistent_trace<true, COUNT>(n, &ps.cursors[MAX_DEPTH_SLOTS + k], io, status, work);
+    };
+    if (staged) run(sj);  // a separate inlined copy that reads the jobs from shared memory
+    else run(w.jobs);
 }
 
 // Per-pixel running sum, in sample order, of each job's paths of this wave

@@ -1,21 +1,25 @@
-// vr_traverse.cuh — BVH2 traversal of the sm_103a kernels (closest and any hit).
+// vr_traverse.cuh — 4-wide BVH traversal of the sm_103a kernels (closest and any hit).
 //
-// Node layout (64 bytes, four 128-bit loads):
-//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   n3 = (code0, code1, count0, count1); code >= 0: inner node index,
-//        code < 0: leaf ~(first << 4 | count - 1) over the leaf-ordered
-//        triangle array (3 x float4 per triangle: v0 | prim id, e1, e2).
+// Node layout (128 bytes; seven 128-bit loads):
+//   f[0] = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)   f[3] = the same for c2
+//   f[1] = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)   f[4] = the same for c3
+//   f[2] = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)   f[5] = the same for c2, c3
+//   f[6] = (code0, code1, code2, code3); code >= 0: wide node index,
+//          code < 0: leaf ~(first << 4 | count - 1) over the leaf-ordered
+//          triangle array (3 x float4 per triangle: v0 | prim id, e1, e2),
+//          SENTINEL: an empty slot;  f[7] unused.
+// The nodes are the binned-SAH BVH2 collapsed to four children per node
+// (vr_build.cpp), which halves the dependent node fetches of a ray.
 //
 // Traversal is the persistent "while-while" scheme of Aila & Laine (2009):
 // resident warps pull rays from a queue; each lane walks inner nodes nearest
 // child first and postpones the first leaf it reaches, so that leaves are
 // intersected when every lane of the warp holds one (the triangle tests then
 // run with the whole warp active).  When enough lanes have finished, the warp
-// stores their results and refills them from the queue.  The far child of two
-// hit children is pushed with its entry distance; popped entries beyond the
-// current closest hit are skipped.
+// stores their results and refills them from the queue.  Of a node's hit
+// children the nearest is visited next and the others are pushed with their
+// entry distances, farthest first; popped entries beyond the current closest
+// hit are skipped.
 #pragma once
 #include "vr_device.cuh"
 
@@ -164,39 +168,84 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, 
         do {
             // inner nodes until every lane in the loop holds a postponed leaf
             while (node >= 0 && node != SENTINEL) {
-                const float4* np = nodes + 4 * node;
-                const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-                const int4 n3 = __ldg(reinterpret_cast<const int4*>(np) + 3);
+                // 4-wide node: slab tests of the four children, the hit ones
+                // visited nearest first (the others pushed farthest first)
+                const float4* np = nodes + 8 * node;
                 if (COUNT) nv++;
-                const float a0 = fmaf(n0.x, ix, -ox), b0 = fmaf(n0.y, ix, -ox);
-                const float c0 = fmaf(n0.z, iy, -oy), d0 = fmaf(n0.w, iy, -oy);
-                const float e0 = fmaf(n2.x, iz, -oz), f0 = fmaf(n2.y, iz, -oz);
-                const float a1 = fmaf(n1.x, ix, -ox), b1 = fmaf(n1.y, ix, -ox);
-                const float c1 = fmaf(n1.z, iy, -oy), d1 = fmaf(n1.w, iy, -oy);
-                const float e1 = fmaf(n2.z, iz, -oz), f1 = fmaf(n2.w, iz, -oz);
-                const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
-                const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), best));
-                const float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
-                const float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), best));
-                const bool hit0 = tn0 <= tf0, hit1 = tn1 <= tf1;
-                if (hit0 && hit1) {
-                    const bool swap = tn1 < tn0;
-                    if (sp >= STACK_SIZE) {
+                float t0, t1, t2, t3;
+                const int4 cd = __ldg(reinterpret_cast<const int4*>(np) + 6);
+                {
+                    const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+                    const float a0 = fmaf(n0.x, ix, -ox), b0 = fmaf(n0.y, ix, -ox);
+                    const float c0 = fmaf(n0.z, iy, -oy), d0 = fmaf(n0.w, iy, -oy);
+                    const float e0 = fmaf(n2.x, iz, -oz), f0 = fmaf(n2.y, iz, -oz);
+                    const float a1 = fmaf(n1.x, ix, -ox), b1 = fmaf(n1.y, ix, -ox);
+                    const float c1 = fmaf(n1.z, iy, -oy), d1 = fmaf(n1.w, iy, -oy);
+                    const float e1 = fmaf(n2.z, iz, -oz), f1 = fmaf(n2.w, iz, -oz);
+                    const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
+                    const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), best));
+                    const float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
+                    const float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), best));
+                    t0 = (tn0 <= tf0 && cd.x != SENTINEL) ? tn0 : INF_F;
+                    t1 = (tn1 <= tf1 && cd.y != SENTINEL) ? tn1 : INF_F;
+                }
+                {
+                    const float4 n0 = __ldg(np + 3), n1 = __ldg(np + 4), n2 = __ldg(np + 5);
+                    const float a0 = fmaf(n0.x, ix, -ox), b0 = fmaf(n0.y, ix, -ox);
+                    const float c0 = fmaf(n0.z, iy, -oy), d0 = fmaf(n0.w, iy, -oy);
+                    const float e0 = fmaf(n2.x, iz, -oz), f0 = fmaf(n2.y, iz, -oz);
+                    const float a1 = fmaf(n1.x, ix, -ox), b1 = fmaf(n1.y, ix, -ox);
+                    const float c1 = fmaf(n1.z, iy, -oy), d1 = fmaf(n1.w, iy, -oy);
+                    const float e1 = fmaf(n2.z, iz, -oz), f1 = fmaf(n2.w, iz, -oz);
+                    const float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
+                    const float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), best));
+                    const float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
+                    const float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), best));
+                    t2 = (tn0 <= tf0 && cd.z != SENTINEL) ? tn0 : INF_F;
+                    t3 = (tn1 <= tf1 && cd.w != SENTINEL) ? tn1 : INF_F;
+                }
+                int k0 = cd.x, k1 = cd.y, k2 = cd.z, k3 = cd.w;
+                const int nh = (t0 < INF_F) + (t1 < INF_F) + (t2 < INF_F) + (t3 < INF_F);
+                // sort by entry distance (misses, at infinity, end up last)
+                auto cswap = [](float& ta, int& ka, float& tb, int& kb) {
+                    const bool sw = tb < ta;
+                    const float tt = sw ? tb : ta;
+                    const int kk = sw ? kb : ka;
+                    tb = sw ? ta : tb;
+                    kb = sw ? ka : kb;
+                    ta = tt;
+                    ka = kk;
+                };
+                cswap(t0, k0, t1, k1);
+                cswap(t2, k2, t3, k3);
+                cswap(t0, k0, t2, k2);
+                cswap(t1, k1, t3, k3);
+                cswap(t1, k1, t2, k2);
+                if (nh == 0) {
+                    node = pop();
+                } else {
+                    if (sp + nh - 1 > STACK_SIZE) {
                         overflow = true;
                         node = SENTINEL;
                         leaf = 0;
                         break;
                     }
-                    stack_node[sp] = swap ? n3.x : n3.y;
-                    stack_t[sp] = swap ? tn0 : tn1;
-                    ++sp;
-                    node = swap ? n3.y : n3.x;
-                } else if (hit0) {
-                    node = n3.x;
-                } else if (hit1) {
-                    node = n3.y;
-                } else {
-                    node = pop();
+                    if (nh > 3) {
+                        stack_node[sp] = k3;
+                        stack_t[sp] = t3;
+                        ++sp;
+                    }
+                    if (nh > 2) {
+                        stack_node[sp] = k2;
+                        stack_t[sp] = t2;
+                        ++sp;
+                    }
+                    if (nh > 1) {
+                        stack_node[sp] = k1;
+                        stack_t[sp] = t1;
+                        ++sp;
+                    }
+                    node = k0;
                 }
                 // postpone the first leaf reached
                 if (node < 0 && leaf >= 0) {
