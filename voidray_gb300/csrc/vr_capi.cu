@@ -333,6 +333,10 @@ struct HostJob {
     float4* normal = nullptr;
 };
 
+// Single-job waves of at least this many paths launch their stages directly
+// even when graphs are on.
+constexpr uint32_t SINGLE_JOB_GRAPH_LIMIT = 1u << 22;
+
 // Plans waves of at most `cap` slots over the jobs (each wave takes, in job
 // order, as many of every unfinished job's next paths as fit), uploads the
 // Job entries of up to `table_cap` entries at a time, and launches the stage
@@ -416,8 +420,15 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
         if (plan.empty()) return fail(VR_ERR_INVALID, "wave table too small for one wave");
         // pageable host -> device: the host vector may be reused once the call returns
         VR_CK(cudaMemcpyAsync(table, chunk.data(), chunk.size() * sizeof(vr::Job), cudaMemcpyHostToDevice, cs));
-        const bool use_graphs = graphs && !graphs->broken && cs && !instr;
+        const bool graphs_on = graphs && !graphs->broken && cs && !instr;
         for (const WaveHost& wh : plan) {
+            // A replayed graph reads its jobs from the device table, i.e. runs
+            // the multi-job kernel variants, which cost about 5% over the
+            // single-job ones (job fields from shared memory instead of kernel
+            // parameters); a large single-job wave gains nothing from a graph
+            // (its launches are microseconds against a wave of milliseconds),
+            // so it launches directly.
+            const bool use_graphs = graphs_on && (wh.njobs > 1 || wh.total < SINGLE_JOB_GRAPH_LIMIT);
             const vr::Wave wv{table + wh.first, (uint32_t)wh.njobs, wh.total,         wh.max_bounces,
                               wh.any_nee ? 1u : 0u, use_graphs ? 1u : 0u, chunk[wh.first]};
             auto stages = [&]() -> vr_status {

@@ -813,7 +813,7 @@ __device__ __forceinline__ void shade_path(const Job& j, const PathState& ps, ui
 }
 
 template <bool ONE>
-__global__ void __launch_bounds__(256, ONE ? 3 : 2) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
+__global__ void __launch_bounds__(256, 3) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;
     if (ONE) {
@@ -829,11 +829,19 @@ __global__ void __launch_bounds__(256, ONE ? 3 : 2) k_shade(Wave w, PathState ps
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
     // the jobs this block's entries belong to (a contiguous range: job
-    // segments are concatenated); up to BIN_JOBS of them are copied to shared
-    // memory, so that every thread reads its job there instead of from the
-    // job table in global memory
+    // segments are concatenated); they are copied to shared memory, so that
+    // every thread reads its job there instead of from the job table in
+    // global memory
     __shared__ uint32_t s_rlo, s_nj;
     __shared__ Job s_jobs[ONE ? 1 : BIN_JOBS];
+    const bool all_staged = !ONE && w.njobs <= BIN_JOBS;
+    if (all_staged) {
+        const uint32_t words = w.njobs * (uint32_t)(sizeof(Job) / 4);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(w.jobs);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(s_jobs);
+        for (uint32_t t = threadIdx.x; t < words; t += blockDim.x) dst[t] = src[t];
+        __syncthreads();
+    }
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         const uint32_t i = i0 + threadIdx.x;
         if (threadIdx.x == 0) {
@@ -843,27 +851,33 @@ __global__ void __launch_bounds__(256, ONE ? 3 : 2) k_shade(Wave w, PathState ps
             s_nj = (ONE ? 0u : find_job(pre, w.njobs, last)) - rlo + 1u;
         }
         __syncthreads();
-        if (!ONE && s_nj <= BIN_JOBS) {
-            const uint32_t words = s_nj * (uint32_t)(sizeof(Job) / 4);
-            const uint32_t* src = reinterpret_cast<const uint32_t*>(w.jobs + s_rlo);
-            uint32_t* dst = reinterpret_cast<uint32_t*>(s_jobs);
-            for (uint32_t t = threadIdx.x; t < words; t += blockDim.x) dst[t] = src[t];
-            __syncthreads();
-        }
         bool cont = false, want_shadow = false;
         V3 new_o, new_d, sh_dir, sh_c;
         uint32_t p = 0, r = 0;
-        if (i < n) {
-            r = ONE ? 0u : find_job(pre, w.njobs, i);
-            const uint32_t local = i - pre[r];
-            if (ONE)
-                shade_path(w.first, ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d, sh_dir, sh_c, p);
-            else if (s_nj <= BIN_JOBS)
-                shade_path(s_jobs[r - s_rlo], ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d,
-                           sh_dir, sh_c, p);
-            else
-                shade_path(w.jobs[r], ps, k, in_half, local, retired, cont, want_shadow, new_o, new_d, sh_dir,
-                           sh_c, p);
+        if (ONE) {
+            if (i < n)
+                shade_path(w.first, ps, k, in_half, i, retired, cont, want_shadow, new_o, new_d, sh_dir, sh_c, p);
+        } else {
+            // a wave of at most BIN_JOBS jobs was copied to shared memory
+            // once; otherwise the block's jobs pass through shared memory
+            // BIN_JOBS at a time (one round unless the block spans more jobs)
+            if (i < n) r = find_job(pre, w.njobs, i);
+            const uint32_t rend = s_rlo + s_nj;
+            for (uint32_t c0 = all_staged ? 0u : s_rlo; c0 < rend; c0 += BIN_JOBS) {
+                const uint32_t cn = all_staged ? w.njobs : min(BIN_JOBS, rend - c0);
+                if (!all_staged) {
+                    if (c0 != s_rlo) __syncthreads();  // the previous round's paths have read their jobs
+                    const uint32_t words = cn * (uint32_t)(sizeof(Job) / 4);
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(w.jobs + c0);
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(s_jobs);
+                    for (uint32_t t = threadIdx.x; t < words; t += blockDim.x) dst[t] = src[t];
+                    __syncthreads();
+                }
+                if (i < n && r >= c0 && r < c0 + cn)
+                    shade_path(s_jobs[r - c0], ps, k, in_half, i - pre[r], retired, cont, want_shadow, new_o, new_d,
+                               sh_dir, sh_c, p);
+                if (all_staged) break;
+            }
         }
         // queue conservation (instrumented runs): every path that does not
         // continue is retired here, exactly once

@@ -34,7 +34,7 @@ struct HitOut {
 #define VR_TRACE_MINB 8  // minimum resident blocks per SM requested from ptxas (64 registers, no spills)
 #endif
 #ifndef VR_DYN_FETCH
-#define VR_DYN_FETCH 12  // refill a warp's lanes once at least this many have finished
+#define VR_DYN_FETCH 16  // refill a warp's lanes once at least this many have finished
 #endif
 constexpr int SENTINEL = 0x7fffffff;  // "no node": the walk is finished
 constexpr int DYN_FETCH = VR_DYN_FETCH;
