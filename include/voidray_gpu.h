@@ -388,6 +388,21 @@ typedef struct vr_stats_job {
 #define VR_STATS_MAX_JOBS 128  /* per call */
 vr_status vr_serve_stats_device(const vr_stats_job* jobs, uint32_t count, double* out_device, void* stream);
 
+/* A served job's final image, on the device (no reference counterpart).
+ * vr_serve_sum_device: out[k] = a[k] + b[k] for `pairs` (1-3) pairs of RGBA
+ * f32 buffers of `pixels` pixels (the full sums of the job's radiance,
+ * albedo and normal halves, the denoiser's input with scale 1/samples).
+ * vr_serve_blend_device: rgb (3 f32 per pixel) = the plain mean
+ * (sum_a + sum_b) / samples, or with `denoised` (RGBA, the denoised full
+ * mean) and `alpha_tiles` (one weight per VR_STATS_TILE x VR_STATS_TILE tile,
+ * row-major over the tiles) alpha D + (1 - alpha) mean per pixel.  All
+ * buffers are device memory; RGBA buffers 16-byte aligned. */
+vr_status vr_serve_sum_device(const float* const* a, const float* const* b, float* const* out, uint32_t pairs,
+                              uint64_t pixels, void* stream);
+vr_status vr_serve_blend_device(const float* sum_a, const float* sum_b, uint32_t samples, const float* denoised,
+                                const float* alpha_tiles, uint32_t width, uint32_t height, float* rgb,
+                                void* stream);
+
 typedef struct vr_render_stats {
     uint64_t paths;          /* camera paths traced                            */
     uint64_t extend_rays;    /* closest-hit rays                               */

@@ -462,6 +462,25 @@ extern "C" {
         out_device: *mut f64,
         stream: *mut c_void,
     ) -> vr_status;
+    pub fn vr_serve_sum_device(
+        a: *const *const f32,
+        b: *const *const f32,
+        out: *const *mut f32,
+        pairs: u32,
+        pixels: u64,
+        stream: *mut c_void,
+    ) -> vr_status;
+    pub fn vr_serve_blend_device(
+        sum_a: *const f32,
+        sum_b: *const f32,
+        samples: u32,
+        denoised: *const f32,
+        alpha_tiles: *const f32,
+        width: u32,
+        height: u32,
+        rgb: *mut f32,
+        stream: *mut c_void,
+    ) -> vr_status;
     // Statistics and instrumentation
     pub fn vr_render_stats_get(scene: *const vr_scene, stats: *mut vr_render_stats) -> vr_status;
     pub fn vr_scene_instrument(scene: *mut vr_scene, flags: u32) -> vr_status;

@@ -16,13 +16,14 @@ def _strip(text: str) -> str:
     return re.sub(r"//[^\n]*", " ", text)
 
 
-def _ctype(tok: str) -> tuple[str, int, bool]:
-    """'const float *' -> (base, pointer depth, outermost pointee const)."""
+def _ctype(tok: str) -> tuple[str, int, tuple]:
+    """'const float * const *' -> (base, pointer depth, per pointer level from
+    the innermost: whether what it points to is const)."""
     t = tok.replace("*", " * ").split()
-    depth = t.count("*")
-    const = "const" in t[: t.index("*")] if depth else False
+    stars = [i for i, x in enumerate(t) if x == "*"]
+    consts = tuple("const" in t[(stars[k - 1] + 1 if k else 0):stars[k]] for k in range(len(stars)))
     base = " ".join(x for x in t if x not in ("*", "const", "struct", "enum"))
-    return base, depth, const
+    return base, len(stars), consts
 
 
 def _decl(d: str):

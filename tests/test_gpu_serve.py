@@ -138,6 +138,50 @@ def test_stats_kernel_matches_numpy(gpu, denoised):
     assert np.array_equal(out2.cpu().numpy(), v)   # deterministic
 
 
+@pytest.mark.parametrize("h,w", [(40, 24), (17, 33)])
+def test_result_kernels_match_numpy(gpu, h, w):
+    """vr_serve_sum_device and vr_serve_blend_device (a served job's final
+    image) against the formulas they compute: sums of half-buffer pairs, the
+    plain mean (A + B) / n, and alpha D + (1 - alpha) mean with alpha per
+    16 x 16 tile (ragged tiles at the edges); the output is packed RGB."""
+    import ctypes as C
+
+    import torch
+
+    from voidray_gb300 import _native as N
+    from voidray_gb300.serve import BLEND_TILE
+
+    rng = np.random.default_rng(7)
+    n = 96
+    A, B, D = (rng.gamma(1.0, 0.4, (h, w, 4)).astype(np.float32) * s for s in (48.0, 48.0, 1.0))
+    ty, tx = -(-h // BLEND_TILE), -(-w // BLEND_TILE)
+    alpha = rng.uniform(0.0, 1.0, (ty, tx)).astype(np.float32)
+    alpha[0, 0] = 0.0
+    tA, tB, tD, tal = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (A, B, D, alpha))
+    p = lambda x: C.c_void_p(x.data_ptr())
+    # sums of three pairs
+    outs = [torch.full((h, w, 4), -1.0, dtype=torch.float32, device="cuda") for _ in range(3)]
+    arr = C.c_void_p * 3
+    N.check(N.lib().vr_serve_sum_device(arr(tA.data_ptr(), tB.data_ptr(), tD.data_ptr()),
+                                        arr(tB.data_ptr(), tD.data_ptr(), tA.data_ptr()),
+                                        arr(*[o.data_ptr() for o in outs]), 3, h * w, None))
+    torch.cuda.synchronize()
+    for o, (x, y) in zip(outs, [(A, B), (B, D), (D, A)]):
+        assert np.array_equal(o.cpu().numpy(), x + y)
+    # plain mean and blend
+    mean = (A[..., :3] + B[..., :3]) * np.float32(1.0 / n)
+    rgb = torch.full((h, w, 3), -1.0, dtype=torch.float32, device="cuda")
+    N.check(N.lib().vr_serve_blend_device(p(tA), p(tB), n, None, None, w, h, p(rgb), None))
+    torch.cuda.synchronize()
+    assert np.allclose(rgb.cpu().numpy(), mean, rtol=1e-6, atol=0)
+    N.check(N.lib().vr_serve_blend_device(p(tA), p(tB), n, p(tD), p(tal), w, h, p(rgb), None))
+    torch.cuda.synchronize()
+    am = np.repeat(np.repeat(alpha, BLEND_TILE, 0), BLEND_TILE, 1)[:h, :w, None]
+    want = am * D[..., :3] + (1.0 - am) * mean
+    assert np.allclose(rgb.cpu().numpy(), want, rtol=1e-5, atol=1e-7)
+    assert N.lib().vr_serve_blend_device(p(tA), p(tB), n, p(tD), None, w, h, p(rgb), None) == 1
+
+
 def test_backend_estimates_through_the_stats_kernel(gpu):
     """GpuBackend's per-pass estimate (one vr_serve_stats_device launch) equals
     the numpy half-buffer formula on the same buffers."""

@@ -20,10 +20,10 @@ PRIM = {"float": "f32", "double": "f64", "uint32_t": "u32", "int32_t": "i32", "u
 
 
 def rust_type(t, arr=0):
-    base, depth, const = t
+    base, depth, consts = t
     s = PRIM.get(base, base)
     for k in range(depth):
-        s = ("*const " if (k == 0 and const) else "*mut ") + s
+        s = ("*const " if consts[k] else "*mut ") + s
     return f"[{s}; {arr}]" if arr else s
 
 
@@ -75,7 +75,7 @@ def test_functions_match_header_signature_for_signature():
     assert set(fns) == set(h["functions"]), set(fns) ^ set(h["functions"])
     for name, (ret, params) in h["functions"].items():
         rret, rparams = fns[name]
-        assert rret == ("()" if ret == ("void", 0, False) else rust_type(ret)), name
+        assert rret == ("()" if ret[:2] == ("void", 0) else rust_type(ret)), name
         assert rparams == [rust_type(t) for _, t in params], (name, rparams)
     # the C enum types travel as i32 aliases
     assert {"vr_status", "vr_material_kind", "vr_env_kind", "vr_estimator"} <= aliases

@@ -181,6 +181,8 @@ _SIGS = [
     ("vr_batch_set_graphs", C.c_int, [P, C.c_int32]),
     ("vr_batch_graph_stats", C.c_int, [P, P, P]),
     ("vr_serve_stats_device", C.c_int, [P, C.c_uint32, P, P]),
+    ("vr_serve_sum_device", C.c_int, [P, P, P, C.c_uint32, C.c_uint64, P]),
+    ("vr_serve_blend_device", C.c_int, [P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, P, P]),
     ("vr_batch_stats_get", C.c_int, [P, P]),
     ("vr_scene_instrument", C.c_int, [P, C.c_uint32]),
     ("vr_scene_instrument_get", C.c_int, [P, P]),

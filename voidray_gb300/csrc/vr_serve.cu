@@ -92,7 +92,90 @@ __global__ void __launch_bounds__(THREADS) k_serve_stats(const __grid_constant__
     }
 }
 
+// out[i] = a[i] + b[i] over the float4 elements of `pairs` buffer pairs
+// (the full sums of a job's radiance, albedo and normal halves).
+struct SumPairs {
+    const float4* a[3];
+    const float4* b[3];
+    float4* out[3];
+};
+__global__ void k_serve_sum(const SumPairs sp, uint32_t pairs, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint32_t k = 0; k < pairs; ++k)
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const float4 x = sp.a[k][i], y = sp.b[k][i];
+            sp.out[k][i] = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+        }
+}
+
+// rgb[p] = alpha D[p] + (1 - alpha) (A[p] + B[p]) / n, alpha the weight of
+// p's TILE x TILE tile (0 everywhere without a denoised image).
+__global__ void k_serve_blend(const float4* __restrict__ a, const float4* __restrict__ b, float inv_n,
+                              const float4* __restrict__ d, const float* __restrict__ alpha, uint32_t w, uint32_t h,
+                              float* __restrict__ rgb) {
+    const uint64_t np = (uint64_t)w * h, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t tiles_x = (w + TILE - 1) / TILE;
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+        const float4 x = a[p], y = b[p];
+        float r = (x.x + y.x) * inv_n, g = (x.y + y.y) * inv_n, bl = (x.z + y.z) * inv_n;
+        if (d) {
+            const uint32_t px = (uint32_t)(p % w), py = (uint32_t)(p / w);
+            const float al = alpha[(py / TILE) * tiles_x + px / TILE];
+            if (al != 0.0f) {
+                const float4 dv = d[p];
+                r = al * dv.x + (1.0f - al) * r;
+                g = al * dv.y + (1.0f - al) * g;
+                bl = al * dv.z + (1.0f - al) * bl;
+            }
+        }
+        rgb[3 * p] = r;
+        rgb[3 * p + 1] = g;
+        rgb[3 * p + 2] = bl;
+    }
+}
+
+unsigned serve_grid(uint64_t n) {
+    const uint64_t g = (n + 255) / 256;
+    return (unsigned)(g < 4096 ? (g ? g : 1) : 4096);
+}
+
+bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; }
+
 }  // namespace
+
+vr_status vr_serve_sum_device(const float* const* a, const float* const* b, float* const* out, uint32_t pairs,
+                              uint64_t pixels, void* stream) {
+    if (!a || !b || !out || pairs == 0 || pairs > 3) return vr::set_error(VR_ERR_INVALID, "serve sum: bad arguments");
+    if (pixels == 0) return VR_OK;
+    if (!vr::device_usable()) return vr::set_error(VR_ERR_NO_DEVICE, "no CUDA device");
+    SumPairs sp{};
+    for (uint32_t k = 0; k < pairs; ++k) {
+        if (!a[k] || !b[k] || !out[k] || misaligned16(a[k]) || misaligned16(b[k]) || misaligned16(out[k]))
+            return vr::set_error(VR_ERR_INVALID, "serve sum: buffers must be set and 16-byte aligned");
+        sp.a[k] = reinterpret_cast<const float4*>(a[k]);
+        sp.b[k] = reinterpret_cast<const float4*>(b[k]);
+        sp.out[k] = reinterpret_cast<float4*>(out[k]);
+    }
+    k_serve_sum<<<serve_grid(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(sp, pairs, pixels);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return vr::set_error(VR_ERR_CUDA, std::string("serve sum: ") + cudaGetErrorString(e));
+    return VR_OK;
+}
+
+vr_status vr_serve_blend_device(const float* sum_a, const float* sum_b, uint32_t samples, const float* denoised,
+                                const float* alpha_tiles, uint32_t width, uint32_t height, float* rgb, void* stream) {
+    if (!sum_a || !sum_b || !rgb || !width || !height || !samples || (!denoised) != (!alpha_tiles))
+        return vr::set_error(VR_ERR_INVALID, "serve blend: bad arguments");
+    if (misaligned16(sum_a) || misaligned16(sum_b) || (denoised && misaligned16(denoised)))
+        return vr::set_error(VR_ERR_INVALID, "serve blend: RGBA buffers must be 16-byte aligned");
+    if (!vr::device_usable()) return vr::set_error(VR_ERR_NO_DEVICE, "no CUDA device");
+    k_serve_blend<<<serve_grid((uint64_t)width * height), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(sum_a), reinterpret_cast<const float4*>(sum_b), 1.0f / (float)samples,
+        reinterpret_cast<const float4*>(denoised), alpha_tiles, width, height, rgb);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return vr::set_error(VR_ERR_CUDA, std::string("serve blend: ") + cudaGetErrorString(e));
+    return VR_OK;
+}
 
 vr_status vr_serve_stats_device(const vr_stats_job* jobs, uint32_t count, double* out, void* stream) {
     if (!jobs || !out) return vr::set_error(VR_ERR_INVALID, "null argument");

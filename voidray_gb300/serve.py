@@ -578,7 +578,13 @@ class GpuBackend:
     # -- results ---------------------------------------------------------
     def result(self, job: JobState) -> np.ndarray:
         """The plain mean, or the blend alpha D(P) + (1 - alpha) P with alpha
-        per BLEND_TILE tile (piecewise constant)."""
+        per BLEND_TILE tile (piecewise constant): the half-buffer sums, the
+        denoiser's input and the blend are library kernels
+        (vr_serve_sum_device, vr_serve_blend_device) on the result stream."""
+        import ctypes as C
+
+        from . import _native as N
+
         t = self.torch
         t0 = time.perf_counter()
         n = job.n_a + job.n_b
@@ -586,24 +592,30 @@ class GpuBackend:
         es = self.res_stream
         for b in job.bufs:
             b.record_stream(es)
+        ptr = lambda x: C.c_void_p(x.data_ptr())
         with t.cuda.stream(es):
-            p = (job.bufs[0] + job.bufs[1]) / n
+            rgb = t.empty((h, w, 3), dtype=t.float32, device="cuda")
             alpha = np.asarray(job.alpha, np.float32)
             if not alpha.any():
-                y = p[..., :3]
+                N.check(N.lib().vr_serve_blend_device(ptr(job.bufs[0]), ptr(job.bufs[1]), n, None, None, w, h,
+                                                       ptr(rgb), C.c_void_p(es.cuda_stream)))
             else:
-                alb = (job.bufs[2] + job.bufs[3]) / n
-                nrm = (job.bufs[4] + job.bufs[5]) / n
+                sums = [t.empty((h, w, 4), dtype=t.float32, device="cuda") for _ in range(3)]
+                arr = C.c_void_p * 3
+                N.check(N.lib().vr_serve_sum_device(arr(*[b.data_ptr() for b in job.bufs[0::2]]),
+                                                     arr(*[b.data_ptr() for b in job.bufs[1::2]]),
+                                                     arr(*[x.data_ptr() for x in sums]), 3, h * w,
+                                                     C.c_void_p(es.cuda_stream)))
                 d = t.empty((h, w, 4), dtype=t.float32, device="cuda")
-                self.dn_result.denoise(p, alb, nrm, 1.0, d, w, h, stream=es.cuda_stream)
+                self.dn_result.denoise(sums[0], sums[1], sums[2], 1.0 / n, d, w, h, stream=es.cuda_stream)
                 self.denoise_calls += 1
-                am = t.from_numpy(np.atleast_2d(alpha)).to("cuda")
-                if am.numel() > 1:
-                    am = am.repeat_interleave(BLEND_TILE, 0).repeat_interleave(BLEND_TILE, 1)[:h, :w]
-                am = am.reshape(am.shape[0], am.shape[1], 1)
-                y = am * d[..., :3] + (1.0 - am) * p[..., :3]
+                ty, tx = -(-h // BLEND_TILE), -(-w // BLEND_TILE)
+                tiles = np.broadcast_to(alpha, (ty, tx)) if alpha.ndim < 2 else alpha
+                am = t.from_numpy(np.ascontiguousarray(tiles, np.float32)).to("cuda")
+                N.check(N.lib().vr_serve_blend_device(ptr(job.bufs[0]), ptr(job.bufs[1]), n, ptr(d), ptr(am), w, h,
+                                                       ptr(rgb), C.c_void_p(es.cuda_stream)))
         es.synchronize()
-        out = y.cpu().numpy()
+        out = rgb.cpu().numpy()
         self.time["result"] += time.perf_counter() - t0
         return out
 
