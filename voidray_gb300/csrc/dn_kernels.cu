@@ -717,6 +717,12 @@ __global__ void __launch_bounds__(32 * (BM / 16) * (BN / 16)) k_conv3x3_wgrad9(c
         cp_commit();
     }
     const int i4 = lane >> 3;
+    // fused bias gradient (CTAs of the first ci tile): thread -> one output
+    // channel column of the staged dz block and a quarter... of its 32 rows
+    const bool bias = a.db && blockIdx.y == 0;
+    constexpr int BIAS_PARTS = NTHREADS / BM;  // threads per column
+    const int bcol = tid % BM, bpart = tid / BM;
+    float bsum = 0.0f;
     for (int kb = 0; kb < nk; ++kb) {
         cp_wait<STAGES - 2>();
         __syncthreads();
@@ -724,6 +730,9 @@ __global__ void __launch_bounds__(32 * (BM / 16) * (BN / 16)) k_conv3x3_wgrad9(c
         cp_commit();
         const bf16* tA = sA[kb % STAGES];
         const bf16* tB = sB[kb % STAGES];
+        if (bias)
+            for (int row = bpart; row < A_ROWS; row += BIAS_PARTS)
+                bsum += __bfloat162float(tA[row * BM + (((bcol >> 3) ^ swz<CPA>(row)) << 3) + (bcol & 7)]);
 #pragma unroll
         for (int kk = 0; kk < 32; kk += 16) {
             // A: 16 pixels x 16 co (transposed load of the [pixel][co] tile)
@@ -749,6 +758,16 @@ __global__ void __launch_bounds__(32 * (BM / 16) * (BN / 16)) k_conv3x3_wgrad9(c
         }
     }
     cp_wait<0>();
+    if (bias) {  // the column's partial sums, one atomic per output channel
+        __shared__ float bred[NTHREADS];
+        bred[tid] = bsum;
+        __syncthreads();
+        if (bpart == 0 && co0 + bcol < a.cout) {
+            float s = 0.0f;
+            for (int k = 0; k < BIAS_PARTS; ++k) s += bred[k * BM + bcol];
+            atomicAdd(a.db + co0 + bcol, s);
+        }
+    }
 
 #pragma unroll
     for (int t = 0; t < 9; ++t)
@@ -822,12 +841,16 @@ cudaError_t conv3x3_wgrad(const WgradArgs& a, cudaStream_t st) {
         (a.up1 && ((a.h | a.w) & 1)))
         return cudaErrorInvalidValue;
     const bool bn32 = cin % 32 == 0;
-    if (a.h % 4 == 0 && a.w % 8 == 0 && !wgrad_per_tap()) {
+    if (a.h % 4 == 0 && a.w % 8 == 0 && !wgrad_per_tap()) {  // the bias gradient rides along
         if (a.cout >= 64) return bn32 ? launch_wgrad9<64, 32>(a, st) : launch_wgrad9<64, 16>(a, st);
         return bn32 ? launch_wgrad9<32, 32>(a, st) : launch_wgrad9<32, 16>(a, st);
     }
-    if (a.cout >= 64) return bn32 ? launch_wgrad<64, 32>(a, st) : launch_wgrad<64, 16>(a, st);
-    return bn32 ? launch_wgrad<32, 32>(a, st) : launch_wgrad<32, 16>(a, st);
+    WgradArgs b = a;
+    b.db = nullptr;
+    const cudaError_t e = (a.cout >= 64) ? (bn32 ? launch_wgrad<64, 32>(b, st) : launch_wgrad<64, 16>(b, st))
+                                         : (bn32 ? launch_wgrad<32, 32>(b, st) : launch_wgrad<32, 16>(b, st));
+    if (e != cudaSuccess || !a.db) return e;
+    return bias_grad(a.dz, a.n * a.h * a.w, a.cout, a.db, st);
 }
 
 cudaError_t bias_grad(const bf16* dz, int p, int c, float* db, cudaStream_t st) {

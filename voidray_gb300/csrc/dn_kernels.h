@@ -43,6 +43,7 @@ struct WgradArgs {
     int c1, c2, cout;
     int up1;
     int pix_per_split;   // multiple of 32
+    float* db;           // optional [Cout]: the bias gradient (sum of dz over pixels) is added here too
 };
 
 cudaError_t conv3x3(const ConvArgs& a, cudaStream_t st);

@@ -274,8 +274,8 @@ vr_status backward(vr_denoiser* d, cudaStream_t st) {
         g.c2 = c2;
         g.cout = L.cout;
         g.up1 = L.up1;
+        g.db = d->g32 + d->off.b[l];  // the bias gradient, fused into the weight gradient's pass over dz
         DN_CK(dn::conv3x3_wgrad(g, st));
-        DN_CK(dn::bias_grad(cur, n * hl * wl, L.cout, d->g32 + d->off.b[l], st));
         if (l == 0) break;
         // input gradient: conv of dz with the flipped weights
         dn::ConvArgs a{};
