@@ -377,9 +377,21 @@ vr_status run_waves(std::vector<HostJob>& jobs, const vr::PathState& ps, uint32_
         while (pending()) {
             WaveHost wh{chunk.size(), 0, 0, 0, 0, false, {}};
             uint32_t left = cap;
-            for (size_t i = 0; i < jobs.size() && left > 0 && wh.njobs < vr::MAX_JOBS; ++i) {
+            // A job with at least a full wave of paths left gets the wave to
+            // itself (whole sample rows): single-job waves run the single-job
+            // kernel variants, about 5% faster than the multi-job ones.  The
+            // jobs' tails and the small jobs share the remaining waves.
+            size_t solo = jobs.size();
+            for (size_t i = 0; i < jobs.size(); ++i)
+                if (jobs[i].total - jobs[i].done >= cap) {
+                    solo = i;
+                    break;
+                }
+            for (size_t i = (solo < jobs.size() ? solo : 0); i < jobs.size() && left > 0 && wh.njobs < vr::MAX_JOBS;
+                 ++i) {
                 HostJob& j = jobs[i];
                 if (j.done >= j.total) continue;
+                if (solo < jobs.size() && i != solo) break;
                 uint32_t take = (uint32_t)std::min<uint64_t>(left, j.total - j.done);
                 // a job that does not finish in this wave takes whole sample rows
                 // when it can (pixel-major slot order), leaving the rest of the
