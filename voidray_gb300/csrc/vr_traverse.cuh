@@ -37,7 +37,11 @@ struct HitOut {
 #define VR_DYN_FETCH 16  // refill a warp's lanes once at least this many have finished
 #endif
 constexpr int SENTINEL = 0x7fffffff;  // "no node": the walk is finished
+#ifndef VR_DYN_FETCH_ANY
+#define VR_DYN_FETCH_ANY VR_DYN_FETCH  // the same for any-hit (shadow) traversal
+#endif
 constexpr int DYN_FETCH = VR_DYN_FETCH;
+constexpr int DYN_FETCH_ANY = VR_DYN_FETCH_ANY;
 
 // Triangle::hit (mesh.rs:144-188) on the precomputed (v0, e1, e2): the same
 // operations in the same order, each rounded separately (-fmad=false), so
@@ -267,7 +271,7 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, 
                 leaf = node;
                 if (node < 0) node = pop();
             }
-        } while (__popc(__ballot_sync(FULL, node == SENTINEL)) < DYN_FETCH);
+        } while (__popc(__ballot_sync(FULL, node == SENTINEL)) < (ANY ? DYN_FETCH_ANY : DYN_FETCH));
     }
     if (COUNT) add_work(work, nv, nt);
 }
