@@ -258,6 +258,8 @@ struct vr_scene {
     uint32_t psum_cap = 0;
     DevBuf aov_psum;                       // first-hit AOV sums (2 float4 per pixel)
     DevBuf stage_a, stage_b;               // host-call staging
+    DevBuf sortbuf;                        // batch queries: sort keys, trace order, histogram
+    float blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};  // bounds of the triangles (the root node's children)
     Instr instr;
 };
 
@@ -562,6 +564,23 @@ vr_status vr_scene_create(const vr_scene_desc* desc, vr_scene** out) {
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(fail(VR_ERR_CUDA, "stream creation failed"));
     s->view = hs.view;
+    if (!hs.wide.empty()) {  // triangle bounds: the union of the root's child boxes
+        for (int a = 0; a < 3; ++a) {
+            s->blo[a] = INFINITY;
+            s->bhi[a] = -INFINITY;
+        }
+        int32_t cd[4];
+        std::memcpy(cd, &hs.wide[6], sizeof cd);
+        for (int c = 0; c < 4; ++c) {
+            if (cd[c] == 0x7fffffff) continue;
+            const float4 xy = hs.wide[3 * (c >> 1) + (c & 1)], z = hs.wide[3 * (c >> 1) + 2];
+            const float lo[3] = {xy.x, xy.z, (c & 1) ? z.z : z.x}, hi[3] = {xy.y, xy.w, (c & 1) ? z.w : z.y};
+            for (int a = 0; a < 3; ++a) {
+                s->blo[a] = std::min(s->blo[a], lo[a]);
+                s->bhi[a] = std::max(s->bhi[a], hi[a]);
+            }
+        }
+    }
     if ((st = upload(s, hs.wide, &s->view.nodes)) != VR_OK) return cleanup(st);  // the 4-wide tree
     if ((st = upload(s, hs.tris, &s->view.tris)) != VR_OK) return cleanup(st);
     if ((st = upload(s, hs.shade, &s->view.shade)) != VR_OK) return cleanup(st);
@@ -678,6 +697,7 @@ vr_status vr_scene_destroy(vr_scene* s) {
     if (s->aov_psum.p) cudaFree(s->aov_psum.p);
     if (s->stage_a.p) cudaFree(s->stage_a.p);
     if (s->stage_b.p) cudaFree(s->stage_b.p);
+    if (s->sortbuf.p) cudaFree(s->sortbuf.p);
     for (void* p : s->allocs) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -996,10 +1016,26 @@ vr_status vr_intersect_device(vr_scene* s, const vr_ray* rays, uint64_t n, vr_hi
         return VR_OK;
     }
     const uint64_t chunk = 1ull << 30;  // the persistent kernel indexes rays with 32 bits
+    // closest-hit batches of at least SORT_MIN rays are traced in sorted order
+    // (octant, origin cell): same results, more coherent warps (1M-triangle
+    // soup, 16.8M rays: 1033 -> 1072 M rays/s); any-hit rays stop early and
+    // do not repay the sort (2266 -> 2232 M rays/s with it)
+    constexpr uint64_t SORT_MIN = 1u << 16;
+    const bool sort = n >= SORT_MIN && s->view.nodes && !any_hit;
+    vr_status r;
+    if (sort && (r = ensure_buf(s->sortbuf, (2 * std::min(chunk, n) + vr::RAY_SORT_BINS) * sizeof(uint32_t))) != VR_OK)
+        return r;
     for (uint64_t b = 0; b < n; b += chunk) {
         const uint64_t m = std::min(chunk, n - b);
-        VR_CK(vr::launch_intersect(s->view, reinterpret_cast<const float4*>(rays + b), m,
-                                   reinterpret_cast<float4*>(hits + b), any_hit != 0, s->fetch, s->status, cs));
+        const float4* rb = reinterpret_cast<const float4*>(rays + b);
+        uint32_t* perm = nullptr;
+        if (sort && m >= SORT_MIN) {
+            uint32_t* keys = static_cast<uint32_t*>(s->sortbuf.p);
+            perm = keys + m;
+            VR_CK(vr::launch_ray_sort(rb, (uint32_t)m, s->blo, s->bhi, keys, perm + m, perm, cs));
+        }
+        VR_CK(vr::launch_intersect(s->view, rb, m, reinterpret_cast<float4*>(hits + b), any_hit != 0, s->fetch,
+                                   s->status, cs, perm));
     }
     return VR_OK;
 }

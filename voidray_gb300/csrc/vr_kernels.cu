@@ -39,13 +39,16 @@ struct BatchIo {
     const float4* ana;  // analytic surfaces, tested after the BVH
     uint32_t nana, ntris;
     bool any;
+    const uint32_t* perm;  // trace order (k_ray_scatter), or null: the caller's order
     __device__ __forceinline__ void load(uint32_t i, float4& ro, float4& rd, const float4*& n, const float4*& t) const {
+        if (perm) i = __ldg(perm + i);
         ro = __ldg(rays + 2 * (size_t)i);
         rd = __ldg(rays + 2 * (size_t)i + 1);
         n = nodes;
         t = tris;
     }
     __device__ __forceinline__ void store(uint32_t i, const HitOut& h, bool overflow) const {
+        if (perm) i = __ldg(perm + i);
         HitOut o = h;
         if (overflow) o.prim = MISS;
         if (nana && !overflow && !(any && o.prim != MISS)) {
@@ -62,6 +65,83 @@ struct BatchIo {
         hits[i] = pack_hit(o);
     }
 };
+
+// Trace order of a batch query: rays grouped by direction octant and by a
+// cell of their origin (3 bits per axis, Morton order) in the scene's bounds,
+// so that a warp's rays start near each other heading into one octant.  A
+// counting sort over the 4096 keys: per-block histograms, one scan, a scatter
+// with warp-aggregated cursors.
+constexpr uint32_t RAY_BINS = RAY_SORT_BINS;
+__device__ __forceinline__ uint32_t ray_key(float4 ro, float4 rd, float3 lo, float3 sc) {
+    auto cell = [](float v, float l, float s) { return (uint32_t)fminf(fmaxf((v - l) * s, 0.0f), 7.0f); };
+    const uint32_t cx = cell(ro.x, lo.x, sc.x), cy = cell(ro.y, lo.y, sc.y), cz = cell(ro.z, lo.z, sc.z);
+    uint32_t m = 0;
+    for (int b = 0; b < 3; ++b)
+        m |= (((cx >> b) & 1u) << (3 * b)) | (((cy >> b) & 1u) << (3 * b + 1)) | (((cz >> b) & 1u) << (3 * b + 2));
+    const uint32_t oct = (rd.x < 0.0f ? 1u : 0u) | (rd.y < 0.0f ? 2u : 0u) | (rd.z < 0.0f ? 4u : 0u);
+    return (oct << 9) | m;
+}
+__global__ void k_ray_hist(const float4* __restrict__ rays, uint32_t n, float3 lo, float3 sc, uint32_t* keys,
+                           uint32_t* hist) {
+    __shared__ uint32_t h[RAY_BINS];
+    for (uint32_t t = threadIdx.x; t < RAY_BINS; t += blockDim.x) h[t] = 0;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t k = ray_key(__ldg(rays + 2 * (size_t)i), __ldg(rays + 2 * (size_t)i + 1), lo, sc);
+        keys[i] = k;
+        atomicAdd(&h[k], 1u);
+    }
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < RAY_BINS; t += blockDim.x)
+        if (h[t]) atomicAdd(&hist[t], h[t]);
+}
+// exclusive prefix of the 4096 counts, in place (one block of 1024 threads)
+__global__ void __launch_bounds__(1024) k_ray_scan(uint32_t* hist) {
+    __shared__ uint32_t wsum[32];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t v[4], s = 0;
+    for (int k = 0; k < 4; ++k) {
+        v[k] = hist[4 * t + k];
+        s += v[k];
+    }
+    uint32_t x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        wsum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t base = x - s + (warp ? wsum[warp - 1] : 0u);
+    for (int k = 0; k < 4; ++k) {
+        hist[4 * t + k] = base;
+        base += v[k];
+    }
+}
+__global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* cursor, uint32_t* perm) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {  // warp-uniform trip count
+        const uint32_t i = i0 + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t k = valid ? keys[i] : 0xffffffffu;
+        const uint32_t grp = __match_any_sync(0xffffffffu, k);
+        const uint32_t leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&cursor[k], (uint32_t)__popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (valid) perm[base + __popc(grp & ((1u << lane) - 1u))] = i;
+    }
+}
 
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128, VR_TRACE_MINB) k_intersect(BatchIo io, uint32_t n, uint32_t* counter,
@@ -1230,25 +1310,41 @@ static unsigned persistent_grid(K kernel, int block) {
     return (unsigned)(num_sms() * per_sm);
 }
 
+cudaError_t launch_ray_sort(const float4* rays, uint32_t n, const float* lo, const float* hi, uint32_t* keys,
+                            uint32_t* hist, uint32_t* perm, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(hist, 0, RAY_BINS * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    float3 l = make_float3(lo[0], lo[1], lo[2]), sc;
+    auto scale = [](float a, float b) { return b > a ? 8.0f / (b - a) : 0.0f; };
+    sc = make_float3(scale(lo[0], hi[0]), scale(lo[1], hi[1]), scale(lo[2], hi[2]));
+    const unsigned grid = grid_for(n, 256, 4);
+    k_ray_hist<<<grid, 256, 0, st>>>(rays, n, l, sc, keys, hist);
+    k_ray_scan<<<1, 1024, 0, st>>>(hist);
+    k_ray_scatter<<<grid, 256, 0, st>>>(keys, n, hist, perm);
+    return cudaGetLastError();
+}
+
 template <bool ANY, bool COUNT>
 static cudaError_t intersect_impl(const SceneView& s, const float4* rays, uint64_t n, float4* hits,
-                                  uint32_t* counter, uint32_t* status, unsigned long long* work, cudaStream_t st) {
+                                  uint32_t* counter, uint32_t* status, unsigned long long* work, cudaStream_t st,
+                                  const uint32_t* perm = nullptr) {
     static unsigned grid = 0;
     if (!grid) grid = persistent_grid(k_intersect<ANY, COUNT>, 128);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     k_intersect<ANY, COUNT><<<grid, 128, 0, st>>>(BatchIo{rays, hits, s.nodes, s.tris, s.analytic, s.num_analytic,
-                                                           s.num_tris, ANY},
+                                                           s.num_tris, ANY, perm},
                                                    (uint32_t)n, counter, status,
                                                    work);
     return cudaGetLastError();
 }
 
 cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
-                             uint32_t* counter, uint32_t* status, cudaStream_t st) {
+                             uint32_t* counter, uint32_t* status, cudaStream_t st, const uint32_t* perm) {
     if (n == 0) return cudaSuccess;
-    return any ? intersect_impl<true, false>(s, rays, n, hits, counter, status, nullptr, st)
-               : intersect_impl<false, false>(s, rays, n, hits, counter, status, nullptr, st);
+    return any ? intersect_impl<true, false>(s, rays, n, hits, counter, status, nullptr, st, perm)
+               : intersect_impl<false, false>(s, rays, n, hits, counter, status, nullptr, st, perm);
 }
 
 cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,

@@ -89,8 +89,16 @@ bool set_tuning(const Tuning& t);  // false: out of range (unchanged)
 
 // Batch closest/any hit; `counter` is a device word the persistent kernel
 // uses as its ray-fetch cursor (reset by the launcher).
+// `perm` (optional): the order to trace the rays in (launch_ray_sort);
+// hits are written back at the rays' own indices.
 cudaError_t launch_intersect(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
-                             uint32_t* counter, uint32_t* status, cudaStream_t st);
+                             uint32_t* counter, uint32_t* status, cudaStream_t st, const uint32_t* perm = nullptr);
+// Trace order of n rays: grouped by direction octant, then by origin cell
+// (Morton order of 8 x 8 x 8 cells of the box lo..hi).  keys and perm hold n
+// words each, hist 4096.
+constexpr uint32_t RAY_SORT_BINS = 4096;
+cudaError_t launch_ray_sort(const float4* rays, uint32_t n, const float* lo, const float* hi, uint32_t* keys,
+                            uint32_t* hist, uint32_t* perm, cudaStream_t st);
 cudaError_t launch_intersect_count(const SceneView& s, const float4* rays, uint64_t n, float4* hits, bool any,
                                    uint32_t* counter, unsigned long long* work, uint32_t* status, cudaStream_t st);
 // Wavefront stages, in launch order: raygen (clears the wave's counters),
