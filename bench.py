@@ -335,11 +335,11 @@ def batch_benchmark(args):
                 "graph_captures": caps, "graph_replays": reps})
     batch.destroy()
     # the same jobs one at a time (one single-job render call each, library
-    # launch shapes and 2^26-path wavefronts, one shared scratch); pass 0 again
+    # launch shapes and wavefronts of up to 2^28 paths, one shared scratch); pass 0 again
     # for the comparison
     autotune.set_tuning({k: v for k, v in autotune.DEFAULT.items() if k != "wavefront_paths"})
     alone = [torch.zeros_like(o) for o in outs]
-    single = Batch(1 << 26)
+    single = Batch(1 << 28)
 
     def alone_pass():
         for (acc, st, spp, w, h, seed), o in zip(jobs, alone):
@@ -831,7 +831,7 @@ def main():
                           f"accumulation {npx * 16 / 1e6:.0f} MB",
                     "bvh": {"nodes": int(info.num_nodes), "max_depth": int(info.max_depth),
                             "sah_cost": round(info.sah_cost, 2), "build_s": round(build_s, 2)},
-                    "wavefront_paths": st.wavefront_paths or (1 << 26),
+                    "wavefront_paths": st.wavefront_paths or (1 << 28),
                     "parallelism": f"replicas x{world}, disjoint sample ranges",
                     "tuning": tuning})
         line = {

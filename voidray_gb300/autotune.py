@@ -27,10 +27,10 @@ from pathlib import Path
 from . import _native as N
 from ._native import check, lib
 
-WAVEFRONTS = (1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26)
+WAVEFRONTS = (1 << 22, 1 << 24, 1 << 26, 1 << 27, 1 << 28)
 BLOCKS = (64, 128, 256)
 PER_SM = (4, 8, 16)
-DEFAULT = {"wavefront_paths": 1 << 26, "shade_block": 256, "shade_blocks_per_sm": 8, "raygen_block": 256}
+DEFAULT = {"wavefront_paths": 1 << 28, "shade_block": 256, "shade_blocks_per_sm": 8, "raygen_block": 256}
 
 
 def cache_path() -> Path:
@@ -141,7 +141,7 @@ def tune(acc, settings, width: int, height: int, spp: int, *, use_cache: bool = 
     return dict(best, cached=False, key=key)
 
 
-BATCH_WAVEFRONTS = (1 << 24, 1 << 25, 1 << 26)
+BATCH_WAVEFRONTS = (1 << 26, 1 << 27, 1 << 28)
 
 
 def tune_batch(jobs, *, scale: int = 8, use_cache: bool = True, log=None) -> dict:

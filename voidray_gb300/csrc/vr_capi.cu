@@ -736,10 +736,12 @@ vr_status vr_render_device(vr_scene* s, const vr_render_settings* st, uint32_t s
         return VR_OK;
     }
     const uint64_t total = (uint64_t)samples * np;
-    // default wavefront: 2^26 paths (about 12 GB of path state with the NEE
-    // estimator, 21 GB with the reference estimator at depth 12); deep
-    // bounces then still hold enough rays to fill the GPU
-    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
+    // default wavefront: 2^28 paths (at most: a render of fewer paths holds
+    // only those; about 48 GB of path state with the NEE estimator).  Fewer,
+    // larger waves spend less time in their deep-bounce tails, whose
+    // launches keep few rays alive: on the 2M-triangle 1080p frame 2^26
+    // paths gave 952 M samples/s, 2^27 1017 M, 2^28 1053 M
+    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 28);
     if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
     if (cap > np) cap -= cap % np;  // whole sample rows per wavefront: every slot in pixel-major order
@@ -777,7 +779,7 @@ vr_status vr_render_aov_device(vr_scene* s, const vr_render_settings* st, uint32
         return VR_OK;
     }
     const uint64_t total = (uint64_t)samples * np;
-    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 26);
+    uint64_t cap = st->wavefront_paths ? st->wavefront_paths : (1ull << 28);
     if (cap > (1ull << 28)) cap = 1ull << 28;
     if (cap > total) cap = total;
     if (cap > np) cap -= cap % np;  // whole sample rows per wavefront
