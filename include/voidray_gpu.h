@@ -333,7 +333,8 @@ typedef struct vr_render_job {
 } vr_render_job;
 
 typedef struct vr_batch vr_batch;
-/* max_wave_paths: paths per wavefront over all jobs (0 = 2^26). */
+/* max_wave_paths: paths per wavefront over all jobs (0 = 2^26; at most 2^28).  A batch keeps
+ * scratch for its largest wave (about 180 bytes per path with NEE) until destroyed. */
 vr_status vr_batch_create(uint64_t max_wave_paths, vr_batch** out);
 vr_status vr_batch_destroy(vr_batch* batch);
 /* Enqueues all jobs on `stream` (NULL = legacy default stream); scenes must
