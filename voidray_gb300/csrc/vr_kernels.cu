@@ -893,7 +893,7 @@ __device__ __forceinline__ void shade_path(const Job& j, const PathState& ps, ui
 }
 
 template <bool ONE>
-__global__ void __launch_bounds__(256, 3) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
+__global__ void __launch_bounds__(256, 4) k_shade(Wave w, PathState ps, uint32_t k, unsigned long long* retired) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;
     if (ONE) {
