@@ -31,7 +31,7 @@ struct HitOut {
 };
 
 #ifndef VR_TRACE_MINB
-#define VR_TRACE_MINB 8  // minimum resident blocks per SM requested from ptxas (64 registers, no spills)
+#define VR_TRACE_MINB 9  // minimum resident blocks per SM requested from ptxas (55 registers, no spills)
 #endif
 #ifndef VR_DYN_FETCH
 #define VR_DYN_FETCH 16  // refill a warp's lanes once at least this many have finished
