@@ -33,12 +33,12 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
+# bytes a 4-wide node visit reads: six float4 of child boxes and one of child codes
+NODE_BYTES = 112
 # DRAM and L2 bytes per closest-hit ray of k_extend on the default scene,
 # from an ncu capture of all twelve k_extend launches of one 960x540 x 32 spp
 # frame of it (the same 2M-triangle scene and HDRI, 34.4M extend rays); the
 # bench scales them to its own launches by the extend rays per launch
-# bytes a 4-wide node visit reads: six float4 of child boxes and one of child codes
-NODE_BYTES = 112
 K_EXTEND_DRAM_BYTES_PER_RAY = 149.9
 K_EXTEND_L2_BYTES_PER_RAY = 1005.1
 sys.path.insert(0, str(ROOT))
@@ -73,6 +73,7 @@ def parse_args():
                     help="requests of the 1920x1080, 2M-triangle serving run (0 = skip)")
     ap.add_argument("--no-isect", action="store_true", help="skip the intersection microbenchmark")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched workload")
+    ap.add_argument("--no-cornell", action="store_true", help="skip the Cornell box workload")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2, help="timed steps of the batched workload")
     ap.add_argument("--isect-tris", type=int, default=1_000_000)
@@ -279,6 +280,85 @@ def intersection_benchmark(args, hbm_peak, peak_source):
     return out
 
 
+def cornell_benchmark(args):
+    """The Cornell box workload (code-built box, 34 triangles, 256x256, 16 spp,
+    depth 8, Russian roulette from depth 3, the reference estimator, PCG32 seed
+    0, ACES tonemap), whole frames: on the GPU through vr_render_device +
+    vr_tonemap_device (device-timed) and vr_render + vr_tonemap (host buffers,
+    wall clock), and by the oracle on all host cores. The first GPU frame and
+    the oracle's frame are compared pixel for pixel, and after the tonemap."""
+    import numpy as np
+    import torch
+
+    import voidray_gb300 as vr
+    from voidray_gb300 import _native as N
+    from voidray_gb300 import workloads as W
+    from voidray_gb300.scene import ColorManagementSettings, Tonemap
+
+    lib = vr.lib()
+    w = h = 256
+    spp = 16
+    scene, st = W.cornell_box(width=w, height=h, spp=spp, max_depth=8, rr_depth=3)
+    cm = ColorManagementSettings(tonemap=Tonemap.ACES, gamma=2.2, exposure=0.0).to_c()
+    acc = scene.build_acceleration()
+    cst = st.to_c()
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    accum = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    ldr = torch.empty_like(accum)
+
+    def frame(k):
+        accum.zero_()
+        N.check(lib.vr_render_device(acc.handle, C.byref(cst), spp, accum.data_ptr(), w, h, 0, k * spp, sh))
+        N.check(lib.vr_tonemap_device(accum.data_ptr(), ldr.data_ptr(), w, h, C.byref(cm), 1.0, sh))
+
+    with torch.cuda.stream(stream):
+        frame(0)
+        torch.cuda.synchronize()
+        g_hdr, g_ldr = accum.cpu().numpy(), ldr.cpu().numpy()
+        for k in range(3):
+            frame(k + 1)
+        frames = 200
+        ms = timed_on(stream, lambda: [frame(k + 4) for k in range(frames)], 1) / frames
+    out = {"workload": "Cornell box, 34 triangles, 256x256 x 16 spp, depth 8, RR from depth 3, reference "
+                       "estimator, seed 0, ACES", "frames": frames,
+           "ms_per_frame": ms, "samples_per_s": w * h * spp / (ms / 1e3)}
+    # host buffers through the C ABI: the accumulation buffer in and out, the LDR frame out
+    host = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory()
+    hl = torch.empty_like(host).pin_memory()
+    reps = 50
+    t0 = time.perf_counter()
+    for k in range(reps):
+        host.zero_()
+        N.check(lib.vr_render(acc.handle, C.byref(cst), spp, host.data_ptr(), w, h, 0, k * spp))
+        N.check(lib.vr_tonemap(host.data_ptr(), hl.data_ptr(), w, h, C.byref(cm), 1.0))
+    e2e_s = (time.perf_counter() - t0) / reps
+    out["e2e"] = {"samples_per_s": w * h * spp / e2e_s, "ms_per_frame": e2e_s * 1e3,
+                  "call": "vr_render + vr_tonemap (host buffers, pinned)"}
+    acc.destroy()
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        pyoracle.build()
+        osc = pyoracle.OracleScene(scene)
+        t0 = time.perf_counter()
+        o_hdr, rays = osc.render(st, spp, w, h, seed=0)
+        dt = time.perf_counter() - t0
+        o_ldr = pyoracle.tonemap(o_hdr, int(Tonemap.ACES), 2.2, 0.0, 1.0)
+        out["cpu_baseline"] = {"samples_per_s": w * h * spp / dt, "ms_per_frame": dt * 1e3,
+                               "cores": pyoracle.max_threads(), "kind": "port",
+                               "sample": f"the whole frame, {int(rays[0])} rays"}
+        d = o_hdr[..., :3].astype(np.float64) - g_hdr[..., :3]
+        # the integrator's arithmetic is reproduced operation for operation
+        # (bit-equal pixels); the tonemap's pow/exp are the device's and the
+        # host's own functions, so the LDR frames agree to a few ulp
+        out["parity"] = {"pixels_bit_equal": float(np.mean(np.all(g_hdr == o_hdr, axis=-1))),
+                         "relmse": float(np.mean(d * d / (o_hdr[..., :3].astype(np.float64) ** 2 + 1e-2))),
+                         "ldr_max_abs_diff": float(np.max(np.abs(g_ldr[..., :3].astype(np.float64) - o_ldr[..., :3])))}
+    return out
+
+
 def batch_benchmark(args):
     """The batched workload: 64 displaced-icosphere scenes (10k-2M triangles,
     log-uniform; materials per 64-triangle patch; one shared 2048x1024 sky +
@@ -403,7 +483,7 @@ def serving_references(pool, w, h, spp=4096):
 
 
 def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_passes, warm_jobs, max_samples,
-                dn_first_pass=96, only=None, dn_overshoot=1.2):
+                dn_first_pass=96, only=None, dn_overshoot=1.2, max_inflight=3):
     """One Poisson request stream (seeded) served by every mode:
     plain_<n>: the plain single-scene GPU path, one job at a time, n spp per
     pass (plain_adaptive: one job at a time with predictive pass sizes, the
@@ -440,7 +520,7 @@ def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_pass
                                                      min_samples=64), False))
     modes.append(("served", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True, pipelined=True,
                                          pass_paths=1 << 24, first_pass_spp=64, min_samples=64, overshoot=1.15,
-                                         max_inflight=3), False))
+                                         max_inflight=max_inflight), False))
     # the denoised path starts with a larger first pass: its blend estimate
     # needs a less noisy input (a smaller first pass makes the prediction
     # noisier and more conservative: 32 spp first passes ended at 134 spp per
@@ -448,11 +528,12 @@ def serving_run(pool, refs, net, w, h, n_jobs, rate, target, streams, plain_pass
     modes.append(("served_denoised", ServerConfig(memory_budget=150 * 10**9, max_active=64, adaptive=True,
                                                   pipelined=True, pass_paths=1 << 24, first_pass_spp=dn_first_pass,
                                                   min_samples=min(64, dn_first_pass), overshoot=dn_overshoot,
-                                                  max_inflight=3), True))
+                                                  max_inflight=max_inflight), True))
     if only is not None:
         modes = [m for m in modes if m[0] in only]
     out["served_config"] = {"adaptive": True, "pipelined": True, "pass_paths": 1 << 24, "max_active": 64,
-                            "max_inflight": 3, "render_streams": streams,
+                            "max_inflight": max_inflight, "fill_paths": ServerConfig.fill_paths,
+                            "render_streams": streams,
                             "first_pass_spp": {"served": 64, "served_denoised": dn_first_pass},
                             "overshoot": {"served": 1.15, "served_denoised": dn_overshoot}}
     for name, cfg, dn in modes:
@@ -808,6 +889,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_isect:
         isect = intersection_benchmark(args, hbm_peak, "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                                        else "fallback")
+    cornell = None
+    if rank == 0 and world == 1 and not args.no_cornell:
+        cornell = cornell_benchmark(args)
     batched = None
     if rank == 0 and world == 1 and not args.no_batch:
         batched = batch_benchmark(args)
@@ -841,7 +925,7 @@ def main():
             "mrays_per_s": (ext_rays + shd_rays) / (ms / 1e3) / 1e6,
             "rays": {"extend": int(ext_rays), "shadow": int(shd_rays)},
             "stages": stage, "gpu_launches": gpu_launches, "clocks": clk, "e2e": e2e, "roofline": roofline,
-            "cpu_baseline": cpu, "image_finite": finite, "intersection": isect, "batched": batched, "serving": serve, "denoiser": dnb,
+            "cpu_baseline": cpu, "image_finite": finite, "intersection": isect, "cornell": cornell, "batched": batched, "serving": serve, "denoiser": dnb,
         }
         print(json.dumps(line), flush=True)
     acc.destroy()

@@ -286,6 +286,39 @@ def test_pipelined_renders_while_estimates_are_in_flight():
     assert all(s.status(i).state == "done" for i in ids)
 
 
+class DepthBackend(LaggingBackend):
+    """Records how many passes had estimates outstanding when each pass was issued."""
+
+    def __init__(self, server_ref, **kw):
+        super().__init__(**kw)
+        self.server_ref = server_ref
+        self.depths = []
+
+    def render_async(self, work):
+        self.depths.append(len(self.server_ref[0].pending))
+        return super().render_async(work)
+
+
+@pytest.mark.parametrize("fill_paths, deep", [(0, True), (1, False)])
+def test_gpu_filling_passes_wait_for_their_estimates(fill_paths, deep):
+    """A pass of at least fill_paths paths is not followed by another pass
+    until its estimates are back; smaller passes still pipeline."""
+    ref = [None]
+    be = DepthBackend(ref, lag=3, noise=0.3)
+    cfg = ServerConfig(adaptive=True, pipelined=True, pass_paths=4 * 64 * 64, first_pass_spp=64, min_samples=64,
+                       max_active=64, max_inflight=3, fill_paths=fill_paths)
+    s = Server(be, cfg, clock=Clock())
+    ref[0] = s
+    ids = [s.submit(req(seed=60 + k, target=1e-3, max_samples=100000)) for k in range(6)]
+    while not s.idle():
+        s.step()
+    assert all(s.status(i).state == "done" for i in ids)
+    # fill_paths=1: every pass fills the GPU, so none is issued behind another
+    assert (max(be.depths) > 1) == deep
+    if not deep:
+        assert max(be.depths) == 0
+
+
 def test_blend_samples_needed_is_consistent():
     """The planned sample count brings the predicted error to the target:
     scaling the noise moments by n / n' at the returned n' lands on it."""

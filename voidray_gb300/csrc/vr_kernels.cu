@@ -144,9 +144,9 @@ __global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n, uin
 }
 
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_intersect(BatchIo io, uint32_t n, uint32_t* counter,
+__global__ void __launch_bounds__(128, VR_ISECT_MINB) k_intersect(BatchIo io, uint32_t n, uint32_t* counter,
                                                                   uint32_t* status, unsigned long long* work) {
-    persistent_trace<ANY, COUNT>(n, counter, io, status, work);
+    persistent_trace<ANY, COUNT, BatchIo, true>(n, counter, io, status, work);
 }
 
 // ----------------------------------------------------------------------------
@@ -1064,7 +1064,7 @@ struct ShadowIo {
 };
 
 template <bool COUNT, bool ONE>
-__global__ void __launch_bounds__(128, VR_TRACE_MINB) k_shadow(Wave w, PathState ps, uint32_t k, uint32_t* status,
+__global__ void __launch_bounds__(128, VR_SHADOW_MINB) k_shadow(Wave w, PathState ps, uint32_t k, uint32_t* status,
                                                                unsigned long long* work) {
     __shared__ uint32_t pre[MAX_JOBS + 1];
     uint32_t n;

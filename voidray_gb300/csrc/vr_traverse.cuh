@@ -19,7 +19,9 @@
 // stores their results and refills them from the queue.  Of a node's hit
 // children the nearest is visited next and the others are pushed with their
 // entry distances, farthest first; popped entries beyond the current closest
-// hit are skipped.
+// hit are skipped.  Any-hit traversal pushes node indices alone and keeps no
+// order among a node's hit children (shadow rays), or only visits the nearest
+// first (queries of the batch intersection API).
 #pragma once
 #include "vr_device.cuh"
 
@@ -32,6 +34,12 @@ struct HitOut {
 
 #ifndef VR_TRACE_MINB
 #define VR_TRACE_MINB 9  // minimum resident blocks per SM requested from ptxas (55 registers, no spills)
+#endif
+#ifndef VR_SHADOW_MINB
+#define VR_SHADOW_MINB VR_TRACE_MINB  // the same for the any-hit shadow kernel
+#endif
+#ifndef VR_ISECT_MINB
+#define VR_ISECT_MINB VR_TRACE_MINB  // the same for the batch intersection kernel
 #endif
 #ifndef VR_DYN_FETCH
 #define VR_DYN_FETCH 16  // refill a warp's lanes once at least this many have finished
@@ -101,15 +109,18 @@ __device__ __forceinline__ void add_work(unsigned long long* work, uint32_t nv, 
 // store(i, hit, overflow).  `counter` is the queue's fetch cursor (zero
 // before the launch).  Every lane of the block's warps must call this
 // (warp-uniform control flow at the votes).
-template <bool ANY, bool COUNT, class Io>
+template <bool ANY, bool COUNT, class Io, bool NEAREST_ANY = false>
 __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, const Io& io, uint32_t* status,
                                                  unsigned long long* work) {
     const uint32_t lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const float4* nodes = nullptr;  // BVH of the current ray's scene
     const float4* tris = nullptr;
-    int stack_node[STACK_SIZE];
-    float stack_t[STACK_SIZE];
+    // closest hit: (node, entry distance) pairs, one 64-bit access each;
+    // any hit: node indices alone (every pushed child lies within the ray's
+    // fixed [tmin, tmax], so no entry is ever culled)
+    int2 stack[ANY ? 1 : STACK_SIZE];
+    int stack_node[ANY ? STACK_SIZE : 1];
     V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
     float ix = 0.0f, iy = 0.0f, iz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f, tmin = 0.0f, best = 0.0f;
     int node = SENTINEL, leaf = 0, sp = 0;
@@ -118,12 +129,14 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, 
     bool has = false, alive = true, overflow = false;
 
     auto pop = [&]() -> int {
+        if (ANY) return sp > 0 ? stack_node[--sp] : SENTINEL;
         while (sp > 0) {
-            --sp;
-            if (stack_t[sp] <= best) return stack_node[sp];
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= best) return e.x;
         }
         return SENTINEL;
     };
+    auto push = [&](int k, float t) { stack[sp++] = make_int2(k, __float_as_int(t)); };
 
     while (true) {
         // finished lanes store their result
@@ -210,6 +223,55 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, 
                 }
                 int k0 = cd.x, k1 = cd.y, k2 = cd.z, k3 = cd.w;
                 const int nh = (t0 < INF_F) + (t1 < INF_F) + (t2 < INF_F) + (t3 < INF_F);
+                if (ANY) {
+                    // any hit: visit one hit child and push the others, in
+                    // no particular order (NEAREST_ANY: the nearest first,
+                    // by an argmin rather than a sort)
+                    if (nh == 0) {
+                        node = pop();
+                    } else if (sp + nh - 1 > STACK_SIZE) {
+                        overflow = true;
+                        node = SENTINEL;
+                        leaf = 0;
+                        break;
+                    } else {
+                        if (NEAREST_ANY) {
+                            auto lower_first = [](float& ta, int& ka, float& tb, int& kb) {
+                                if (tb < ta) {
+                                    const float tt = ta;
+                                    const int kk = ka;
+                                    ta = tb;
+                                    ka = kb;
+                                    tb = tt;
+                                    kb = kk;
+                                }
+                            };
+                            lower_first(t0, k0, t1, k1);
+                            lower_first(t2, k2, t3, k3);
+                            lower_first(t0, k0, t2, k2);
+                        }
+                        node = SENTINEL;
+                        if (t3 < INF_F) node = k3;
+                        if (t2 < INF_F) {
+                            if (node != SENTINEL) stack_node[sp++] = node;
+                            node = k2;
+                        }
+                        if (t1 < INF_F) {
+                            if (node != SENTINEL) stack_node[sp++] = node;
+                            node = k1;
+                        }
+                        if (t0 < INF_F) {
+                            if (node != SENTINEL) stack_node[sp++] = node;
+                            node = k0;
+                        }
+                    }
+                    if (node < 0 && leaf >= 0) {
+                        leaf = node;
+                        node = pop();
+                    }
+                    if (!__any_sync(__activemask(), leaf >= 0)) break;
+                    continue;
+                }
                 // sort by entry distance (misses, at infinity, end up last)
                 auto cswap = [](float& ta, int& ka, float& tb, int& kb) {
                     const bool sw = tb < ta;
@@ -234,21 +296,9 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* counter, 
                         leaf = 0;
                         break;
                     }
-                    if (nh > 3) {
-                        stack_node[sp] = k3;
-                        stack_t[sp] = t3;
-                        ++sp;
-                    }
-                    if (nh > 2) {
-                        stack_node[sp] = k2;
-                        stack_t[sp] = t2;
-                        ++sp;
-                    }
-                    if (nh > 1) {
-                        stack_node[sp] = k1;
-                        stack_t[sp] = t1;
-                        ++sp;
-                    }
+                    if (nh > 3) push(k3, t3);
+                    if (nh > 2) push(k2, t2);
+                    if (nh > 1) push(k1, t1);
                     node = k0;
                 }
                 // postpone the first leaf reached

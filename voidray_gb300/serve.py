@@ -129,6 +129,11 @@ class ServerConfig:
     # renders the jobs whose next pass size is already known
     pipelined: bool = False
     max_inflight: int = 2      # pipelined: passes whose estimates may be outstanding
+    # pipelined: after a pass of at least this many paths (one that fills the
+    # GPU by itself) the next pass waits for its estimates: issuing later
+    # jobs' passes behind it would add their time to its jobs' latency and
+    # gain no fill (0 = off)
+    fill_paths: int = 1 << 26
     # adaptive: order in which jobs take a pass: "fifo" (admission order) or
     # "srpt" (shortest predicted remaining work first: paths the job still
     # needs by its last estimate; jobs before their first estimate count
@@ -633,6 +638,7 @@ class Server:
         self.used = 0
         self.passes = 0
         self.pending: list = []   # pipelined: (estimate handle, jobs) in issue order
+        self.last_pass_paths = 0
 
     # -- requests --------------------------------------------------------
     def submit(self, req: JobRequest, arrival: Optional[float] = None, resume: Optional[str] = None) -> int:
@@ -800,7 +806,10 @@ class Server:
         self._harvest(block=False)
         # a bounded number of passes in flight: a deeper queue would put later
         # jobs' passes ahead of the next pass of the jobs waiting for estimates
-        while len(self.pending) >= self.cfg.max_inflight:
+        limit = self.cfg.max_inflight
+        if self.cfg.fill_paths and self.last_pass_paths >= self.cfg.fill_paths:
+            limit = 1
+        while len(self.pending) >= limit:
             self._harvest(block=True)
             self._admit()
         while True:
@@ -820,6 +829,7 @@ class Server:
                 self.active.remove(job.job_id)
             return 0
         self.passes += 1
+        self.last_pass_paths = sum(n * job.req.width * job.req.height for job, _, _, n in work)
         rendered = {}
         for job, b, first, n in work:
             job.samples += n
