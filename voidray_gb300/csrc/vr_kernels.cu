@@ -161,6 +161,14 @@ __device__ __forceinline__ size_t sat_usize(float x) {
 __device__ __forceinline__ V3 env_px(const float* img, size_t i) {
     return v3(__ldg(img + 3 * i), __ldg(img + 3 * i + 1), __ldg(img + 3 * i + 2));
 }
+// i % len for i <= 2 len: the linear index of a bilinear neighbour of a texel
+// (x0 < W, y0 < H) wraps at most twice, so two conditional subtractions give
+// the reference's modulo without a 64-bit division.
+__device__ __forceinline__ size_t wrap_index(size_t i, size_t len) {
+    if (i >= len) i -= len;
+    if (i >= len) i -= len;
+    return i;
+}
 __device__ V3 env_eval(const SceneView& s, V3 dir) {
     if (s.env_kind == 1) return load3(s.env_color);
     if (s.env_kind != 2) return v3(0.0f, 0.0f, 0.0f);
@@ -177,8 +185,9 @@ __device__ V3 env_eval(const SceneView& s, V3 dir) {
     float ax = x - (float)x0;
     float ay = y - (float)y0;
     const float* img = s.env_img;
-    return lerp3(lerp3(env_px(img, (y0 * W + x0) % len), env_px(img, (y0 * W + x0 + 1) % len), ax),
-                 lerp3(env_px(img, ((y0 + 1) * W + x0) % len), env_px(img, ((y0 + 1) * W + x0 + 1) % len), ax), ay);
+    const size_t i0 = y0 * W + x0;  // < len
+    return lerp3(lerp3(env_px(img, i0), env_px(img, wrap_index(i0 + 1, len)), ax),
+                 lerp3(env_px(img, wrap_index(i0 + W, len)), env_px(img, wrap_index(i0 + W + 1, len)), ax), ay);
 }
 // Largest i < n with cdf[i] <= u (cdf[0] = 0 <= u): a binary search of the
 // non-decreasing CDF, started from the guide table's bracket.  u in [0, 1)
@@ -257,11 +266,11 @@ __device__ V3 tex_sample(const SceneView& s, int32_t tix, float u, float v) {
     const float x = fmodf(u, 1.0f) * (float)W;
     const float y = (1.0f - fmodf(v, 1.0f)) * (float)H;
     const size_t x0 = min(sat_usize(x), W - 1), y0 = min(sat_usize(y), H - 1);
-    if (ti.w == 0) return env_px(img, (y0 * W + x0) % len);
+    const size_t i0 = y0 * W + x0;  // < len
+    if (ti.w == 0) return env_px(img, i0);
     const float ax = x - (float)x0, ay = y - (float)y0;
-    return lerp3(lerp3(env_px(img, (y0 * W + x0) % len), env_px(img, (y0 * W + x0 + 1) % len), ax),
-                 lerp3(env_px(img, ((y0 + 1) * W + x0) % len), env_px(img, ((y0 + 1) * W + x0 + 1) % len), ax),
-                 ay);
+    return lerp3(lerp3(env_px(img, i0), env_px(img, wrap_index(i0 + 1, len)), ax),
+                 lerp3(env_px(img, wrap_index(i0 + W, len)), env_px(img, wrap_index(i0 + W + 1, len)), ax), ay);
 }
 
 // MixMaterial::scatter (legacy voidray/src/common/materials.rs:195-203): one
